@@ -1,0 +1,345 @@
+"""Benchmark: tomograms/s of the hologram -> RI path on one GB300 (or N replicas).
+
+Workloads (seeded synthetic data with the shapes of the benchmark configurations;
+see ctdm_gb300.phantom):
+  plain_small  49 x 256^2 holograms -> 256^3, DCT unwrap, 10 positivity iterations
+  wrap_heavy   121 x 1024^2 holograms -> 256^2 windows -> 256^3, DCT + Goldstein, 20 iterations
+
+`value`  tomograms/s with holograms resident in HBM (CUDA events per step, L2
+         flushed between steps by writing a 256 MiB buffer outside the timed region).
+`e2e`    the same through ctdm_reconstruct (C ABI) with pinned host buffers: the
+         H2D copy of the holograms and the D2H copy of the RI volume are inside
+         the timed region.
+`--impl reference` times the FP64 CPU implementation of the path on the host
+cores (the reference's path is CUDA; its CPU restatement is the oracle).
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CONFIGS = {
+    "plain_small": dict(iterations=10, goldstein=False),
+    "wrap_heavy": dict(iterations=20, goldstein=True),
+}
+
+
+def make_workload(name, seed):
+    from ctdm_gb300 import phantom
+    if name == "plain_small":
+        return phantom.config_plain_small(seed=seed)
+    if name == "wrap_heavy":
+        return phantom.config_wrap_heavy(seed=seed)
+    raise ValueError(name)
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except FileNotFoundError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm = [float(r[1]) for r in self.rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) >= 9 and r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            if len(r) < 9:
+                continue
+            for k, nm in enumerate(names):
+                if r[5 + k].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel, workload):
+    """Per-launch DRAM bytes from the committed ncu summary, if one exists."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None
+    d = json.load(open(p))
+    return d.get(workload, {}).get(kernel)
+
+
+# ---------------------------------------------------------------- CPU baseline (oracle)
+def cpu_sample(acq, iters, threads=None):
+    """FP64 oracle on a bounded sample of one tomogram: the per-angle front end on
+    two angles and the positivity loop with 0 and 1 iterations at full volume size;
+    extrapolated to the whole tomogram.  Returns (seconds per tomogram, threads, text)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    if threads:
+        O.set_threads(threads)
+    nthr = O.get_threads()
+    A = len(acq.ang_x)
+    s = 2
+    par = O.make_params(acq.n_holo, acq.m_crop, acq.r_vol, 0, acq.fm0, acq.df, acq.dx, acq.k2, acq.n_med)
+    t0 = time.perf_counter()
+    ph, am, _ = O.front_end(par, acq.holograms[:s], acq.background)
+    t_front = (time.perf_counter() - t0) / s
+    t0 = time.perf_counter()
+    U = np.stack([O.rytov_spectrum(ph[a], am[a]) for a in range(s)])
+    t_spec = (time.perf_counter() - t0) / s
+    t0 = time.perf_counter()
+    F2, C = O.ewald_map(U, acq.ang_x[:s], acq.ang_y[:s], acq.fm0, acq.df, acq.dx)
+    t_map = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    O.positivity(F2, C, 0, acq.k2, acq.n_med)
+    t_p0 = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    O.positivity(F2, C, 1, acq.k2, acq.n_med)
+    t_p1 = time.perf_counter() - t0
+    t_iter = max(t_p1 - t_p0, 0.0)
+    total = A * (t_front + t_spec) + t_map + t_p0 + iters * t_iter
+    text = (f"oracle on {s} of {A} angles + positivity loop with 0 and 1 iterations at {acq.r_vol}^3, "
+            f"extrapolated: {A}x{t_front + t_spec:.3f}s/angle + {t_map + t_p0:.2f}s + {iters}x{t_iter:.2f}s/iter")
+    return total, nthr, text
+
+
+# ---------------------------------------------------------------- GPU arm
+def run_ours(args):
+    import torch
+    import ctdm_gb300 as C
+    from ctdm_gb300 import build
+
+    rank, world, local = dist_info()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    build.build()
+    cfg = CONFIGS[args.config]
+    acq = make_workload(args.config, seed=1000 + rank)
+    A = len(acq.ang_x)
+    p = C.params_for(acq, cfg["iterations"], run_goldstein=int(cfg["goldstein"]))
+    ctx = C.Context(local)
+    holo = torch.from_numpy(acq.holograms).to(dev)
+    bg = torch.from_numpy(acq.background).to(dev)
+    r = acq.r_vol
+    out = torch.empty((r, r, r), dtype=torch.complex64, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        ctx.reconstruct_device(p, holo, bg, acq.ang_x, acq.ang_y, out, stream=stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    barrier()
+    launches0 = C.launch_count()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for k in range(args.steps):
+        flush.zero_()
+        ev[k][0].record(stream)
+        step()
+        ev[k][1].record(stream)
+    barrier()
+    launches = C.launch_count() - launches0
+    dev_ms = sum(a.elapsed_time(b) for a, b in ev)
+    # e2e: host buffers through the C ABI (pinned), copies inside the timed region
+    h_holo = torch.from_numpy(acq.holograms).pin_memory()
+    h_bg = torch.from_numpy(acq.background).pin_memory()
+    h_out = torch.empty((r, r, r), dtype=torch.complex64).pin_memory()
+    lib = C.load()
+    ax, ay = np.ascontiguousarray(acq.ang_x, np.float32), np.ascontiguousarray(acq.ang_y, np.float32)
+
+    def e2e_step():
+        C.check(lib.ctdm_reconstruct(ctx.handle, ctypes.byref(p), A, h_holo.data_ptr(), h_bg.data_ptr(),
+                                     ax.ctypes.data, ay.ctypes.data, h_out.data_ptr()), "ctdm_reconstruct")
+
+    e2e_step()
+    torch.cuda.synchronize()
+    barrier()
+    e2e_ms = 0.0
+    for k in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(torch.cuda.default_stream(dev))
+        e2e_step()
+        b.record(torch.cuda.default_stream(dev))
+        b.synchronize()
+        e2e_ms += a.elapsed_time(b)
+    barrier()
+    clocks = sampler.stop()
+
+    # per-stage timing (separate untimed run with events at stage boundaries)
+    ctx.set_timing(True)
+    flush.zero_()
+    step()
+    torch.cuda.synchronize()
+    stages = ctx.stage_times()
+    ctx.set_timing(False)
+
+    if world > 1:
+        t = torch.tensor([dev_ms, e2e_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        dev_ms, e2e_ms = float(t[0]), float(t[1])
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+
+    r3 = float(r) ** 3
+    bytes_per = {"x_pass": 16 * r3, "y_forward": 16 * r3, "y_inverse": 16 * r3, "z_pass": 24 * r3,
+                 "ewald": A * 8.0 * r * r + 16 * r3}
+    best = max(bytes_per, key=lambda k: stages[k][0])
+    ms_total, cnt = stages[best]
+    avg_ms = ms_total / max(cnt, 1)
+    achieved = bytes_per[best] / (avg_ms * 1e-3) / 1e9
+    peak, peak_kind = measured_peaks()
+    traffic = ncu_traffic(best, args.config)
+    cpu_s, cores, text = cpu_sample(acq, cfg["iterations"])
+    tomos = world * args.steps
+    line = {
+        "metric": "tomograms/s (hologram->RI)",
+        "value": tomos / (dev_ms / 1e3),
+        "unit": "tomograms/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": dev_ms / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32/c64",
+        "data": "synthetic (seeded Rytov phantom, Poisson noise)",
+        "config": {"workload": args.config, "holograms": f"{A}x{acq.n_holo}^2", "window": acq.m_crop,
+                   "volume": f"{r}^3", "iterations": cfg["iterations"], "goldstein": cfg["goldstein"],
+                   "parallelism": f"replicas{world}", "l2": "flushed between steps (256 MiB write)"},
+        "e2e": {"value": tomos / (e2e_ms / 1e3), "unit": "tomograms/s",
+                "h2d_bytes_per_step": int(acq.holograms.nbytes + acq.background.nbytes),
+                "d2h_bytes_per_step": int(r3 * 8)},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": best, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+                     "bytes_per_launch": bytes_per[best], "avg_launch_ms": avg_ms},
+        "stages_ms": {k: round(v[0], 4) for k, v in stages.items()},
+        "clocks": clocks,
+        "cpu_baseline": {"value": 1.0 / cpu_s, "unit": "tomograms/s", "cores": cores, "kind": "port",
+                         "sample": text},
+    }
+    print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_reference(args):
+    rank, world, local = dist_info()
+    if rank != 0:
+        return
+    cfg = CONFIGS[args.config]
+    acq = make_workload(args.config, seed=1000)
+    times = []
+    for k in range(args.warmup + args.steps):
+        s, cores, text = cpu_sample(acq, cfg["iterations"])
+        if k >= args.warmup:
+            times.append(s)
+    per = sum(times) / len(times)
+    value = 1.0 / per
+    line = {
+        "impl": "reference",
+        "metric": "tomograms/s (hologram->RI)",
+        "value": value,
+        "unit": "tomograms/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": per * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded Rytov phantom, Poisson noise)",
+        "config": {"workload": args.config, "holograms": f"{len(acq.ang_x)}x{acq.n_holo}^2",
+                   "volume": f"{acq.r_vol}^3", "iterations": cfg["iterations"]},
+        "cpu_baseline": {"value": value, "unit": "tomograms/s", "cores": cores, "kind": "port", "sample": text},
+        "e2e": {"value": value, "unit": "tomograms/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="plain_small", choices=sorted(CONFIGS))
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

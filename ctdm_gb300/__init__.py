@@ -1,0 +1,176 @@
+"""GB300-native cTDM hologram -> refractive-index reconstruction.
+
+Python host side over the C ABI of libctdm_gb300.so (include/ctdm.h).  Device
+memory is passed as raw pointers; torch CUDA tensors are accepted for
+convenience (torch is used for allocation and streams only).  Nothing here runs
+on the CPU: every call launches the library's CUDA kernels and fails loudly when
+the library is missing.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import CtdmError, Params, check, load  # noqa: F401
+
+CTDM_UNWRAP_REF, CTDM_UNWRAP_EXACT = 0, 1
+CTDM_CHECK_REF, CTDM_CHECK_MASK = 0, 1
+CTDM_METHOD_DCT, CTDM_METHOD_FAST, CTDM_METHOD_GOLDSTEIN = 0, 1, 2
+
+
+def _ptr(x):
+    """Device (or host) address of a torch tensor, numpy array or int."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        return x.data_ptr()
+    if isinstance(x, np.ndarray):
+        return x.ctypes.data
+    raise TypeError(f"cannot take the address of {type(x)}")
+
+
+def _stream(stream):
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream
+
+
+def default_params(**kw):
+    p = Params()
+    load().ctdm_params_default(ctypes.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def params_for(acq, iterations, **kw):
+    """Parameters matching a ctdm_gb300.phantom.Acquisition."""
+    return default_params(n_holo=acq.n_holo, m_crop=acq.m_crop, r_vol=acq.r_vol, iterations=iterations,
+                          n_med=acq.n_med, wavelength=acq.wavelength, dx=acq.dx, **kw)
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+class Context:
+    """A device context (ctdm_ctx): workspace, tables and the last carrier."""
+
+    def __init__(self, device=0):
+        self.lib = load()
+        h = ctypes.c_void_p()
+        check(self.lib.ctdm_ctx_create(int(device), ctypes.byref(h)), "ctdm_ctx_create")
+        self.handle = h
+        self.device = device
+
+    def close(self):
+        if self.handle:
+            self.lib.ctdm_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- whole path ----------------------------------------------------------
+    def reconstruct_device(self, params, holo, bg, angx, angy, out, stream=None):
+        angx, angy = _f32(angx), _f32(angy)
+        check(self.lib.ctdm_reconstruct_device(self.handle, ctypes.byref(params), len(angx), _ptr(holo), _ptr(bg),
+                                               _ptr(angx), _ptr(angy), _ptr(out), _stream(stream)),
+              "ctdm_reconstruct_device")
+
+    def reconstruct(self, params, holo, bg, angx, angy, out=None):
+        """Host arrays in, host RI volume (R, R, R) complex64 out."""
+        holo, bg, angx, angy = _f32(holo), _f32(bg), _f32(angx), _f32(angy)
+        r = params.r_vol
+        if out is None:
+            out = np.empty((r, r, r), np.complex64)
+        check(self.lib.ctdm_reconstruct(self.handle, ctypes.byref(params), len(angx), _ptr(holo), _ptr(bg),
+                                        _ptr(angx), _ptr(angy), _ptr(out)), "ctdm_reconstruct")
+        return out
+
+    def carrier(self):
+        c = (ctypes.c_int * 3)()
+        check(self.lib.ctdm_ctx_carrier(self.handle, c), "ctdm_ctx_carrier")
+        return tuple(c)
+
+    STAGES = ("qpi", "unwrap", "goldstein", "spectra", "ewald", "y_inverse", "x_pass", "y_forward", "z_pass",
+              "x_final")
+
+    def set_timing(self, on=True):
+        check(self.lib.ctdm_ctx_set_timing(self.handle, int(on)), "ctdm_ctx_set_timing")
+
+    def stage_times(self):
+        """{stage: (ms, launches)} of the last timed pipeline call."""
+        n = len(self.STAGES)
+        ms = (ctypes.c_double * n)()
+        cnt = (ctypes.c_int * n)()
+        check(self.lib.ctdm_ctx_stage_times(self.handle, ms, cnt, n), "ctdm_ctx_stage_times")
+        return {name: (ms[i], cnt[i]) for i, name in enumerate(self.STAGES)}
+
+    def buffer(self, which):
+        p, n = ctypes.c_void_p(), ctypes.c_size_t()
+        check(self.lib.ctdm_ctx_buffer(self.handle, int(which), ctypes.byref(p), ctypes.byref(n)), "ctdm_ctx_buffer")
+        return p.value, n.value
+
+    # -- stages (device pointers) ----------------------------------------------
+    def qpi(self, n, m, holo, bg, phase, amp, n_angles, bg_per_angle=False, carrier=(-1, -1, -1), stream=None):
+        c = (ctypes.c_int * 3)(*carrier)
+        check(self.lib.ctdm_qpi(self.handle, n, m, n_angles, _ptr(holo), _ptr(bg), int(bg_per_angle), c, _ptr(phase),
+                                _ptr(amp), _stream(stream)), "ctdm_qpi")
+        return tuple(c)
+
+    def unwrap_dct(self, phi, out, n_maps, m, mode=CTDM_UNWRAP_REF, stream=None):
+        check(self.lib.ctdm_unwrap_dct(self.handle, n_maps, m, mode, _ptr(phi), _ptr(out), _stream(stream)),
+              "ctdm_unwrap_dct")
+
+    def unwrap_fast(self, phi, out, n_maps, m, stream=None):
+        check(self.lib.ctdm_unwrap_fast(self.handle, n_maps, m, _ptr(phi), _ptr(out), _stream(stream)),
+              "ctdm_unwrap_fast")
+
+    def goldstein(self, phi, charges, cuts, out, n_maps, w, h, stream=None):
+        st = (ctypes.c_int * n_maps)()
+        rc = self.lib.ctdm_goldstein(self.handle, n_maps, w, h, _ptr(phi), _ptr(charges), _ptr(cuts), _ptr(out), st,
+                                     _stream(stream))
+        if rc not in (0, 5):
+            check(rc, "ctdm_goldstein")
+        return list(st)
+
+    def prepare_spectra(self, phase, amp, U, n_angles, m, n, r, stream=None):
+        check(self.lib.ctdm_prepare_spectra(self.handle, n_angles, m, n, r, _ptr(phase), _ptr(amp), _ptr(U),
+                                            _stream(stream)), "ctdm_prepare_spectra")
+
+    def stack_spectra(self, ph, am, U, n_angles, r, stream=None):
+        check(self.lib.ctdm_stack_spectra(self.handle, n_angles, r, _ptr(ph), _ptr(am), _ptr(U), _stream(stream)),
+              "ctdm_stack_spectra")
+
+    def prepare_stack(self, phase, amp, ph_out, am_out, n_angles, m, n, r, stream=None):
+        check(self.lib.ctdm_prepare_stack(self.handle, n_angles, m, n, r, _ptr(phase), _ptr(amp), _ptr(ph_out),
+                                          _ptr(am_out), _stream(stream)), "ctdm_prepare_stack")
+
+    def map_ewald(self, U, angx, angy, fm0, df, dx, F2, counts=None, stream=None):
+        angx, angy = _f32(angx), _f32(angy)
+        r = int(round(np.sqrt(U.numel() // len(angx)))) if hasattr(U, "numel") else U.shape[-1]
+        check(self.lib.ctdm_map_ewald(self.handle, len(angx), r, _ptr(U), _ptr(angx), _ptr(angy), fm0, df, dx,
+                                      _ptr(F2), _ptr(counts), _stream(stream)), "ctdm_map_ewald")
+
+    def positivity(self, F2, r, iterations, k2, n_med, out, check_mode=CTDM_CHECK_REF, counts=None, stream=None):
+        check(self.lib.ctdm_positivity(self.handle, r, iterations, check_mode, k2, n_med, _ptr(F2), _ptr(counts),
+                                       _ptr(out), _stream(stream)), "ctdm_positivity")
+
+
+def launch_count():
+    """Kernels launched by the library in this process so far."""
+    return int(load().ctdm_launch_count())
+
+
+def fft(data, dims, batch=1, inverse=False, stream=None):
+    """Unnormalised in-place FFT of a device buffer (dims fastest-first)."""
+    d = (ctypes.c_int * len(dims))(*dims)
+    check(load().ctdm_fft(_ptr(data), len(dims), d, batch, int(inverse), _stream(stream)), "ctdm_fft")

@@ -1,0 +1,106 @@
+"""ctypes binding of libctdm_gb300.so (the C ABI declared in include/ctdm.h).
+
+The library is built in-tree (ctdm_gb300/_build) by ctdm_gb300.build.  Loading
+fails loudly when it is missing: there is no CPU or library fallback.
+"""
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libctdm_gb300.so")
+
+c_int, c_double, c_float, c_void_p, c_size_t = ctypes.c_int, ctypes.c_double, ctypes.c_float, ctypes.c_void_p, ctypes.c_size_t
+P_int = ctypes.POINTER(ctypes.c_int)
+
+
+class Params(ctypes.Structure):
+    """ctdm_params (include/ctdm.h)."""
+    _fields_ = [
+        ("n_holo", c_int), ("m_crop", c_int), ("r_vol", c_int), ("iterations", c_int),
+        ("unwrap_mode", c_int), ("check_mode", c_int), ("unwrap_method", c_int), ("run_goldstein", c_int),
+        ("bg_per_angle", c_int), ("carrier_r", c_int), ("carrier_c", c_int), ("carrier_radius", c_int),
+        ("n_med", c_double), ("wavelength", c_double), ("dx", c_double),
+    ]
+
+
+# name -> (restype, argtypes)
+_SIGS = {
+    "ctdm_params_default": (None, [ctypes.POINTER(Params)]),
+    "ctdm_last_error": (ctypes.c_char_p, []),
+    "ctdm_version": (ctypes.c_char_p, []),
+    "ctdm_ctx_create": (c_int, [c_int, ctypes.POINTER(c_void_p)]),
+    "ctdm_ctx_destroy": (None, [c_void_p]),
+    "ctdm_ctx_carrier": (c_int, [c_void_p, P_int]),
+    "ctdm_ctx_buffer": (c_int, [c_void_p, c_int, ctypes.POINTER(c_void_p), ctypes.POINTER(c_size_t)]),
+    "ctdm_ctx_set_timing": (c_int, [c_void_p, c_int]),
+    "ctdm_ctx_stage_times": (c_int, [c_void_p, ctypes.POINTER(c_double), P_int, c_int]),
+    "ctdm_launch_count": (ctypes.c_ulonglong, []),
+    "ctdm_reconstruct_device": (c_int, [c_void_p, ctypes.POINTER(Params), c_int, c_void_p, c_void_p, c_void_p,
+                                        c_void_p, c_void_p, c_void_p]),
+    "ctdm_reconstruct": (c_int, [c_void_p, ctypes.POINTER(Params), c_int, c_void_p, c_void_p, c_void_p, c_void_p,
+                                 c_void_p]),
+    "ctdm_qpi": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_int, P_int, c_void_p, c_void_p,
+                         c_void_p]),
+    "ctdm_unwrap_dct": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p]),
+    "ctdm_unwrap_fast": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p]),
+    "ctdm_goldstein": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, P_int,
+                               c_void_p]),
+    "ctdm_prepare_spectra": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "ctdm_stack_spectra": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "ctdm_prepare_stack": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
+                                   c_void_p]),
+    "ctdm_map_ewald": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_double, c_double, c_double,
+                               c_void_p, c_void_p, c_void_p]),
+    "ctdm_positivity": (c_int, [c_void_p, c_int, c_int, c_int, c_double, c_double, c_void_p, c_void_p, c_void_p,
+                                c_void_p]),
+    "ctdm_fft": (c_int, [c_void_p, c_int, P_int, c_int, c_int, c_void_p]),
+    "ctdm_set_recon_globals": (None, [c_int, c_double, c_double, c_double, c_double, c_int, c_int, ctypes.c_char_p]),
+    "DCT_UWLS_Unwrapped": (None, [c_void_p, c_void_p, c_int, c_int]),
+    "FastUnwrapping": (None, [c_void_p, c_void_p, c_int, c_int]),
+    "cudaGoldsteinUnwrap2D": (None, [c_void_p, c_void_p, c_int, c_int, c_int]),
+    "MedianFilter": (None, [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_int]),
+    "CopyDataArray": (None, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_int]),
+    "EdwardSphere": (None, [c_void_p, c_void_p, c_void_p, c_float, c_float, c_float, c_float, c_int, c_int, c_int]),
+    "initial_F_and_F2": (None, [c_void_p, c_void_p, c_void_p, c_float, c_int, c_int, c_int]),
+    "est_n_3D": (None, [c_void_p, c_void_p, c_float, c_float, c_int, c_int, c_int]),
+    "modify_F_3D": (None, [c_void_p, c_void_p, c_float, c_float, c_int, c_int, c_int]),
+    "check_F_3D": (None, [c_void_p, c_void_p, c_int, c_int, c_int]),
+    "cuFFT3D": (None, [c_void_p, c_int, c_int, c_int, c_int]),
+    "cuFFT2D": (None, [c_void_p, c_int, c_int, c_int]),
+    "BatchRecon": (None, [c_void_p, c_void_p, c_void_p, c_void_p, c_int]),
+}
+
+EXPORTED = tuple(_SIGS)
+_lib = None
+
+
+def load(path=None):
+    """Load the shared library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise RuntimeError(f"libctdm_gb300.so not built ({path}); run ctdm_gb300.build.build()")
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def last_error():
+    return load().ctdm_last_error().decode()
+
+
+class CtdmError(RuntimeError):
+    def __init__(self, status, where):
+        self.status = status
+        super().__init__(f"{where} failed with status {status}: {last_error()}")
+
+
+def check(status, where):
+    if status != 0:
+        raise CtdmError(status, where)

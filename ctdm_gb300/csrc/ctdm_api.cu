@@ -1,0 +1,997 @@
+// Host runtime and C ABI of libctdm_gb300: device tables, contexts, workspace,
+// the fused hologram -> RI pipeline and the reference-named entry points.
+#include <atomic>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "ctdm.h"
+#include "ctdm_common.cuh"
+#include "kernels_front.cuh"
+
+namespace ctdm {
+cudaError_t compat_copy_data_array(float2 *u, const float *ph, const float *am, int W, int H, int numZ,
+                                   cudaStream_t s);
+cudaError_t compat_edward_sphere(const float2 *u, float2 *F, float *C, const AngleGeom &g, double df, double fm02,
+                                 float fm02s, int W, int H, int Z, cudaStream_t s);
+cudaError_t compat_initial_f(const float *C, float2 *F, float2 *F2, float dx, long n, cudaStream_t s);
+cudaError_t compat_est_n(float2 *n, const float2 *F, float k2, float nm, long cnt, cudaStream_t s);
+cudaError_t compat_modify(const float2 *n, float2 *F, float k2, float nm2, long cnt, cudaStream_t s);
+cudaError_t compat_check(float2 *F, const float2 *F2, long cnt, cudaStream_t s);
+cudaError_t counts_to_mask(const uint32_t *c, uint8_t *m, long n, cudaStream_t s);
+cudaError_t median_stack(const float *ph, const float *am, int A, int R, float *ph_out, float *am_out,
+                         cudaStream_t s);
+cudaError_t set_carrier(int *carrier, int r, int c, int rad, cudaStream_t s);
+}  // namespace ctdm
+
+using namespace ctdm;
+
+// ---------------------------------------------------------------- errors
+static thread_local std::string g_err;
+
+static void set_err(const char *fmt, ...)
+{
+    char b[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(b, sizeof b, fmt, ap);
+    va_end(ap);
+    g_err = b;
+}
+
+static ctdm_status cuda_fail(cudaError_t e, const char *what)
+{
+    set_err("%s: %s", what, cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? CTDM_ERR_NOMEM : CTDM_ERR_CUDA;
+}
+
+#define CK(x, what)                                    \
+    do {                                               \
+        cudaError_t e_ = (x);                          \
+        if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+    } while (0)
+
+static ctdm_status invalid(const char *fmt, ...)
+{
+    char b[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(b, sizeof b, fmt, ap);
+    va_end(ap);
+    g_err = b;
+    return CTDM_ERR_INVALID;
+}
+
+extern "C" const char *ctdm_last_error(void) { return g_err.c_str(); }
+
+static std::atomic<unsigned long long> g_launches{0};
+namespace ctdm {
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+}  // namespace ctdm
+extern "C" unsigned long long ctdm_launch_count(void) { return g_launches.load(); }
+extern "C" const char *ctdm_version(void) { return "ctdm_gb300 0.1 (sm_103a)"; }
+
+// ---------------------------------------------------------------- device tables
+static const int kLengths[] = {16, 32, 64, 128, 256, 384, 512, 768, 1024, 1536, 2048};
+static const int kCrops[] = {16, 32, 64, 128, 256, 384, 512, 768};
+static const int kVolumes[] = {32, 64, 128, 256, 384, 512, 768};
+
+static bool in_set(int v, const int *s, int n)
+{
+    for (int i = 0; i < n; i++)
+        if (s[i] == v) return true;
+    return false;
+}
+static bool ok_length(int L) { return in_set(L, kLengths, 11); }
+static bool ok_crop(int M) { return in_set(M, kCrops, 8); }
+static bool ok_volume(int R) { return in_set(R, kVolumes, 7); }
+
+struct DevTables {
+    std::map<int, float2 *> tw, dtw;
+    std::map<int, float *> eig;
+    bool complete = false;
+};
+static std::mutex g_tab_mu;
+static std::map<int, DevTables> g_tables;
+
+static cudaError_t build_tables(int dev, DevTables &t)
+{
+    for (int L : kLengths) {
+        std::vector<float2> h(L);
+        for (int e = 0; e < L; e++) {
+            const double a = -2.0 * CTDM_PI_D * (double)e / (double)L;
+            h[e] = make_float2((float)cos(a), (float)sin(a));
+        }
+        float2 *d = nullptr;
+        cudaError_t err = cudaMalloc(&d, sizeof(float2) * L);
+        if (err != cudaSuccess) return err;
+        err = cudaMemcpy(d, h.data(), sizeof(float2) * L, cudaMemcpyHostToDevice);
+        if (err != cudaSuccess) return err;
+        t.tw[L] = d;
+    }
+    for (int M : kCrops) {
+        std::vector<float2> h(2 * M + 1);
+        for (int k = 0; k <= 2 * M; k++) {
+            const double a = (double)k * CTDM_PI_D / (2.0 * M);
+            h[k] = make_float2((float)cos(a), (float)sin(a));
+        }
+        std::vector<float> e(M);
+        for (int k = 0; k < M; k++) {
+            const double s = sin(2.0 * CTDM_PI_D * (double)k / (4.0 * M - 1.0));
+            e[k] = (float)(4.0 * s * s);
+        }
+        float2 *d = nullptr;
+        float *de = nullptr;
+        cudaError_t err = cudaMalloc(&d, sizeof(float2) * (2 * M + 1));
+        if (err == cudaSuccess) err = cudaMemcpy(d, h.data(), sizeof(float2) * (2 * M + 1), cudaMemcpyHostToDevice);
+        if (err == cudaSuccess) err = cudaMalloc(&de, sizeof(float) * M);
+        if (err == cudaSuccess) err = cudaMemcpy(de, e.data(), sizeof(float) * M, cudaMemcpyHostToDevice);
+        if (err != cudaSuccess) return err;
+        t.dtw[M] = d;
+        t.eig[M] = de;
+    }
+    t.complete = true;
+    (void)dev;
+    return cudaSuccess;
+}
+
+static cudaError_t ensure_tables()
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(g_tab_mu);
+    DevTables &t = g_tables[dev];
+    if (t.complete) return cudaSuccess;
+    return build_tables(dev, t);
+}
+
+static DevTables *tables_here()
+{
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(g_tab_mu);
+    auto it = g_tables.find(dev);
+    return it == g_tables.end() ? nullptr : &it->second;
+}
+
+namespace ctdm {
+const float2 *twiddles(int L)
+{
+    DevTables *t = tables_here();
+    if (!t) return nullptr;
+    auto it = t->tw.find(L);
+    return it == t->tw.end() ? nullptr : it->second;
+}
+const float2 *dct_twiddles(int M)
+{
+    DevTables *t = tables_here();
+    if (!t) return nullptr;
+    auto it = t->dtw.find(M);
+    return it == t->dtw.end() ? nullptr : it->second;
+}
+const float *dct_eigen(int M)
+{
+    DevTables *t = tables_here();
+    if (!t) return nullptr;
+    auto it = t->eig.find(M);
+    return it == t->eig.end() ? nullptr : it->second;
+}
+}  // namespace ctdm
+
+// ---------------------------------------------------------------- context
+enum BufId {
+    B_PHASE, B_AMP, B_PHU, B_CHG, B_CUT, B_GOLD, B_U, B_F2, B_COUNTS, B_G, B_T1, B_S, B_BGF, B_DCT, B_MASK, B_GEOM,
+    B_CARRIER, B_KEY, B_SCRATCH, B_HOLO, B_BG, B_RI, B_GSTATE, B_GLIST, B_GSTATUS, B_FASTW, B_FASTIN, B_TMP, NBUF
+};
+
+// Stage boundaries recorded with CUDA events when timing is enabled.
+enum StageTag { S_QPI, S_UNWRAP, S_GOLD, S_SPECTRA, S_EWALD, S_YINV, S_XPASS, S_YFWD, S_ZPASS, S_XFINAL, S_COUNT };
+
+struct StageTimer {
+    static const int kMax = 1024;
+    cudaEvent_t ev[kMax] = {};
+    int tag[kMax] = {};
+    int n = 0;
+    bool on = false;
+    void start(cudaStream_t s)
+    {
+        if (!on) return;
+        n = 0;
+        mark(-1, s);
+    }
+    void mark(int t, cudaStream_t s)
+    {
+        if (!on || n >= kMax) return;
+        if (!ev[n]) cudaEventCreate(&ev[n]);
+        tag[n] = t;
+        cudaEventRecord(ev[n], s);
+        n++;
+    }
+};
+
+struct ctdm_ctx {
+    int device = 0;
+    void *buf[NBUF] = {};
+    size_t cap[NBUF] = {};
+    size_t used[NBUF] = {};
+    int carrier[3] = {-1, -1, -1};
+    StageTimer timer;
+};
+
+static cudaError_t ensure(ctdm_ctx *c, int id, size_t bytes)
+{
+    c->used[id] = bytes;
+    if (c->cap[id] >= bytes && c->buf[id]) return cudaSuccess;
+    if (c->buf[id]) cudaFree(c->buf[id]);
+    c->buf[id] = nullptr;
+    c->cap[id] = 0;
+    if (bytes == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc(&c->buf[id], bytes);
+    if (e == cudaSuccess) c->cap[id] = bytes;
+    return e;
+}
+
+template <class T> static T *B(ctdm_ctx *c, int id) { return reinterpret_cast<T *>(c->buf[id]); }
+
+extern "C" void ctdm_params_default(ctdm_params *p)
+{
+    std::memset(p, 0, sizeof *p);
+    p->n_holo = 1024;
+    p->m_crop = 0;
+    p->r_vol = 256;
+    p->iterations = 101;   // IterTime = 100 runs IterTime + 1 bodies (cTDM/HilbertTransform.cu:34,1957)
+    p->unwrap_mode = CTDM_UNWRAP_REF;
+    p->check_mode = CTDM_CHECK_REF;
+    p->unwrap_method = CTDM_METHOD_DCT;
+    p->carrier_r = p->carrier_c = p->carrier_radius = -1;
+    p->n_med = 1.333;      // cTDM/HilbertTransform.cu:18
+    p->wavelength = 532e-9;
+    p->dx = 5.5e-6 / 85.0 * 1024.0 / 256.0;   // CameraPixelSize/Mag*1024/R (:1854) at the defaults
+}
+
+extern "C" ctdm_status ctdm_ctx_create(int device, ctdm_ctx **out)
+{
+    if (!out) return invalid("ctdm_ctx_create: out is NULL");
+    CK(cudaSetDevice(device), "cudaSetDevice");
+    CK(ensure_tables(), "building twiddle tables");
+    ctdm_ctx *c = new ctdm_ctx();
+    c->device = device;
+    *out = c;
+    g_err.clear();
+    return CTDM_OK;
+}
+
+extern "C" void ctdm_ctx_destroy(ctdm_ctx *c)
+{
+    if (!c) return;
+    cudaSetDevice(c->device);
+    for (int i = 0; i < NBUF; i++)
+        if (c->buf[i]) cudaFree(c->buf[i]);
+    for (int i = 0; i < StageTimer::kMax; i++)
+        if (c->timer.ev[i]) cudaEventDestroy(c->timer.ev[i]);
+    delete c;
+}
+
+extern "C" ctdm_status ctdm_ctx_set_timing(ctdm_ctx *c, int on)
+{
+    if (!c) return invalid("ctdm_ctx_set_timing: NULL context");
+    c->timer.on = on != 0;
+    c->timer.n = 0;
+    return CTDM_OK;
+}
+
+// Per-stage device time (ms) and launch-group count of the last timed pipeline call.
+extern "C" ctdm_status ctdm_ctx_stage_times(ctdm_ctx *c, double *ms, int *counts, int n)
+{
+    if (!c || !ms || n < 1) return invalid("ctdm_ctx_stage_times: bad argument");
+    for (int i = 0; i < n; i++) {
+        ms[i] = 0;
+        if (counts) counts[i] = 0;
+    }
+    StageTimer &t = c->timer;
+    if (t.n < 2) return CTDM_OK;
+    CK(cudaEventSynchronize(t.ev[t.n - 1]), "stage timing");
+    for (int i = 1; i < t.n; i++) {
+        float dt = 0;
+        CK(cudaEventElapsedTime(&dt, t.ev[i - 1], t.ev[i]), "stage timing");
+        if (t.tag[i] >= 0 && t.tag[i] < n) {
+            ms[t.tag[i]] += dt;
+            if (counts) counts[t.tag[i]]++;
+        }
+    }
+    return CTDM_OK;
+}
+
+extern "C" ctdm_status ctdm_ctx_carrier(ctdm_ctx *c, int *carrier3)
+{
+    if (!c || !carrier3) return invalid("ctdm_ctx_carrier: NULL argument");
+    std::memcpy(carrier3, c->carrier, sizeof c->carrier);
+    return CTDM_OK;
+}
+
+extern "C" ctdm_status ctdm_ctx_buffer(ctdm_ctx *c, int which, void **dptr, size_t *bytes)
+{
+    static const int map[] = {B_PHASE, B_AMP, B_PHU, B_CHG, B_CUT, B_GOLD, B_U, B_F2, B_COUNTS};
+    if (!c || !dptr || which < 0 || which > 8) return invalid("ctdm_ctx_buffer: bad argument");
+    *dptr = c->buf[map[which]];
+    if (bytes) *bytes = c->used[map[which]];
+    return CTDM_OK;
+}
+
+// ---------------------------------------------------------------- geometry
+// Per-angle illumination for the voxel rule, computed like the FP64 oracle:
+// fx0 = fm0 sin(AngY), fy0 = fm0 sin(AngX) (EdwardSphere, cTDM/Recon_kernel.cu:171-185).
+static void angle_geometry(const float *angx, const float *angy, int A, double fm0, double df,
+                           std::vector<AngleGeom> &g)
+{
+    g.resize(A);
+    const double fm02 = fm0 * fm0;
+    for (int a = 0; a < A; a++) {
+        const double fx0 = fm0 * sin((double)angy[a]);
+        const double fy0 = fm0 * sin((double)angx[a]);
+        double rad0 = fm02 - fx0 * fx0;
+        rad0 = rad0 - fy0 * fy0;
+        AngleGeom &q = g[a];
+        q.fx0 = fx0;
+        q.fy0 = fy0;
+        q.valid = rad0 >= 0.0;
+        q.fz0 = q.valid ? sqrt(rad0) : 0.0;
+        q.fx0s = (float)(fx0 / df);
+        q.fy0s = (float)(fy0 / df);
+        q.fz0s = (float)(q.fz0 / df);
+    }
+}
+
+static ctdm_status upload_geometry(ctdm_ctx *c, const float *angx, const float *angy, int A, double fm0, double df,
+                                   cudaStream_t s)
+{
+    std::vector<AngleGeom> g;
+    angle_geometry(angx, angy, A, fm0, df, g);
+    CK(ensure(c, B_GEOM, sizeof(AngleGeom) * A), "alloc geometry");
+    // pageable source: the copy is staged before the call returns
+    CK(cudaMemcpyAsync(c->buf[B_GEOM], g.data(), sizeof(AngleGeom) * A, cudaMemcpyHostToDevice, s), "upload geometry");
+    return CTDM_OK;
+}
+
+// ---------------------------------------------------------------- stage helpers
+static const int kMaxAngles = 512;
+
+static ctdm_status do_qpi(ctdm_ctx *c, int N, int M, int A, const float *holo, const float *bg, int bg_per_angle,
+                          const int *carrier_in, float *phase, float *amp, cudaStream_t s)
+{
+    if (N < 64 || N > 2048 || (N & (N - 1))) return invalid("hologram side %d unsupported", N);
+    if (!ok_length(M) || M > N) return invalid("window side %d unsupported", M);
+    if (A < 1) return invalid("no angles");
+    CK(ensure(c, B_CARRIER, sizeof(int) * 3), "alloc carrier");
+    CK(ensure(c, B_KEY, sizeof(unsigned long long)), "alloc key");
+    int *car = B<int>(c, B_CARRIER);
+    if (carrier_in && carrier_in[0] >= 0 && carrier_in[1] >= 0 && carrier_in[2] >= 0) {
+        if (carrier_in[1] - M / 2 < 0 || carrier_in[1] + M / 2 > N || carrier_in[0] - M / 2 < 0 ||
+            carrier_in[0] + M / 2 > N)
+            return invalid("window around carrier (%d, %d) leaves the spectrum", carrier_in[0], carrier_in[1]);
+        CK(set_carrier(car, carrier_in[0], carrier_in[1], carrier_in[2], s), "set carrier");
+    } else {
+        CK(ensure(c, B_SCRATCH, sizeof(float2) * N * N), "alloc carrier scratch");
+        CK(qpi_find_carrier(bg, N, B<float2>(c, B_SCRATCH), B<unsigned long long>(c, B_KEY), car, s),
+           "carrier search");
+    }
+    // window chunk: T1 <= 64 MB
+    long chunk = (64l << 20) / ((long)N * M * 8);
+    if (chunk < 2) chunk = 2;
+    if (chunk > A) chunk = A;
+    const long mm = (long)M * M, nn = (long)N * N;
+    CK(ensure(c, B_T1, sizeof(float2) * chunk * N * M), "alloc T1");
+    CK(ensure(c, B_S, sizeof(float2) * chunk * mm), "alloc S");
+    const int nbg = bg_per_angle ? A : 1;
+    CK(ensure(c, B_BGF, sizeof(float2) * nbg * mm), "alloc BG field");
+    for (long a0 = 0; a0 < nbg; a0 += chunk) {
+        const int ac = (int)std::min<long>(chunk, nbg - a0);
+        CK(qpi_forward_window(bg + a0 * nn, ac, N, M, car, B<float2>(c, B_T1), B<float2>(c, B_S), s), "qpi bg fwd");
+        CK(qpi_inverse_window(B<float2>(c, B_S), ac, M, B<float2>(c, B_BGF) + a0 * mm, nullptr, 0, nullptr, nullptr,
+                              s),
+           "qpi bg inv");
+    }
+    for (long a0 = 0; a0 < A; a0 += chunk) {
+        const int ac = (int)std::min<long>(chunk, A - a0);
+        CK(qpi_forward_window(holo + a0 * nn, ac, N, M, car, B<float2>(c, B_T1), B<float2>(c, B_S), s), "qpi fwd");
+        const float2 *bgf = B<float2>(c, B_BGF) + (bg_per_angle ? a0 * mm : 0);
+        CK(qpi_inverse_window(B<float2>(c, B_S), ac, M, nullptr, bgf, bg_per_angle ? mm : 0, phase + a0 * mm,
+                              amp + a0 * mm, s),
+           "qpi inv");
+    }
+    return CTDM_OK;
+}
+
+static ctdm_status do_positivity(ctdm_ctx *c, int R, int iters, int check_mode, double k2, double n_med,
+                                 const float2 *F2, const uint8_t *mask, float2 *G, float2 *ri, cudaStream_t s)
+{
+    LoopArgs la;
+    la.G = G;
+    la.F2 = F2;
+    la.mask = mask;
+    la.out = ri;
+    la.R = R;
+    la.inv_n3 = (float)(1.0 / ((double)R * R * R));
+    la.k2 = (float)k2;
+    la.n_med = (float)n_med;
+    la.n_med2 = (float)(n_med * n_med);
+    StageTimer &tm = c->timer;
+    CK(launch_ypass(la, true, s), "y inverse pass");
+    tm.mark(S_YINV, s);
+    for (int it = 0; it < iters; it++) {
+        CK(launch_xpass(la, false, s), "x pass");
+        tm.mark(S_XPASS, s);
+        CK(launch_ypass(la, false, s), "y forward pass");
+        tm.mark(S_YFWD, s);
+        CK(launch_zpass(la, check_mode, s), "z pass");
+        tm.mark(S_ZPASS, s);
+        CK(launch_ypass(la, true, s), "y inverse pass");
+        tm.mark(S_YINV, s);
+    }
+    CK(launch_xpass(la, true, s), "final x pass");
+    tm.mark(S_XFINAL, s);
+    return CTDM_OK;
+}
+
+static ctdm_status validate(const ctdm_params *p, int A, int &M)
+{
+    if (!p) return invalid("params is NULL");
+    const int N = p->n_holo;
+    M = p->m_crop ? p->m_crop : N / 4;
+    if (N < 64 || N > 2048 || (N & (N - 1))) return invalid("hologram side %d unsupported", N);
+    if (!ok_crop(M) || M > N) return invalid("window side %d unsupported", M);
+    if (!ok_volume(p->r_vol) || p->r_vol > N) return invalid("volume side %d unsupported", p->r_vol);
+    if (A < 1 || A > kMaxAngles) return invalid("angle count %d outside 1..%d", A, kMaxAngles);
+    if (p->iterations < 0) return invalid("negative iteration count");
+    if (p->n_med <= 0 || p->wavelength <= 0 || p->dx <= 0) return invalid("non-positive physical parameter");
+    if (p->unwrap_method < 0 || p->unwrap_method > 2) return invalid("unknown unwrap method");
+    return CTDM_OK;
+}
+
+// ---------------------------------------------------------------- pipeline
+extern "C" ctdm_status ctdm_reconstruct_device(ctdm_ctx *c, const ctdm_params *p, int A, const float *d_holo,
+                                               const float *d_bg, const float *h_angx, const float *h_angy,
+                                               ctdm_cfloat *d_ri, void *stream)
+{
+    if (!c || !d_holo || !d_bg || !h_angx || !h_angy || !d_ri) return invalid("ctdm_reconstruct_device: NULL argument");
+    int M;
+    ctdm_status st = validate(p, A, M);
+    if (st != CTDM_OK) return st;
+    CK(cudaSetDevice(c->device), "cudaSetDevice");
+    cudaStream_t s = (cudaStream_t)stream;
+    const int N = p->n_holo, R = p->r_vol;
+    const long mm = (long)M * M, rr = (long)R * R, r3 = rr * R;
+    CK(ensure(c, B_PHASE, sizeof(float) * A * mm), "alloc phase");
+    CK(ensure(c, B_AMP, sizeof(float) * A * mm), "alloc amp");
+    CK(ensure(c, B_PHU, sizeof(float) * A * mm), "alloc unwrapped");
+    CK(ensure(c, B_DCT, sizeof(float) * A * mm), "alloc dct scratch");
+    CK(ensure(c, B_U, sizeof(float2) * A * rr), "alloc spectra");
+    CK(ensure(c, B_F2, sizeof(float2) * r3), "alloc F2");
+    CK(ensure(c, B_G, sizeof(float2) * r3), "alloc G");
+    const bool mask_mode = p->check_mode == CTDM_CHECK_MASK;
+    CK(ensure(c, B_COUNTS, mask_mode ? sizeof(uint32_t) * r3 : 0), "alloc counts");
+    CK(ensure(c, B_MASK, mask_mode ? r3 : 0), "alloc mask");
+
+    StageTimer &tm = c->timer;
+    tm.start(s);
+    const int car_in[3] = {p->carrier_r, p->carrier_c, p->carrier_radius};
+    st = do_qpi(c, N, M, A, d_holo, d_bg, p->bg_per_angle, car_in, B<float>(c, B_PHASE), B<float>(c, B_AMP), s);
+    if (st != CTDM_OK) return st;
+    tm.mark(S_QPI, s);
+
+    const float *unwrapped = B<float>(c, B_PHU);
+    if (p->run_goldstein || p->unwrap_method == CTDM_METHOD_GOLDSTEIN) {
+        CK(ensure(c, B_CHG, A * mm), "alloc charges");
+        CK(ensure(c, B_CUT, A * mm), "alloc cuts");
+        CK(ensure(c, B_GOLD, sizeof(float) * A * mm), "alloc goldstein out");
+        CK(ensure(c, B_GSTATE, A * mm), "alloc goldstein state");
+        CK(ensure(c, B_GLIST, sizeof(int) * 2 * A * mm), "alloc goldstein lists");
+        CK(ensure(c, B_GSTATUS, sizeof(int) * A), "alloc goldstein status");
+        CK(goldstein_residues(B<float>(c, B_PHASE), A, M, M, B<int8_t>(c, B_CHG), s), "goldstein residues");
+        CK(goldstein_cuts(B<int8_t>(c, B_CHG), A, M, M, B<uint8_t>(c, B_CUT), reinterpret_cast<int8_t *>(B<float>(c, B_DCT)),
+                          s),
+           "goldstein cuts");
+        CK(goldstein_floodfill(B<uint8_t>(c, B_CUT), B<float>(c, B_PHASE), A, M, M, B<float>(c, B_GOLD),
+                               B<uint8_t>(c, B_GSTATE), B<int>(c, B_GLIST), B<int>(c, B_GSTATUS), s),
+           "goldstein flood fill");
+        tm.mark(S_GOLD, s);
+    }
+    if (p->unwrap_method == CTDM_METHOD_DCT) {
+        CK(dct_unwrap(B<float>(c, B_PHASE), B<float>(c, B_PHU), B<float>(c, B_DCT), A, M, p->unwrap_mode, s),
+           "dct unwrap");
+    } else if (p->unwrap_method == CTDM_METHOD_FAST) {
+        CK(ensure(c, B_FASTIN, sizeof(float) * A * mm), "alloc fast-unwrap input");
+        CK(ensure(c, B_FASTW, sizeof(float2) * 3 * 4 * mm), "alloc fast-unwrap work");
+        CK(cudaMemcpyAsync(c->buf[B_FASTIN], c->buf[B_PHASE], sizeof(float) * A * mm, cudaMemcpyDeviceToDevice, s),
+           "copy phase");
+        CK(fast_unwrap(B<float>(c, B_FASTIN), B<float>(c, B_PHU), B<float2>(c, B_FASTW), A, M, s), "fast unwrap");
+    } else {
+        unwrapped = B<float>(c, B_GOLD);
+    }
+    tm.mark(S_UNWRAP, s);
+    CK(prep_rytov(unwrapped, B<float>(c, B_AMP), A, M, N, R, B<float2>(c, B_U), s), "prep");
+    CK(fft_rows(B<float2>(c, B_U), R, (long)A * R, false, s), "spectra rows");
+    CK(fft_cols(B<float2>(c, B_U), R, (long)A * R, R, rr, R, false, s), "spectra cols");
+    tm.mark(S_SPECTRA, s);
+
+    const double fm0 = p->n_med / p->wavelength;
+    const double df = 1.0 / (R * p->dx);
+    const double k = 2.0 * CTDM_PI_D * p->n_med / p->wavelength;
+    st = upload_geometry(c, h_angx, h_angy, A, fm0, df, s);
+    if (st != CTDM_OK) return st;
+    EwaldArgs ea;
+    ea.U = B<float2>(c, B_U);
+    ea.geom = B<AngleGeom>(c, B_GEOM);
+    ea.A = A;
+    ea.R = R;
+    ea.fm0 = fm0;
+    ea.df = df;
+    ea.fm02 = fm0 * fm0;
+    ea.fm02s = (float)((fm0 / df) * (fm0 / df));
+    ea.dx = (float)p->dx;
+    ea.F2 = B<float2>(c, B_F2);
+    ea.G = B<float2>(c, B_G);
+    ea.counts = mask_mode ? B<uint32_t>(c, B_COUNTS) : nullptr;
+    ea.mask = mask_mode ? B<uint8_t>(c, B_MASK) : nullptr;
+    CK(launch_ewald(ea, s), "ewald mapping");
+    tm.mark(S_EWALD, s);
+    st = do_positivity(c, R, p->iterations, p->check_mode, k * k, p->n_med, B<float2>(c, B_F2),
+                       mask_mode ? B<uint8_t>(c, B_MASK) : nullptr, B<float2>(c, B_G),
+                       reinterpret_cast<float2 *>(d_ri), s);
+    if (st != CTDM_OK) return st;
+    CK(cudaMemcpyAsync(c->carrier, c->buf[B_CARRIER], sizeof(int) * 3, cudaMemcpyDeviceToHost, s), "carrier readback");
+    g_err.clear();
+    return CTDM_OK;
+}
+
+extern "C" ctdm_status ctdm_reconstruct(ctdm_ctx *c, const ctdm_params *p, int A, const float *h_holo,
+                                        const float *h_bg, const float *h_angx, const float *h_angy,
+                                        ctdm_cfloat *h_ri)
+{
+    if (!c || !p || !h_holo || !h_bg || !h_ri) return invalid("ctdm_reconstruct: NULL argument");
+    int M;
+    ctdm_status st = validate(p, A, M);
+    if (st != CTDM_OK) return st;
+    CK(cudaSetDevice(c->device), "cudaSetDevice");
+    const long nn = (long)p->n_holo * p->n_holo, r3 = (long)p->r_vol * p->r_vol * p->r_vol;
+    const int nbg = p->bg_per_angle ? A : 1;
+    CK(ensure(c, B_HOLO, sizeof(float) * A * nn), "alloc holograms");
+    CK(ensure(c, B_BG, sizeof(float) * nbg * nn), "alloc background");
+    CK(ensure(c, B_RI, sizeof(float2) * r3), "alloc volume");
+    cudaStream_t s = 0;
+    CK(cudaMemcpyAsync(c->buf[B_BG], h_bg, sizeof(float) * nbg * nn, cudaMemcpyHostToDevice, s), "upload background");
+    CK(cudaMemcpyAsync(c->buf[B_HOLO], h_holo, sizeof(float) * A * nn, cudaMemcpyHostToDevice, s), "upload holograms");
+    st = ctdm_reconstruct_device(c, p, A, B<float>(c, B_HOLO), B<float>(c, B_BG), h_angx, h_angy,
+                                 B<ctdm_cfloat>(c, B_RI), s);
+    if (st != CTDM_OK) return st;
+    CK(cudaMemcpyAsync(h_ri, c->buf[B_RI], sizeof(float2) * r3, cudaMemcpyDeviceToHost, s), "download volume");
+    CK(cudaStreamSynchronize(s), "synchronise");
+    return CTDM_OK;
+}
+
+// ---------------------------------------------------------------- stage API
+extern "C" ctdm_status ctdm_qpi(ctdm_ctx *c, int N, int M, int A, const float *d_holo, const float *d_bg,
+                                int bg_per_angle, int *carrier3, float *d_phase, float *d_amp, void *stream)
+{
+    if (!c || !d_holo || !d_bg || !d_phase || !d_amp) return invalid("ctdm_qpi: NULL argument");
+    CK(cudaSetDevice(c->device), "cudaSetDevice");
+    cudaStream_t s = (cudaStream_t)stream;
+    ctdm_status st = do_qpi(c, N, M, A, d_holo, d_bg, bg_per_angle, carrier3, d_phase, d_amp, s);
+    if (st != CTDM_OK) return st;
+    CK(cudaMemcpyAsync(c->carrier, c->buf[B_CARRIER], sizeof(int) * 3, cudaMemcpyDeviceToHost, s), "carrier");
+    CK(cudaStreamSynchronize(s), "synchronise");
+    if (carrier3) std::memcpy(carrier3, c->carrier, sizeof c->carrier);
+    return CTDM_OK;
+}
+
+extern "C" ctdm_status ctdm_unwrap_dct(ctdm_ctx *c, int A, int M, int mode, const float *d_phi, float *d_out,
+                                       void *stream)
+{
+    if (!c || !d_phi || !d_out) return invalid("ctdm_unwrap_dct: NULL argument");
+    if (!ok_crop(M) || A < 1) return invalid("ctdm_unwrap_dct: size %d unsupported", M);
+    CK(cudaSetDevice(c->device), "cudaSetDevice");
+    CK(ensure(c, B_TMP, sizeof(float) * A * M * M), "alloc scratch");
+    CK(dct_unwrap(d_phi, d_out, B<float>(c, B_TMP), A, M, mode, (cudaStream_t)stream), "dct unwrap");
+    return CTDM_OK;
+}
+
+extern "C" ctdm_status ctdm_unwrap_fast(ctdm_ctx *c, int A, int M, float *d_phi, float *d_out, void *stream)
+{
+    if (!c || !d_phi || !d_out) return invalid("ctdm_unwrap_fast: NULL argument");
+    if (!ok_crop(M) || A < 1) return invalid("ctdm_unwrap_fast: size %d unsupported", M);
+    CK(cudaSetDevice(c->device), "cudaSetDevice");
+    CK(ensure(c, B_FASTW, sizeof(float2) * 3 * 4 * M * M), "alloc scratch");
+    CK(fast_unwrap(d_phi, d_out, B<float2>(c, B_FASTW), A, M, (cudaStream_t)stream), "fast unwrap");
+    return CTDM_OK;
+}
+
+extern "C" ctdm_status ctdm_goldstein(ctdm_ctx *c, int A, int W, int H, const float *d_phi, int8_t *d_charges,
+                                      uint8_t *d_cuts, float *d_out, int *h_status, void *stream)
+{
+    if (!c || !d_phi || !d_charges || !d_cuts || !d_out) return invalid("ctdm_goldstein: NULL argument");
+    if (W < 4 || H < 4 || W > 1024 || H > 1024 || A < 1) return invalid("ctdm_goldstein: size unsupported");
+    CK(cudaSetDevice(c->device), "cudaSetDevice");
+    cudaStream_t s = (cudaStream_t)stream;
+    const long n = (long)W * H;
+    CK(ensure(c, B_GSTATE, A * n), "alloc state");
+    CK(ensure(c, B_GLIST, sizeof(int) * 2 * A * n), "alloc lists");
+    CK(ensure(c, B_GSTATUS, sizeof(int) * A), "alloc status");
+    CK(ensure(c, B_TMP, A * n), "alloc work");
+    CK(goldstein_residues(d_phi, A, W, H, d_charges, s), "residues");
+    CK(goldstein_cuts(d_charges, A, W, H, d_cuts, B<int8_t>(c, B_TMP), s), "branch cuts");
+    CK(goldstein_floodfill(d_cuts, d_phi, A, W, H, d_out, B<uint8_t>(c, B_GSTATE), B<int>(c, B_GLIST),
+                           B<int>(c, B_GSTATUS), s),
+       "flood fill");
+    std::vector<int> stv(A);
+    CK(cudaMemcpyAsync(stv.data(), c->buf[B_GSTATUS], sizeof(int) * A, cudaMemcpyDeviceToHost, s), "status");
+    CK(cudaStreamSynchronize(s), "synchronise");
+    bool stalled = false;
+    for (int a = 0; a < A; a++) stalled |= stv[a] != 0;
+    if (h_status) std::memcpy(h_status, stv.data(), sizeof(int) * A);
+    if (stalled) {
+        set_err("ctdm_goldstein: flood fill stopped early on at least one map");
+        return CTDM_ERR_STALLED;
+    }
+    return CTDM_OK;
+}
+
+extern "C" ctdm_status ctdm_prepare_spectra(ctdm_ctx *c, int A, int M, int N, int R, const float *d_phase,
+                                            const float *d_amp, ctdm_cfloat *d_U, void *stream)
+{
+    if (!c || !d_phase || !d_amp || !d_U) return invalid("ctdm_prepare_spectra: NULL argument");
+    if (!ok_volume(R) || R > N || M < 2 || A < 1) return invalid("ctdm_prepare_spectra: size unsupported");
+    CK(cudaSetDevice(c->device), "cudaSetDevice");
+    cudaStream_t s = (cudaStream_t)stream;
+    float2 *U = reinterpret_cast<float2 *>(d_U);
+    CK(prep_rytov(d_phase, d_amp, A, M, N, R, U, s), "prep");
+    CK(fft_rows(U, R, (long)A * R, false, s), "rows");
+    CK(fft_cols(U, R, (long)A * R, R, (long)R * R, R, false, s), "cols");
+    return CTDM_OK;
+}
+
+extern "C" ctdm_status ctdm_stack_spectra(ctdm_ctx *c, int A, int R, const float *d_ph, const float *d_am,
+                                          ctdm_cfloat *d_U, void *stream)
+{
+    if (!c || !d_ph || !d_am || !d_U) return invalid("ctdm_stack_spectra: NULL argument");
+    if (!ok_volume(R) || A < 1) return invalid("ctdm_stack_spectra: size unsupported");
+    CK(cudaSetDevice(c->device), "cudaSetDevice");
+    cudaStream_t s = (cudaStream_t)stream;
+    float2 *U = reinterpret_cast<float2 *>(d_U);
+    CK(stack_to_rytov(d_ph, d_am, A, R, U, s), "stack prep");
+    CK(fft_rows(U, R, (long)A * R, false, s), "rows");
+    CK(fft_cols(U, R, (long)A * R, R, (long)R * R, R, false, s), "cols");
+    return CTDM_OK;
+}
+
+extern "C" ctdm_status ctdm_prepare_stack(ctdm_ctx *c, int A, int M, int N, int R, const float *d_phase,
+                                          const float *d_amp, float *d_ph_out, float *d_am_out, void *stream)
+{
+    if (!c || !d_phase || !d_amp || !d_ph_out || !d_am_out) return invalid("ctdm_prepare_stack: NULL argument");
+    if (R > N || R < 1 || M < 2 || A < 1) return invalid("ctdm_prepare_stack: size unsupported");
+    CK(cudaSetDevice(c->device), "cudaSetDevice");
+    CK(prep_stack(d_phase, d_amp, A, M, N, R, d_ph_out, d_am_out, (cudaStream_t)stream), "prep stack");
+    return CTDM_OK;
+}
+
+extern "C" ctdm_status ctdm_map_ewald(ctdm_ctx *c, int A, int R, const ctdm_cfloat *d_U, const float *h_angx,
+                                      const float *h_angy, double fm0, double df, double dx, ctdm_cfloat *d_F2,
+                                      uint32_t *d_counts, void *stream)
+{
+    if (!c || !d_U || !h_angx || !h_angy || !d_F2) return invalid("ctdm_map_ewald: NULL argument");
+    if (!ok_volume(R) || A < 1 || A > kMaxAngles) return invalid("ctdm_map_ewald: size unsupported");
+    CK(cudaSetDevice(c->device), "cudaSetDevice");
+    cudaStream_t s = (cudaStream_t)stream;
+    const long r3 = (long)R * R * R;
+    ctdm_status st = upload_geometry(c, h_angx, h_angy, A, fm0, df, s);
+    if (st != CTDM_OK) return st;
+    CK(ensure(c, B_TMP, sizeof(float2) * r3), "alloc G");
+    EwaldArgs ea;
+    ea.U = reinterpret_cast<const float2 *>(d_U);
+    ea.geom = B<AngleGeom>(c, B_GEOM);
+    ea.A = A;
+    ea.R = R;
+    ea.fm0 = fm0;
+    ea.df = df;
+    ea.fm02 = fm0 * fm0;
+    ea.fm02s = (float)((fm0 / df) * (fm0 / df));
+    ea.dx = (float)dx;
+    ea.F2 = reinterpret_cast<float2 *>(d_F2);
+    ea.G = B<float2>(c, B_TMP);
+    ea.counts = d_counts;
+    ea.mask = nullptr;
+    CK(launch_ewald(ea, s), "ewald mapping");
+    return CTDM_OK;
+}
+
+extern "C" ctdm_status ctdm_positivity(ctdm_ctx *c, int R, int iterations, int check_mode, double k2, double n_med,
+                                       const ctdm_cfloat *d_F2, const uint32_t *d_counts, ctdm_cfloat *d_ri,
+                                       void *stream)
+{
+    if (!c || !d_F2 || !d_ri) return invalid("ctdm_positivity: NULL argument");
+    if (!ok_volume(R) || iterations < 0) return invalid("ctdm_positivity: size unsupported");
+    if (check_mode == CTDM_CHECK_MASK && !d_counts) return invalid("ctdm_positivity: mask mode needs counts");
+    CK(cudaSetDevice(c->device), "cudaSetDevice");
+    cudaStream_t s = (cudaStream_t)stream;
+    const long rr = (long)R * R, r3 = rr * R;
+    CK(ensure(c, B_G, sizeof(float2) * r3), "alloc G");
+    float2 *G = B<float2>(c, B_G);
+    CK(cudaMemcpyAsync(G, d_F2, sizeof(float2) * r3, cudaMemcpyDeviceToDevice, s), "copy F2");
+    CK(fft_cols(G, R, rr, (int)rr, 0, rr, true, s), "z inverse");
+    const uint8_t *mask = nullptr;
+    if (check_mode == CTDM_CHECK_MASK) {
+        CK(ensure(c, B_MASK, r3), "alloc mask");
+        CK(counts_to_mask(d_counts, B<uint8_t>(c, B_MASK), r3, s), "mask");
+        mask = B<uint8_t>(c, B_MASK);
+    }
+    return do_positivity(c, R, iterations, check_mode, k2, n_med, reinterpret_cast<const float2 *>(d_F2), mask, G,
+                         reinterpret_cast<float2 *>(d_ri), s);
+}
+
+extern "C" ctdm_status ctdm_fft(ctdm_cfloat *d_data, int rank, const int *dims, int batch, int inverse, void *stream)
+{
+    if (!d_data || !dims || rank < 1 || rank > 3 || batch < 1) return invalid("ctdm_fft: bad argument");
+    for (int r = 0; r < rank; r++)
+        if (!ok_length(dims[r])) return invalid("ctdm_fft: length %d unsupported", dims[r]);
+    if (reinterpret_cast<uintptr_t>(d_data) & 15) return invalid("ctdm_fft: data must be 16-byte aligned");
+    CK(ensure_tables(), "tables");
+    cudaStream_t s = (cudaStream_t)stream;
+    float2 *d = reinterpret_cast<float2 *>(d_data);
+    const long nx = dims[0], ny = rank > 1 ? dims[1] : 1, nz = rank > 2 ? dims[2] : 1;
+    const long per = nx * ny * nz;
+    CK(fft_rows(d, (int)nx, per / nx * batch, inverse != 0, s), "fft x");
+    if (rank > 1) CK(fft_cols(d, (int)ny, nx * nz * batch, (int)nx, nx * ny, nx, inverse != 0, s), "fft y");
+    if (rank > 2) CK(fft_cols(d, (int)nz, nx * ny * batch, (int)(nx * ny), per, nx * ny, inverse != 0, s), "fft z");
+    return CTDM_OK;
+}
+
+// ---------------------------------------------------------------- reference-named entry points
+static std::mutex g_def_mu;
+static std::map<int, ctdm_ctx *> g_default;
+
+static ctdm_ctx *default_ctx()
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+    std::lock_guard<std::mutex> lk(g_def_mu);
+    auto it = g_default.find(dev);
+    if (it != g_default.end()) return it->second;
+    ctdm_ctx *c = nullptr;
+    if (ctdm_ctx_create(dev, &c) != CTDM_OK) return nullptr;
+    g_default[dev] = c;
+    return c;
+}
+
+static bool finish(const char *what)
+{
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        cuda_fail(e, what);
+        return false;
+    }
+    g_err.clear();
+    return true;
+}
+
+// Reference globals for BatchRecon (cTDM/HilbertTransform.cu:11-35).
+static int g_recon = 256, g_iter_time = 100, g_recon_save = 0;
+static double g_nmed = 1.333, g_wavelength_nm = 532, g_pixel_um = 5.5, g_mag = 85.0;
+static std::string g_save_dir = ".";
+
+extern "C" void ctdm_set_recon_globals(int recon_size, double n_med, double wavelength_nm, double camera_pixel_um,
+                                       double mag, int iter_time, int recon_save, const char *save_dir)
+{
+    g_recon = recon_size;
+    g_nmed = n_med;
+    g_wavelength_nm = wavelength_nm;
+    g_pixel_um = camera_pixel_um;
+    g_mag = mag;
+    g_iter_time = iter_time;
+    g_recon_save = recon_save;
+    g_save_dir = save_dir ? save_dir : ".";
+}
+
+extern "C" void DCT_UWLS_Unwrapped(float *ImgDst, float *ImgSrc, int sizeX, int sizeY)
+{
+    ctdm_ctx *c = default_ctx();
+    if (!c) return;
+    if (sizeX != sizeY) { invalid("DCT_UWLS_Unwrapped: square maps only"); return; }
+    if (ctdm_unwrap_dct(c, 1, sizeX, CTDM_UNWRAP_REF, ImgSrc, ImgDst, 0) != CTDM_OK) return;
+    finish("DCT_UWLS_Unwrapped");
+}
+
+extern "C" void FastUnwrapping(float *ImgSrc, float *ImgDst, int sizeX, int sizeY)
+{
+    ctdm_ctx *c = default_ctx();
+    if (!c) return;
+    if (sizeX != sizeY) { invalid("FastUnwrapping: square maps only"); return; }
+    if (ctdm_unwrap_fast(c, 1, sizeX, ImgSrc, ImgDst, 0) != CTDM_OK) return;
+    finish("FastUnwrapping");
+}
+
+extern "C" void cudaGoldsteinUnwrap2D(float *cu_phi, float *cu_UnWrapPhase, int sizeX, int sizeY, int frameNumber)
+{
+    (void)frameNumber;
+    ctdm_ctx *c = default_ctx();
+    if (!c) return;
+    const long n = (long)sizeX * sizeY;
+    int8_t *chg = nullptr;
+    uint8_t *cut = nullptr;
+    if (cudaMalloc(&chg, n) != cudaSuccess || cudaMalloc(&cut, n) != cudaSuccess) {
+        cudaFree(chg);
+        set_err("cudaGoldsteinUnwrap2D: allocation failed");
+        return;
+    }
+    ctdm_goldstein(c, 1, sizeX, sizeY, cu_phi, chg, cut, cu_UnWrapPhase, nullptr, 0);
+    cudaFree(chg);
+    cudaFree(cut);
+}
+
+extern "C" void MedianFilter(float *PhaseData, float *AmpData, float *Phase_img, float *Amp_img, int nx, int ny,
+                             int nz)
+{
+    ctdm_ctx *c = default_ctx();
+    if (!c) return;
+    if (nx != ny) { invalid("MedianFilter: square slices only"); return; }
+    const long n = (long)nx * ny * nz;
+    if (ensure(c, B_TMP, sizeof(float) * 2 * n) != cudaSuccess) { set_err("MedianFilter: allocation failed"); return; }
+    float *tp = B<float>(c, B_TMP), *ta = tp + n;
+    if (cudaMemcpy(tp, Phase_img, sizeof(float) * n, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(ta, Amp_img, sizeof(float) * n, cudaMemcpyHostToDevice) != cudaSuccess) {
+        set_err("MedianFilter: upload failed");
+        return;
+    }
+    cudaError_t e = median_stack(tp, ta, nz, nx, PhaseData, AmpData, 0);
+    if (e != cudaSuccess) { cuda_fail(e, "MedianFilter"); return; }
+    finish("MedianFilter");
+}
+
+extern "C" void CopyDataArray(ctdm_cfloat *u_sp, float *phase, float *amp, int sizeX, int sizeY, int sizeZ, int numZ)
+{
+    (void)sizeZ;
+    cudaError_t e = compat_copy_data_array(reinterpret_cast<float2 *>(u_sp), phase, amp, sizeX, sizeY, numZ, 0);
+    if (e != cudaSuccess) { cuda_fail(e, "CopyDataArray"); return; }
+    finish("CopyDataArray");
+}
+
+extern "C" void EdwardSphere(ctdm_cfloat *u_sp, ctdm_cfloat *F, float *C, float fm0, float df, float AngX, float AngY,
+                             int sizeX, int sizeY, int sizeZ)
+{
+    std::vector<AngleGeom> g;
+    angle_geometry(&AngX, &AngY, 1, (double)fm0, (double)df, g);
+    const double fm02 = (double)fm0 * (double)fm0;
+    const float fm02s = (float)(((double)fm0 / df) * ((double)fm0 / df));
+    cudaError_t e = compat_edward_sphere(reinterpret_cast<const float2 *>(u_sp), reinterpret_cast<float2 *>(F), C, g[0],
+                                         (double)df, fm02, fm02s, sizeX, sizeY, sizeZ, 0);
+    if (e != cudaSuccess) { cuda_fail(e, "EdwardSphere"); return; }
+    finish("EdwardSphere");
+}
+
+extern "C" void initial_F_and_F2(float *C, ctdm_cfloat *cuF, ctdm_cfloat *cuF2, float recon_dx, int W, int H, int S)
+{
+    cudaError_t e = compat_initial_f(C, reinterpret_cast<float2 *>(cuF), reinterpret_cast<float2 *>(cuF2), recon_dx,
+                                     (long)W * H * S, 0);
+    if (e != cudaSuccess) { cuda_fail(e, "initial_F_and_F2"); return; }
+    finish("initial_F_and_F2");
+}
+
+extern "C" void est_n_3D(ctdm_cfloat *n, ctdm_cfloat *F, float recon_k2, float recon_med, int W, int H, int S)
+{
+    cudaError_t e = compat_est_n(reinterpret_cast<float2 *>(n), reinterpret_cast<const float2 *>(F), recon_k2,
+                                 recon_med, (long)W * H * S, 0);
+    if (e != cudaSuccess) { cuda_fail(e, "est_n_3D"); return; }
+    finish("est_n_3D");
+}
+
+extern "C" void modify_F_3D(ctdm_cfloat *n, ctdm_cfloat *F, float recon_k2, float recon_med, int W, int H, int S)
+{
+    cudaError_t e = compat_modify(reinterpret_cast<const float2 *>(n), reinterpret_cast<float2 *>(F), recon_k2,
+                                  recon_med, (long)W * H * S, 0);
+    if (e != cudaSuccess) { cuda_fail(e, "modify_F_3D"); return; }
+    finish("modify_F_3D");
+}
+
+extern "C" void check_F_3D(ctdm_cfloat *F, ctdm_cfloat *F2, int W, int H, int S)
+{
+    cudaError_t e = compat_check(reinterpret_cast<float2 *>(F), reinterpret_cast<const float2 *>(F2), (long)W * H * S, 0);
+    if (e != cudaSuccess) { cuda_fail(e, "check_F_3D"); return; }
+    finish("check_F_3D");
+}
+
+extern "C" void cuFFT3D(ctdm_cfloat *ImgArray, int sizeX, int sizeY, int sizeZ, int dir)
+{
+    const int dims[3] = {sizeX, sizeY, sizeZ};
+    if (ctdm_fft(ImgArray, 3, dims, 1, dir > 0, 0) != CTDM_OK) return;
+    if (dir > 0) {
+        const long n = (long)sizeX * sizeY * sizeZ;
+        cudaError_t e = scale_complex(reinterpret_cast<float2 *>(ImgArray), n, 1.0f / (float)n, false, 0);
+        if (e != cudaSuccess) { cuda_fail(e, "cuFFT3D"); return; }
+    }
+    finish("cuFFT3D");
+}
+
+extern "C" void cuFFT2D(ctdm_cfloat *ImgArray, int sizeX, int sizeY, int dir)
+{
+    const int dims[2] = {sizeX, sizeY};
+    if (ctdm_fft(ImgArray, 2, dims, 1, dir > 0, 0) != CTDM_OK) return;
+    if (dir > 0) {
+        const long n = (long)sizeX * sizeY;
+        cudaError_t e = scale_complex(reinterpret_cast<float2 *>(ImgArray), n, 1.0f / (float)n, true, 0);
+        if (e != cudaSuccess) { cuda_fail(e, "cuFFT2D"); return; }
+    }
+    finish("cuFFT2D");
+}
+
+static bool write_file(const std::string &path, const void *data, size_t bytes)
+{
+    FILE *f = fopen(path.c_str(), "wb");
+    if (!f) return false;
+    const bool ok = fwrite(data, 1, bytes, f) == bytes;
+    fclose(f);
+    return ok;
+}
+
+extern "C" void BatchRecon(float *PhaseStack, float *AmpStack, float *sampleAngleRadX, float *sampleAngleRadY,
+                           int ReconFrame)
+{
+    ctdm_ctx *c = default_ctx();
+    if (!c) return;
+    const int R = g_recon;
+    if (!ok_volume(R) || ReconFrame < 1 || ReconFrame > kMaxAngles) { invalid("BatchRecon: size unsupported"); return; }
+    const long rr = (long)R * R, r3 = rr * R;
+    // constants of BatchRecon (cTDM/HilbertTransform.cu:1839-1862)
+    const double lambda = g_wavelength_nm * 1e-9;
+    const double fm0 = g_nmed / lambda;
+    const double dx = (g_pixel_um * 1e-6) / g_mag * 1024.0 / R;
+    const double k = 2.0 * CTDM_PI_D * g_nmed / lambda;
+    const double df = 1.0 / (R * dx);
+    float *ph = nullptr, *am = nullptr;
+    float2 *U = nullptr, *F2 = nullptr, *ri = nullptr;
+    auto cleanup = [&]() { cudaFree(ph); cudaFree(am); cudaFree(U); cudaFree(F2); cudaFree(ri); };
+    if (cudaMalloc(&ph, sizeof(float) * ReconFrame * rr) != cudaSuccess ||
+        cudaMalloc(&am, sizeof(float) * ReconFrame * rr) != cudaSuccess ||
+        cudaMalloc(&U, sizeof(float2) * ReconFrame * rr) != cudaSuccess ||
+        cudaMalloc(&F2, sizeof(float2) * r3) != cudaSuccess || cudaMalloc(&ri, sizeof(float2) * r3) != cudaSuccess) {
+        cleanup();
+        set_err("BatchRecon: device allocation failed");
+        return;
+    }
+    cudaMemcpy(ph, PhaseStack, sizeof(float) * ReconFrame * rr, cudaMemcpyHostToDevice);
+    cudaMemcpy(am, AmpStack, sizeof(float) * ReconFrame * rr, cudaMemcpyHostToDevice);
+    ctdm_status st = ctdm_stack_spectra(c, ReconFrame, R, ph, am, reinterpret_cast<ctdm_cfloat *>(U), 0);
+    if (st == CTDM_OK)
+        st = ctdm_map_ewald(c, ReconFrame, R, reinterpret_cast<ctdm_cfloat *>(U), sampleAngleRadX, sampleAngleRadY, fm0,
+                            df, dx, reinterpret_cast<ctdm_cfloat *>(F2), nullptr, 0);
+    if (st == CTDM_OK)
+        st = ctdm_positivity(c, R, g_iter_time + 1, CTDM_CHECK_REF, k * k, g_nmed, reinterpret_cast<ctdm_cfloat *>(F2),
+                             nullptr, reinterpret_cast<ctdm_cfloat *>(ri), 0);
+    if (st != CTDM_OK) { cleanup(); return; }
+    std::vector<float2> host(r3);
+    if (cudaMemcpy(host.data(), ri, sizeof(float2) * r3, cudaMemcpyDeviceToHost) != cudaSuccess) {
+        cleanup();
+        set_err("BatchRecon: download failed");
+        return;
+    }
+    cleanup();
+    // export (cTDM/HilbertTransform.cu:2013-2041): raw complex64, or the real / imaginary part
+    char name[256];
+    bool ok = true;
+    if (g_recon_save == 0) {
+        snprintf(name, sizeof name, "/3D-RI-Complex_%dx%dx%d.rimap", R, R, R);
+        ok = write_file(g_save_dir + name, host.data(), sizeof(float2) * r3);
+    } else {
+        std::vector<float> part(r3);
+        for (long i = 0; i < r3; i++) part[i] = g_recon_save == 1 ? host[i].x : host[i].y;
+        snprintf(name, sizeof name, g_recon_save == 1 ? "/3D-RI-Real_%dx%dx%d.rimap" : "/3D-RI-Imag_%dx%dx%d.rimap", R,
+                 R, R);
+        ok = write_file(g_save_dir + name, part.data(), sizeof(float) * r3);
+    }
+    if (!ok) { set_err("BatchRecon: cannot write %s%s", g_save_dir.c_str(), name); return; }
+    g_err.clear();
+}

@@ -1,0 +1,222 @@
+// Batched in-shared-memory Stockham FFT over lines.
+//
+// A CTA holds B lines of length L in shared memory, element p of line b at
+// buf[b * LP + p] (LP = L plus a pad that keeps 64-bit accesses of a half-warp
+// on distinct banks).  Each radix stage loads R strided points per butterfly
+// into registers, applies the stage twiddles, runs an in-register radix-R DFT
+// and writes back in Stockham (self-sorting) order, so the output is in natural
+// order without a bit-reversal pass.  Threads are mapped b-fastest: tid -> (b =
+// tid % B, t = tid / B), T threads per line.
+//
+// Conventions (cuFFT C2C as used by the reference, cTDM/FFT.cu:697-838):
+// forward exp(-2 pi i k n / L), inverse exp(+2 pi i k n / L), both unnormalised.
+// Twiddles come from a per-length table tw[e] = exp(-2 pi i e / L) computed in
+// double on the host.
+#pragma once
+#include "ctdm_common.cuh"
+
+namespace fftl {
+
+// ---------------------------------------------------------------- radix DFTs
+template <bool INV>
+__device__ __forceinline__ void dft2(float2 &a, float2 &b)
+{
+    float2 t = a;
+    a = cadd(t, b);
+    b = csub(t, b);
+}
+
+template <bool INV>
+__device__ __forceinline__ void dft4(float2 &a0, float2 &a1, float2 &a2, float2 &a3)
+{
+    float2 t0 = cadd(a0, a2), t1 = csub(a0, a2), t2 = cadd(a1, a3), t3 = cmul_mi<INV>(csub(a1, a3));
+    a0 = cadd(t0, t2);
+    a2 = csub(t0, t2);
+    a1 = cadd(t1, t3);
+    a3 = csub(t1, t3);
+}
+
+// exp(-+ 2 pi i k / 8) for k = 1, 3
+template <bool INV>
+__device__ __forceinline__ float2 w8(float2 a, int k)
+{
+    const float h = 0.70710678118654752440f;
+    // forward W8^1 = (h, -h), W8^3 = (-h, -h); inverse conjugates
+    float2 w = (k == 1) ? make_float2(h, INV ? h : -h) : make_float2(-h, INV ? h : -h);
+    return cmul(a, w);
+}
+
+template <bool INV>
+__device__ __forceinline__ void dft8(float2 *a)
+{
+    // radix-2 decimation in time over two radix-4 DFTs
+    float2 e0 = a[0], e1 = a[2], e2 = a[4], e3 = a[6];
+    float2 o0 = a[1], o1 = a[3], o2 = a[5], o3 = a[7];
+    dft4<INV>(e0, e1, e2, e3);
+    dft4<INV>(o0, o1, o2, o3);
+    o1 = w8<INV>(o1, 1);
+    o2 = cmul_mi<INV>(o2);
+    o3 = w8<INV>(o3, 3);
+    a[0] = cadd(e0, o0); a[4] = csub(e0, o0);
+    a[1] = cadd(e1, o1); a[5] = csub(e1, o1);
+    a[2] = cadd(e2, o2); a[6] = csub(e2, o2);
+    a[3] = cadd(e3, o3); a[7] = csub(e3, o3);
+}
+
+template <bool INV>
+__device__ __forceinline__ void dft16(float2 *a)
+{
+    // cos(2 pi k/16), sin(2 pi k/16), k = 0..7
+    const float c[8] = {1.0f, 0.92387953251128675613f, 0.70710678118654752440f, 0.38268343236508977173f,
+                        0.0f, -0.38268343236508977173f, -0.70710678118654752440f, -0.92387953251128675613f};
+    const float s[8] = {0.0f, 0.38268343236508977173f, 0.70710678118654752440f, 0.92387953251128675613f,
+                        1.0f, 0.92387953251128675613f, 0.70710678118654752440f, 0.38268343236508977173f};
+    float2 e[8], o[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) { e[k] = a[2 * k]; o[k] = a[2 * k + 1]; }
+    dft8<INV>(e);
+    dft8<INV>(o);
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        float2 w = make_float2(c[k], INV ? s[k] : -s[k]);
+        float2 t = (k == 0) ? o[k] : cmul(o[k], w);
+        a[k] = cadd(e[k], t);
+        a[k + 8] = csub(e[k], t);
+    }
+}
+
+template <bool INV>
+__device__ __forceinline__ void dft3(float2 *a)
+{
+    const float s3 = 0.86602540378443864676f;
+    float2 t1 = cadd(a[1], a[2]);
+    float2 d = csub(a[1], a[2]);
+    // forward: (a1 - a2) * (-i s3); inverse: * (+i s3)
+    float2 t2 = INV ? make_float2(-s3 * d.y, s3 * d.x) : make_float2(s3 * d.y, -s3 * d.x);
+    float2 m = make_float2(a[0].x - 0.5f * t1.x, a[0].y - 0.5f * t1.y);
+    a[0] = cadd(a[0], t1);
+    a[1] = cadd(m, t2);
+    a[2] = csub(m, t2);
+}
+
+template <int R, bool INV>
+__device__ __forceinline__ void dftR(float2 *a)
+{
+    if constexpr (R == 2) dft2<INV>(a[0], a[1]);
+    else if constexpr (R == 3) dft3<INV>(a);
+    else if constexpr (R == 4) dft4<INV>(a[0], a[1], a[2], a[3]);
+    else if constexpr (R == 8) dft8<INV>(a);
+    else if constexpr (R == 16) dft16<INV>(a);
+}
+
+// ---------------------------------------------------------------- plans
+// Per length: radix sequence, lines per CTA (B) and threads per line (T).
+template <int L> struct Plan;
+#define FFTL_PLAN(LL, BB, TT, ...)                                       \
+    template <> struct Plan<LL> {                                       \
+        static constexpr int B = BB, T = TT;                            \
+        static constexpr int PAD = (BB >= 16) ? 1 : (16 / BB);          \
+        static constexpr int LP = LL + PAD;                             \
+        static constexpr int THREADS = BB * TT;                         \
+        template <bool INV>                                             \
+        __device__ static void run(float2 *buf, const float2 *tw);      \
+    };
+FFTL_PLAN(16, 64, 4, 4, 4)
+FFTL_PLAN(32, 64, 4, 8, 4)
+FFTL_PLAN(64, 32, 8, 8, 8)
+FFTL_PLAN(128, 32, 8, 16, 8)
+FFTL_PLAN(256, 16, 16, 16, 16)
+FFTL_PLAN(384, 32, 8, 16, 8, 3)
+FFTL_PLAN(512, 16, 16, 8, 8, 8)
+FFTL_PLAN(768, 16, 16, 16, 16, 3)
+FFTL_PLAN(1024, 8, 32, 16, 16, 4)
+FFTL_PLAN(1536, 8, 32, 16, 16, 3, 2)
+FFTL_PLAN(2048, 4, 64, 16, 16, 8)
+#undef FFTL_PLAN
+
+// One Stockham stage of radix R with span NS (product of the earlier radices).
+template <int L, int B, int T, int LP, bool INV, int NS, int R>
+__device__ __forceinline__ void stage(float2 *buf, const float2 *__restrict__ tw, int b, int t)
+{
+    constexpr int NB = L / R;       // butterflies per line
+    constexpr int PER = NB / T;     // butterflies per thread
+    static_assert(NB % T == 0, "threads per line must divide the butterfly count");
+    float2 v[PER][R];
+    float2 *line = buf + b * LP;
+#pragma unroll
+    for (int q = 0; q < PER; q++) {
+        const int j = t + T * q;
+#pragma unroll
+        for (int r = 0; r < R; r++) v[q][r] = line[j + r * NB];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < PER; q++) {
+        const int j = t + T * q;
+        const int k = j % NS;
+        if constexpr (NS > 1) {
+#pragma unroll
+            for (int r = 1; r < R; r++) {
+                float2 w = __ldg(&tw[r * k * (L / (NS * R))]);
+                v[q][r] = INV ? cmulc(v[q][r], w) : cmul(v[q][r], w);
+            }
+        }
+        dftR<R, INV>(v[q]);
+        const int base = (j / NS) * NS * R + k;
+#pragma unroll
+        for (int r = 0; r < R; r++) line[base + r * NS] = v[q][r];
+    }
+    __syncthreads();
+}
+
+template <int L, int B, int T, int LP, bool INV, int NS, int R, int... REST>
+__device__ __forceinline__ void stages(float2 *buf, const float2 *__restrict__ tw, int b, int t)
+{
+    stage<L, B, T, LP, INV, NS, R>(buf, tw, b, t);
+    if constexpr (sizeof...(REST) > 0) stages<L, B, T, LP, INV, NS * R, REST...>(buf, tw, b, t);
+}
+
+#define FFTL_RUN(LL, ...)                                                                  \
+    template <bool INV>                                                                   \
+    __device__ __forceinline__ void Plan<LL>::run(float2 *buf, const float2 *tw)          \
+    {                                                                                     \
+        const int b = threadIdx.x % B, t = threadIdx.x / B;                              \
+        stages<LL, B, T, LP, INV, 1, __VA_ARGS__>(buf, tw, b, t);                         \
+    }
+FFTL_RUN(16, 4, 4)
+FFTL_RUN(32, 8, 4)
+FFTL_RUN(64, 8, 8)
+FFTL_RUN(128, 16, 8)
+FFTL_RUN(256, 16, 16)
+FFTL_RUN(384, 16, 8, 3)
+FFTL_RUN(512, 8, 8, 8)
+FFTL_RUN(768, 16, 16, 3)
+FFTL_RUN(1024, 16, 16, 4)
+FFTL_RUN(1536, 16, 16, 3, 2)
+FFTL_RUN(2048, 16, 16, 8)
+#undef FFTL_RUN
+
+template <int L>
+__host__ __device__ constexpr size_t smem_bytes()
+{
+    return sizeof(float2) * Plan<L>::B * Plan<L>::LP;
+}
+
+}  // namespace fftl
+
+// Dispatch a templated launcher over the supported line lengths.
+#define CTDM_DISPATCH_L(Lrt, FN, ...)                  \
+    switch (Lrt) {                                     \
+    case 16: return FN<16>(__VA_ARGS__);               \
+    case 32: return FN<32>(__VA_ARGS__);               \
+    case 64: return FN<64>(__VA_ARGS__);               \
+    case 128: return FN<128>(__VA_ARGS__);             \
+    case 256: return FN<256>(__VA_ARGS__);             \
+    case 384: return FN<384>(__VA_ARGS__);             \
+    case 512: return FN<512>(__VA_ARGS__);             \
+    case 768: return FN<768>(__VA_ARGS__);             \
+    case 1024: return FN<1024>(__VA_ARGS__);           \
+    case 1536: return FN<1536>(__VA_ARGS__);           \
+    case 2048: return FN<2048>(__VA_ARGS__);           \
+    default: return cudaErrorInvalidValue;             \
+    }

@@ -1,0 +1,226 @@
+// Least-squares phase unwrapping by a DCT Poisson solve
+// (y-h-Lin/cTDM DCT_UWLS_Unwrapped, cTDM/DCT_Unwrapping.cu:10-59).
+//
+// The reference runs 14 launches and 4 cuFFT calls per map: wrapped
+// derivatives (NumericDerivative1 :336), divergence (SumDerivative :394), a
+// row DCT-II through a 2M-point FFT of the mirrored row (float2cufft :144,
+// countFDCT :202), a transpose (:179), the same for columns, the Poisson divide
+// (devConstant :300) and the inverse (countIDCT :218, cufft2float :164) twice.
+// Here it is three line passes:
+//   rows:    wrapped Laplacian (fused load) -> mirror -> FFT_2M -> DCT-II
+//   columns: mirror -> FFT_2M -> DCT-II -> divide -> IDCT build -> IFFT_2M
+//   rows:    IDCT build -> IFFT_2M -> real part
+// The inverse keeps the reference's twiddle on the mirrored half ((i+1) pi/2M,
+// mode 0) or uses the exact DCT-III (i pi/2M, mode 1).
+#include <cmath>
+
+#include "fft_line.cuh"
+#include "kernels_front.cuh"
+
+namespace ctdm {
+
+using fftl::Plan;
+
+// NumericDerivative1 wrap: t - 2 pi sign(t) floor(|pi sign(t) + t| / 2 pi),
+// evaluated in double as the reference expression is; it is exactly t when
+// |t| < pi, so the double path only runs on wrapped differences.
+__device__ __forceinline__ float wrap_grad(float t)
+{
+    if (fabsf(t) < 3.14159f) return t;
+    const double s = t > 0.f ? 1.0 : (t < 0.f ? -1.0 : 0.0);
+    const double td = (double)t;
+    const double q = floor(fabs(__dadd_rn(CTDM_PI_D * s, td)) / (CTDM_PI_D * 2));
+    return (float)__dsub_rn(td, 2 * CTDM_PI_D * s * q);
+}
+
+__device__ __forceinline__ float lap_at(const float *__restrict__ phi, int x, int y, int M)
+{
+    const long i = x + (long)M * y;
+    const float c = phi[i];
+    // SumDerivative (:394-417): (gx(x) - gx(x-1)) + (gy(y) - gy(y-1)) with zero edges
+    const float c1 = (x == M - 1) ? 0.f : wrap_grad(phi[i + 1] - c);
+    float c2 = 0.f;
+    if (x > 0) {
+        const float l = phi[i - 1];
+        c2 = wrap_grad(c - l);
+    }
+    const float c3 = (y == M - 1) ? 0.f : wrap_grad(phi[i + M] - c);
+    float c4 = 0.f;
+    if (y > 0) {
+        const float u = phi[i - M];
+        c4 = wrap_grad(c - u);
+    }
+    return (c1 - c2) + (c3 - c4);
+}
+
+// countFDCT (:202-216): X_k from the 2M-point transform Y of the mirrored line.
+__device__ __forceinline__ float dct_from_fft(float2 Y, int k, const float2 *__restrict__ dtw, float dT)
+{
+    if (k == 0) return Y.x * dT * 0.70710678118654752440f;
+    const float2 w = __ldg(&dtw[k]);
+    return (Y.x * w.x + Y.y * w.y) * dT;
+}
+
+// countIDCT (:218-246) element p of the 2M-point input built from X[0..M).
+__device__ __forceinline__ float2 idct_input(const float *X, int p, int M, const float2 *__restrict__ dtw, float dT,
+                                             int mode)
+{
+    if (p < M) {
+        const float2 w = __ldg(&dtw[p]);
+        float v = X[p] * dT;
+        float2 r = make_float2(w.x * v, w.y * v);
+        if (p == 0) r = make_float2(r.x * 1.41421356237309504880f, r.y * 1.41421356237309504880f);
+        return r;
+    }
+    const int i = p - M;
+    if (i == 0) return make_float2(0.f, 0.f);
+    const float2 w = __ldg(&dtw[mode == 0 ? i + 1 : i]);
+    const float v2 = X[M - i] * dT;
+    return make_float2(w.y * v2, -w.x * v2);
+}
+
+// Pass 1: rows.  phi: A x M x M; T: A x M x M (row DCT coefficients, [a][y][kx]).
+template <int L2>
+__global__ void __launch_bounds__(Plan<L2>::THREADS) dct_rows_kernel(const float *__restrict__ phi, float *T,
+                                                                    long nlines, int M, const float2 *__restrict__ dtw,
+                                                                    const float2 *__restrict__ tw)
+{
+    using P = Plan<L2>;
+    extern __shared__ float4 smem4[];
+    float2 *buf = reinterpret_cast<float2 *>(smem4);
+    const long line0 = (long)blockIdx.x * P::B;
+    for (int e = threadIdx.x; e < P::B * M; e += P::THREADS) {
+        const int b = e / M, x = e - b * M;
+        const long l = line0 + b;
+        float v = 0.f;
+        if (l < nlines) {
+            const long a = l / M;
+            const int y = (int)(l % M);
+            v = lap_at(phi + a * (long)M * M, x, y, M);
+        }
+        buf[b * P::LP + x] = make_float2(v, 0.f);
+        buf[b * P::LP + (L2 - 1 - x)] = make_float2(v, 0.f);
+    }
+    __syncthreads();
+    P::template run<false>(buf, tw);
+    const float dT = 1.0f / sqrtf((float)L2);
+    for (int e = threadIdx.x; e < P::B * M; e += P::THREADS) {
+        const int b = e / M, k = e - b * M;
+        const long l = line0 + b;
+        if (l < nlines) T[l * M + k] = dct_from_fft(buf[b * P::LP + k], k, dtw, dT);
+    }
+}
+
+// Pass 2: columns.  Line l = kx + M*a, element y at T[a*M*M + y*M + kx].
+template <int L2>
+__global__ void __launch_bounds__(Plan<L2>::THREADS) dct_cols_kernel(float *T, long nlines, int M, int mode,
+                                                                    const float2 *__restrict__ dtw,
+                                                                    const float *__restrict__ eig,
+                                                                    const float2 *__restrict__ tw)
+{
+    using P = Plan<L2>;
+    extern __shared__ float4 smem4[];
+    float2 *buf = reinterpret_cast<float2 *>(smem4);
+    float *X = reinterpret_cast<float *>(buf + P::B * P::LP);   // B x M
+    const long line0 = (long)blockIdx.x * P::B;
+    const int b = threadIdx.x % P::B, t = threadIdx.x / P::B;
+    const long l = line0 + b;
+    const bool ok = l < nlines;
+    const int kx = ok ? (int)(l % M) : 0;
+    const long a = ok ? l / M : 0;
+    float *col = T + a * (long)M * M + kx;
+    for (int y = t; y < M; y += P::T) {
+        const float v = ok ? col[(long)y * M] : 0.f;
+        buf[b * P::LP + y] = make_float2(v, 0.f);
+        buf[b * P::LP + (L2 - 1 - y)] = make_float2(v, 0.f);
+    }
+    __syncthreads();
+    P::template run<false>(buf, tw);
+    const float dT = 1.0f / sqrtf((float)L2);
+    const float ex = __ldg(&eig[kx]);
+    for (int ky = t; ky < M; ky += P::T) {
+        float v = dct_from_fft(buf[b * P::LP + ky], ky, dtw, dT);
+        // devConstant (:300-311): / (2cos(4 pi i/(4M-1)) + 2cos(4 pi j/(4M-1)) - 4), (0,0) -> 0;
+        // the denominator is -(4 sin^2(2 pi i/(4M-1)) + 4 sin^2(2 pi j/(4M-1))), free of cancellation
+        if (kx == 0 && ky == 0) v = 0.f;
+        else v = v / (-(ex + __ldg(&eig[ky])));
+        X[b * M + ky] = v;
+    }
+    __syncthreads();
+    for (int p = t; p < L2; p += P::T) buf[b * P::LP + p] = idct_input(X + b * M, p, M, dtw, dT, mode);
+    __syncthreads();
+    P::template run<true>(buf, tw);
+    if (!ok) return;
+    for (int y = t; y < M; y += P::T) col[(long)y * M] = buf[b * P::LP + y].x;
+}
+
+// Pass 3: rows inverse.  T: [a][y][kx] -> out [a][y][x].
+template <int L2>
+__global__ void __launch_bounds__(Plan<L2>::THREADS) dct_rows_inv_kernel(const float *__restrict__ T, float *out,
+                                                                        long nlines, int M, int mode,
+                                                                        const float2 *__restrict__ dtw,
+                                                                        const float2 *__restrict__ tw)
+{
+    using P = Plan<L2>;
+    extern __shared__ float4 smem4[];
+    float2 *buf = reinterpret_cast<float2 *>(smem4);
+    float *X = reinterpret_cast<float *>(buf + P::B * P::LP);
+    const long line0 = (long)blockIdx.x * P::B;
+    for (int e = threadIdx.x; e < P::B * M; e += P::THREADS) {
+        const int b = e / M, k = e - b * M;
+        const long l = line0 + b;
+        X[b * M + k] = (l < nlines) ? T[l * M + k] : 0.f;
+    }
+    __syncthreads();
+    const float dT = 1.0f / sqrtf((float)L2);
+    for (int e = threadIdx.x; e < P::B * L2; e += P::THREADS) {
+        const int b = e / L2, p = e - b * L2;
+        buf[b * P::LP + p] = idct_input(X + b * M, p, M, dtw, dT, mode);
+    }
+    __syncthreads();
+    P::template run<true>(buf, tw);
+    for (int e = threadIdx.x; e < P::B * M; e += P::THREADS) {
+        const int b = e / M, x = e - b * M;
+        const long l = line0 + b;
+        if (l < nlines) out[l * M + x] = buf[b * P::LP + x].x;
+    }
+}
+
+template <int L2, class K>
+static cudaError_t set_smem2(K kernel, size_t smem)
+{
+    if (smem > 48 * 1024)
+        return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    return cudaSuccess;
+}
+
+template <int L2>
+static cudaError_t dct_launch(const float *phi, float *out, float *T, int A, int M, int mode, cudaStream_t s)
+{
+    using P = Plan<L2>;
+    const long nl = (long)A * M;
+    const unsigned grid = (unsigned)((nl + P::B - 1) / P::B);
+    const size_t smem1 = fftl::smem_bytes<L2>();
+    const size_t smem2 = smem1 + sizeof(float) * P::B * M;
+    const float2 *dtw = dct_twiddles(M);
+    const float2 *tw = twiddles(L2);
+    cudaError_t e = set_smem2<L2>(dct_rows_kernel<L2>, smem1);
+    if (e != cudaSuccess) return e;
+    dct_rows_kernel<L2><<<grid, P::THREADS, smem1, s>>>(phi, T, nl, M, dtw, tw); note_launch();
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    e = set_smem2<L2>(dct_cols_kernel<L2>, smem2);
+    if (e != cudaSuccess) return e;
+    dct_cols_kernel<L2><<<grid, P::THREADS, smem2, s>>>(T, nl, M, mode, dtw, dct_eigen(M), tw); note_launch();
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    e = set_smem2<L2>(dct_rows_inv_kernel<L2>, smem2);
+    if (e != cudaSuccess) return e;
+    dct_rows_inv_kernel<L2><<<grid, P::THREADS, smem2, s>>>(T, out, nl, M, mode, dtw, tw); note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t dct_unwrap(const float *phi, float *out, float *T, int A, int M, int mode, cudaStream_t s)
+{
+    CTDM_DISPATCH_L(2 * M, dct_launch, phi, out, T, A, M, mode, s)
+}
+
+}  // namespace ctdm

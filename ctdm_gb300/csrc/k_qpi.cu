@@ -1,0 +1,272 @@
+// Off-axis phase retrieval, QPI Algorithm A (y-h-Lin/cTDM extractQPI_AlgorithmA,
+// cTDM/HilbertTransform.cu:1546-1585, get1stOrder_new :3566-3586, calcWrapPhase
+// :3618-3639, scaleFFT2D cTDM/FFT.cu:853-868).
+//
+// The reference transforms the whole N x N hologram, swaps quadrants, copies an
+// M x M window around the carrier, swaps again and inverse-transforms.  Only the
+// M window columns and rows of the forward spectrum are ever used, so the
+// forward transform is pruned: a row pass computes full N-point row transforms
+// (two real rows packed in one complex transform) and keeps the M window
+// columns; a column pass transforms those columns and keeps the M window rows,
+// masks to the +-radius box and writes them at their ifftshifted positions.
+// The M x M inverse transform follows (rows, then columns with the 1/M^2 scale,
+// conjugate and the phase/amplitude epilogue fused).
+#include <cmath>
+
+#include "fft_line.cuh"
+#include "kernels_front.cuh"
+
+namespace ctdm {
+
+using fftl::Plan;
+
+template <int L, class K>
+static cudaError_t set_smem(K kernel, size_t smem)
+{
+    if (smem > 48 * 1024)
+        return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    return cudaSuccess;
+}
+
+// ------------------------------------------------------------ carrier search
+// obtainRadius (cTDM/HilbertTransform.cu:3425-3455): argmax of |X| over rows
+// j >= start of the quadrant-swapped spectrum, first maximum in raster order.
+// Packed key: (bits of |X|^2) << 32 | ~(raster index) so that atomicMax picks the
+// largest magnitude and, among equal ones, the smallest index.
+__global__ void carrier_argmax_kernel(const float2 *__restrict__ spec, int N, int start, unsigned long long *key)
+{
+    unsigned long long best = 0ull;
+    const long total = (long)(N - start) * N;
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
+        const int js = start + (int)(e / N), is = (int)(e % N);
+        const int iu = (is + N / 2) % N, ju = (js + N / 2) % N;
+        const float2 v = spec[iu + (long)N * ju];
+        const float m = v.x * v.x + v.y * v.y;
+        const unsigned idx = (unsigned)(is + N * js);
+        const unsigned long long k = ((unsigned long long)__float_as_uint(m) << 32) | (unsigned long long)(~idx);
+        if (k > best) best = k;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long other = __shfl_xor_sync(0xffffffffu, best, o);
+        if (other > best) best = other;
+    }
+    if ((threadIdx.x & 31) == 0) atomicMax(key, best);
+}
+
+__global__ void carrier_finish_kernel(const unsigned long long *key, int N, int *carrier)
+{
+    const unsigned idx = ~(unsigned)(*key & 0xffffffffull);
+    const int r = (int)(idx / (unsigned)N), c = (int)(idx % (unsigned)N);
+    carrier[0] = r;
+    carrier[1] = c;
+    carrier[2] = abs(r - N / 2) / 3;
+}
+
+__global__ void real_to_complex_kernel(const float *__restrict__ in, float2 *out, long n)
+{
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        out[i] = make_float2(in[i], 0.f);
+}
+
+cudaError_t qpi_find_carrier(const float *bg, int N, float2 *scratch, unsigned long long *key, int *carrier,
+                             cudaStream_t s)
+{
+    const long n2 = (long)N * N;
+    real_to_complex_kernel<<<1024, 256, 0, s>>>(bg, scratch, n2); note_launch();
+    cudaError_t e = fft_rows(scratch, N, N, false, s);
+    if (e == cudaSuccess) e = fft_cols(scratch, N, N, N, 0, N, false, s);
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(key, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return e;
+    carrier_argmax_kernel<<<256, 256, 0, s>>>(scratch, N, (600 * N) / 1024, key); note_launch();
+    carrier_finish_kernel<<<1, 1, 0, s>>>(key, N, carrier); note_launch();
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------ forward row pass
+// holo: A holograms N x N (float, [a][y][x]); T1: A x N x M complex ([a][y][m]).
+// Column m of the window is spectrum column k = (c - N/2 + m - M/2) mod N of the
+// unshifted transform (the quadrant swap folded into the index).
+template <int N>
+__global__ void __launch_bounds__(Plan<N>::THREADS) qpi_rows_kernel(const float *__restrict__ holo, float2 *T1,
+                                                                   const int *__restrict__ carrier, long npairs,
+                                                                   int M, const float2 *__restrict__ tw)
+{
+    using P = Plan<N>;
+    extern __shared__ float4 smem4[];
+    float2 *buf = reinterpret_cast<float2 *>(smem4);
+    const long pair0 = (long)blockIdx.x * P::B;   // pair q covers rows 2q, 2q+1 of the stack
+    for (int e = threadIdx.x; e < P::B * N; e += P::THREADS) {
+        const int b = e / N, p = e - b * N;
+        const long q = pair0 + b;
+        float2 v = make_float2(0.f, 0.f);
+        if (q < npairs) v = make_float2(__ldcs(&holo[(2 * q) * N + p]), __ldcs(&holo[(2 * q + 1) * N + p]));
+        buf[b * P::LP + p] = v;
+    }
+    __syncthreads();
+    P::template run<false>(buf, tw);
+    const int c = carrier[1];
+    for (int e = threadIdx.x; e < P::B * M; e += P::THREADS) {
+        const int b = e / M, m = e - b * M;
+        const long q = pair0 + b;
+        if (q >= npairs) continue;
+        int k = (c - N / 2 + m - M / 2) % N;
+        if (k < 0) k += N;
+        const float2 z1 = buf[b * P::LP + k];
+        const float2 z2 = buf[b * P::LP + ((N - k) % N)];
+        // two real rows from one complex transform: Xa = (Z_k + conj Z_{N-k})/2,
+        // Xb = (Z_k - conj Z_{N-k})/(2i)
+        const float2 xa = make_float2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
+        const float2 xb = make_float2(0.5f * (z1.y + z2.y), -0.5f * (z1.x - z2.x));
+        T1[(2 * q) * M + m] = xa;
+        T1[(2 * q + 1) * M + m] = xb;
+    }
+}
+
+// ------------------------------------------------------------ forward column pass
+// Lines l = m + M*a, element y at T1[a*N*M + y*M + m].  Keeps window rows
+// ky = (r - N/2 + j - M/2) mod N, masks to |offsets| <= radius and stores at the
+// ifftshifted position of S (A x M x M).
+template <int N>
+__global__ void __launch_bounds__(Plan<N>::THREADS) qpi_cols_kernel(const float2 *__restrict__ T1, float2 *S,
+                                                                   const int *__restrict__ carrier, long nlines,
+                                                                   int M, const float2 *__restrict__ tw)
+{
+    using P = Plan<N>;
+    extern __shared__ float4 smem4[];
+    float2 *buf = reinterpret_cast<float2 *>(smem4);
+    const long line0 = (long)blockIdx.x * P::B;
+    const int b = threadIdx.x % P::B, t = threadIdx.x / P::B;
+    const long l = line0 + b;
+    const bool ok = l < nlines;
+    const int m = ok ? (int)(l % M) : 0;
+    const long a = ok ? l / M : 0;
+    const float2 *src = T1 + a * (long)N * M + m;
+    for (int p = t; p < N; p += P::T) buf[b * P::LP + p] = ok ? __ldcs(&src[(long)p * M]) : make_float2(0.f, 0.f);
+    __syncthreads();
+    P::template run<false>(buf, tw);
+    if (!ok) return;
+    const int r = carrier[0], rad = carrier[2];
+    const int ox = m - M / 2;
+    const int io = (m + M / 2) % M;
+    float2 *dst = S + a * (long)M * M;
+    for (int j = t; j < M; j += P::T) {
+        const int oy = j - M / 2;
+        int ky = (r - N / 2 + oy) % N;
+        if (ky < 0) ky += N;
+        float2 v = buf[b * P::LP + ky];
+        if (abs(ox) > rad || abs(oy) > rad) v = make_float2(0.f, 0.f);
+        dst[(long)((j + M / 2) % M) * M + io] = v;
+    }
+}
+
+// ------------------------------------------------------------ inverse column pass
+// Lines are the M columns of each M x M spectrum (rows already inverse
+// transformed).  Epilogue: x 1/M^2 and conjugate (scaleFFT2D), then either store
+// the complex field (background) or the phase arg BG - arg SP and amplitude
+// |SP|/|BG| with NaN/inf -> 0 (calcWrapPhase).
+template <int M>
+__global__ void __launch_bounds__(Plan<M>::THREADS) qpi_final_kernel(const float2 *__restrict__ S, long nlines,
+                                                                    float2 *field_out, const float2 *__restrict__ bgf,
+                                                                    long bg_stride, float *phase, float *amp,
+                                                                    const float2 *__restrict__ tw)
+{
+    using P = Plan<M>;
+    extern __shared__ float4 smem4[];
+    float2 *buf = reinterpret_cast<float2 *>(smem4);
+    const long line0 = (long)blockIdx.x * P::B;
+    const int b = threadIdx.x % P::B, t = threadIdx.x / P::B;
+    const long l = line0 + b;
+    const bool ok = l < nlines;
+    const int x = ok ? (int)(l % M) : 0;
+    const long a = ok ? l / M : 0;
+    const long mm = (long)M * M;
+    const float2 *src = S + a * mm + x;
+    for (int p = t; p < M; p += P::T) buf[b * P::LP + p] = ok ? src[(long)p * M] : make_float2(0.f, 0.f);
+    __syncthreads();
+    P::template run<true>(buf, tw);
+    if (!ok) return;
+    const float sc = 1.0f / (float)mm;
+    for (int y = t; y < M; y += P::T) {
+        const float2 raw = buf[b * P::LP + y];
+        const float2 v = make_float2(raw.x * sc, -raw.y * sc);
+        const long o = a * mm + x + (long)M * y;
+        if (field_out) {
+            field_out[o] = v;
+        } else {
+            const float2 g = bgf[a * bg_stride + x + (long)M * y];
+            float ph = atan2f(g.y, g.x) - atan2f(v.y, v.x);
+            if (isnan(ph) || isinf(ph)) ph = 0.f;
+            float am = sqrtf(v.x * v.x + v.y * v.y) / sqrtf(g.x * g.x + g.y * g.y);
+            if (isnan(am) || isinf(am)) am = 0.f;
+            phase[o] = ph;
+            amp[o] = am;
+        }
+    }
+}
+
+template <int N>
+static cudaError_t qpi_fwd_launch(const float *holo, int A, int M, const int *carrier, float2 *T1, float2 *S,
+                                  cudaStream_t s)
+{
+    using P = Plan<N>;
+    const size_t smem = fftl::smem_bytes<N>();
+    const long npairs = (long)A * N / 2;
+    cudaError_t e = set_smem<N>(qpi_rows_kernel<N>, smem);
+    if (e != cudaSuccess) return e;
+    qpi_rows_kernel<N><<<(unsigned)((npairs + P::B - 1) / P::B), P::THREADS, smem, s>>>(holo, T1, carrier, npairs, M,
+                                                                                        twiddles(N)); note_launch();
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    const long nl = (long)A * M;
+    e = set_smem<N>(qpi_cols_kernel<N>, smem);
+    if (e != cudaSuccess) return e;
+    qpi_cols_kernel<N><<<(unsigned)((nl + P::B - 1) / P::B), P::THREADS, smem, s>>>(T1, S, carrier, nl, M,
+                                                                                   twiddles(N)); note_launch();
+    return cudaGetLastError();
+}
+
+template <int M>
+static cudaError_t qpi_inv_launch(float2 *S, int A, float2 *field_out, const float2 *bgf, long bg_stride,
+                                  float *phase, float *amp, cudaStream_t s)
+{
+    using P = Plan<M>;
+    cudaError_t e = fft_rows(S, M, (long)A * M, true, s);
+    if (e != cudaSuccess) return e;
+    const size_t smem = fftl::smem_bytes<M>();
+    e = set_smem<M>(qpi_final_kernel<M>, smem);
+    if (e != cudaSuccess) return e;
+    const long nl = (long)A * M;
+    qpi_final_kernel<M><<<(unsigned)((nl + P::B - 1) / P::B), P::THREADS, smem, s>>>(S, nl, field_out, bgf, bg_stride,
+                                                                                    phase, amp, twiddles(M)); note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t qpi_forward_window(const float *holo, int A, int N, int M, const int *carrier, float2 *T1, float2 *S,
+                               cudaStream_t s)
+{
+    CTDM_DISPATCH_L(N, qpi_fwd_launch, holo, A, M, carrier, T1, S, s)
+}
+
+cudaError_t qpi_inverse_window(float2 *S, int A, int M, float2 *field_out, const float2 *bgf, long bg_stride,
+                               float *phase, float *amp, cudaStream_t s)
+{
+    CTDM_DISPATCH_L(M, qpi_inv_launch, S, A, field_out, bgf, bg_stride, phase, amp, s)
+}
+
+}  // namespace ctdm
+
+namespace ctdm {
+__global__ void set_carrier_kernel(int *carrier, int r, int c, int rad)
+{
+    carrier[0] = r;
+    carrier[1] = c;
+    carrier[2] = rad;
+}
+
+cudaError_t set_carrier(int *carrier, int r, int c, int rad, cudaStream_t s)
+{
+    set_carrier_kernel<<<1, 1, 0, s>>>(carrier, r, c, rad); note_launch();
+    return cudaGetLastError();
+}
+}  // namespace ctdm

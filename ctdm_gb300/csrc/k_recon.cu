@@ -1,0 +1,435 @@
+// Fourier-domain ODT kernels: batched line transforms, Ewald-cap mapping and
+// the fused positivity-loop passes over a complex64 R^3 volume.
+//
+// Reference path (y-h-Lin/cTDM): BatchRecon (cTDM/HilbertTransform.cu:1825-2047)
+// calls EdwardSphere/fillEdwardSphere (cTDM/Recon_kernel.cu:171-229),
+// Initial_F_F2 (:253-276), cuFFT3D (cTDM/FFT.cu:807-838), calculate_n3D
+// (:305-342), Modify_F3D (:370-383) and check_F3D (:396-412) as separate
+// full-volume passes.  Here one loop body {modify, FFT3, replace, IFFT3, est_n}
+// is four line passes over HBM:
+//   x pass: IFFT_x, 1/R^3, est_n, modify, FFT_x   (the real-space operators)
+//   y pass: FFT_y
+//   z pass: FFT_z, replace with the measured data, IFFT_z   (k-space operator)
+//   y pass: IFFT_y
+// The mapping kernel owns whole z columns, so it accumulates the Ewald samples,
+// forms F2 = F/C/dx and applies the first z inverse transform in shared memory.
+#include <cmath>
+
+#include "fft_line.cuh"
+#include "kernels.cuh"
+#include "point_ops.cuh"
+
+namespace ctdm {
+
+using fftl::Plan;
+
+// ------------------------------------------------------------ load / store
+// Contiguous lines: line l occupies data[l*L .. l*L+L).
+template <int L>
+__device__ __forceinline__ void load_rows(float2 *buf, const float2 *__restrict__ src, long line0, long nlines)
+{
+    using P = Plan<L>;
+    const float4 *s4 = reinterpret_cast<const float4 *>(src);
+#pragma unroll 4
+    for (int e = threadIdx.x; e < P::B * L / 2; e += P::THREADS) {
+        const int b = (2 * e) / L, p = 2 * e - b * L;
+        const long l = line0 + b;
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (l < nlines) v = __ldcs(&s4[(l * L + p) / 2]);
+        buf[b * P::LP + p] = make_float2(v.x, v.y);
+        buf[b * P::LP + p + 1] = make_float2(v.z, v.w);
+    }
+}
+
+template <int L>
+__device__ __forceinline__ void store_rows(float2 *dst, const float2 *buf, long line0, long nlines)
+{
+    using P = Plan<L>;
+    float4 *d4 = reinterpret_cast<float4 *>(dst);
+#pragma unroll 4
+    for (int e = threadIdx.x; e < P::B * L / 2; e += P::THREADS) {
+        const int b = (2 * e) / L, p = 2 * e - b * L;
+        const long l = line0 + b;
+        if (l < nlines) {
+            float2 a = buf[b * P::LP + p], c = buf[b * P::LP + p + 1];
+            __stcs(&d4[(l * L + p) / 2], make_float4(a.x, a.y, c.x, c.y));
+        }
+    }
+}
+
+// Strided lines: element p of line l at (l % nx) + (l / nx) * plane + p * ld.
+// Threads are b-fastest so B consecutive lines give coalesced segments.
+template <int L>
+__device__ __forceinline__ long col_base(long line0, int nx, long plane, long nlines, bool &ok)
+{
+    using P = Plan<L>;
+    const int b = threadIdx.x % P::B;
+    const long l = line0 + b;
+    ok = l < nlines;
+    return (l % nx) + (l / nx) * plane;
+}
+
+template <int L>
+__device__ __forceinline__ void load_cols(float2 *buf, const float2 *__restrict__ src, long base, bool ok, long ld)
+{
+    using P = Plan<L>;
+    const int b = threadIdx.x % P::B, t = threadIdx.x / P::B;
+#pragma unroll 4
+    for (int p = t; p < L; p += P::T) buf[b * P::LP + p] = ok ? __ldcs(&src[base + p * ld]) : make_float2(0.f, 0.f);
+}
+
+template <int L>
+__device__ __forceinline__ void store_cols(float2 *dst, const float2 *buf, long base, bool ok, long ld)
+{
+    using P = Plan<L>;
+    const int b = threadIdx.x % P::B, t = threadIdx.x / P::B;
+    if (!ok) return;
+#pragma unroll 4
+    for (int p = t; p < L; p += P::T) __stcs(&dst[base + p * ld], buf[b * P::LP + p]);
+}
+
+// ------------------------------------------------------------ generic passes
+template <int L, bool INV>
+__global__ void __launch_bounds__(Plan<L>::THREADS) rows_kernel(float2 *data, const float2 *__restrict__ tw, long nlines)
+{
+    extern __shared__ float4 smem4[];
+    float2 *buf = reinterpret_cast<float2 *>(smem4);
+    const long line0 = (long)blockIdx.x * Plan<L>::B;
+    load_rows<L>(buf, data, line0, nlines);
+    __syncthreads();
+    Plan<L>::template run<INV>(buf, tw);
+    store_rows<L>(data, buf, line0, nlines);
+}
+
+template <int L, bool INV>
+__global__ void __launch_bounds__(Plan<L>::THREADS) cols_kernel(float2 *data, const float2 *__restrict__ tw, long nlines,
+                                                                int nx, long plane, long ld)
+{
+    extern __shared__ float4 smem4[];
+    float2 *buf = reinterpret_cast<float2 *>(smem4);
+    const long line0 = (long)blockIdx.x * Plan<L>::B;
+    bool ok;
+    const long base = col_base<L>(line0, nx, plane, nlines, ok);
+    load_cols<L>(buf, data, base, ok, ld);
+    __syncthreads();
+    Plan<L>::template run<INV>(buf, tw);
+    store_cols<L>(data, buf, base, ok, ld);
+}
+
+template <int L, class K>
+static cudaError_t prep_launch(K kernel, size_t smem)
+{
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+template <int L>
+static cudaError_t rows_launch(float2 *data, long nlines, bool inv, cudaStream_t s)
+{
+    using P = Plan<L>;
+    const size_t smem = fftl::smem_bytes<L>();
+    const long grid = (nlines + P::B - 1) / P::B;
+    auto k = inv ? rows_kernel<L, true> : rows_kernel<L, false>;
+    cudaError_t e = prep_launch<L>(k, smem);
+    if (e != cudaSuccess) return e;
+    k<<<(unsigned)grid, P::THREADS, smem, s>>>(data, twiddles(L), nlines); note_launch();
+    return cudaGetLastError();
+}
+
+template <int L>
+static cudaError_t cols_launch(float2 *data, long nlines, int nx, long plane, long ld, bool inv, cudaStream_t s)
+{
+    using P = Plan<L>;
+    const size_t smem = fftl::smem_bytes<L>();
+    const long grid = (nlines + P::B - 1) / P::B;
+    auto k = inv ? cols_kernel<L, true> : cols_kernel<L, false>;
+    cudaError_t e = prep_launch<L>(k, smem);
+    if (e != cudaSuccess) return e;
+    k<<<(unsigned)grid, P::THREADS, smem, s>>>(data, twiddles(L), nlines, nx, plane, ld); note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t fft_rows(float2 *data, int L, long nlines, bool inverse, cudaStream_t s)
+{
+    CTDM_DISPATCH_L(L, rows_launch, data, nlines, inverse, s)
+}
+
+cudaError_t fft_cols(float2 *data, int L, long nlines, int nx, long plane, long ld, bool inverse, cudaStream_t s)
+{
+    CTDM_DISPATCH_L(L, cols_launch, data, nlines, nx, plane, ld, inverse, s)
+}
+
+__global__ void scale_kernel(float2 *d, long n, float s, bool conj)
+{
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        float2 v = d[i];
+        d[i] = make_float2(v.x * s, conj ? -v.y * s : v.y * s);
+    }
+}
+
+cudaError_t scale_complex(float2 *data, long n, float s, bool conjugate, cudaStream_t st)
+{
+    long blocks = (n + 255) / 256;
+    if (blocks > 4096) blocks = 4096;
+    scale_kernel<<<(unsigned)blocks, 256, 0, st>>>(data, n, s, conjugate); note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t fft3d(float2 *data, int R, bool inverse, cudaStream_t s)
+{
+    const long r2 = (long)R * R;
+    cudaError_t e = fft_rows(data, R, r2, inverse, s);
+    if (e == cudaSuccess) e = fft_cols(data, R, r2, R, r2, R, inverse, s);
+    if (e == cudaSuccess) e = fft_cols(data, R, r2, R, R, r2, inverse, s);
+    if (e == cudaSuccess && inverse) e = scale_complex(data, r2 * R, 1.0f / (float)(r2 * R), false, s);
+    return e;
+}
+
+// ------------------------------------------------------------ x pass
+template <int L, bool FINAL>
+__global__ void __launch_bounds__(Plan<L>::THREADS) xpass_kernel(LoopArgs a, const float2 *__restrict__ tw)
+{
+    using P = Plan<L>;
+    extern __shared__ float4 smem4[];
+    float2 *buf = reinterpret_cast<float2 *>(smem4);
+    const long nl = (long)L * L;
+    const long line0 = (long)blockIdx.x * P::B;
+    load_rows<L>(buf, a.G, line0, nl);
+    __syncthreads();
+    P::template run<true>(buf, tw);
+    if constexpr (FINAL) {
+        // est_n then the octant shift (cuFFT3Dshift, cTDM/FFT.cu:324-350) on the write
+        for (int e = threadIdx.x; e < P::B * L; e += P::THREADS) {
+            const int b = e / L, p = e - b * L;
+            const long l = line0 + b;
+            const int y = (int)(l % L), z = (int)(l / L);
+            float2 v = cscale(buf[b * P::LP + p], a.inv_n3);
+            const long o = (long)((p + L / 2) % L) + (long)L * ((y + L / 2) % L) + (long)L * L * ((z + L / 2) % L);
+            a.out[o] = est_n(v, a.k2, a.n_med);
+        }
+    } else {
+        for (int e = threadIdx.x; e < P::B * L; e += P::THREADS) {
+            const int b = e / L, p = e - b * L;
+            float2 v = cscale(buf[b * P::LP + p], a.inv_n3);
+            buf[b * P::LP + p] = modify_f(est_n(v, a.k2, a.n_med), a.k2, a.n_med2);
+        }
+        __syncthreads();
+        P::template run<false>(buf, tw);
+        store_rows<L>(a.G, buf, line0, nl);
+    }
+}
+
+// ------------------------------------------------------------ y pass
+template <int L, bool INV>
+__global__ void __launch_bounds__(Plan<L>::THREADS) ypass_kernel(LoopArgs a, const float2 *__restrict__ tw)
+{
+    using P = Plan<L>;
+    extern __shared__ float4 smem4[];
+    float2 *buf = reinterpret_cast<float2 *>(smem4);
+    const long nl = (long)L * L;
+    const long line0 = (long)blockIdx.x * P::B;
+    bool ok;
+    const long base = col_base<L>(line0, L, (long)L * L, nl, ok);
+    load_cols<L>(buf, a.G, base, ok, L);
+    __syncthreads();
+    P::template run<INV>(buf, tw);
+    store_cols<L>(a.G, buf, base, ok, L);
+}
+
+// ------------------------------------------------------------ z pass
+// check_F3D (cTDM/Recon_kernel.cu:396-412): F <- F2 where F2.re != 0 and F2.im != 0
+// (mode 0, the reference predicate) or where the voxel was hit (mode 1).
+template <int L, int MODE>
+__global__ void __launch_bounds__(Plan<L>::THREADS) zpass_kernel(LoopArgs a, const float2 *__restrict__ tw)
+{
+    using P = Plan<L>;
+    extern __shared__ float4 smem4[];
+    float2 *buf = reinterpret_cast<float2 *>(smem4);
+    const long nl = (long)L * L;
+    const long line0 = (long)blockIdx.x * P::B;
+    bool ok;
+    const long base = col_base<L>(line0, L, L, nl, ok);
+    load_cols<L>(buf, a.G, base, ok, nl);
+    __syncthreads();
+    P::template run<false>(buf, tw);
+    {
+        const int b = threadIdx.x % P::B, t = threadIdx.x / P::B;
+        if (ok) {
+            for (int p = t; p < L; p += P::T) {
+                const long idx = base + p * nl;
+                const float2 f2 = __ldcs(&a.F2[idx]);
+                bool keep;
+                if (MODE == 0) keep = (f2.x != 0.0f && f2.y != 0.0f);
+                else keep = a.mask[idx] != 0;
+                if (keep) buf[b * P::LP + p] = f2;
+            }
+        }
+    }
+    __syncthreads();
+    P::template run<true>(buf, tw);
+    store_cols<L>(a.G, buf, base, ok, nl);
+}
+
+template <int L>
+static cudaError_t xpass_launch(const LoopArgs &a, bool fin, cudaStream_t s)
+{
+    using P = Plan<L>;
+    const size_t smem = fftl::smem_bytes<L>();
+    auto k = fin ? xpass_kernel<L, true> : xpass_kernel<L, false>;
+    cudaError_t e = prep_launch<L>(k, smem);
+    if (e != cudaSuccess) return e;
+    k<<<(unsigned)((long)L * L / P::B), P::THREADS, smem, s>>>(a, twiddles(L)); note_launch();
+    return cudaGetLastError();
+}
+
+template <int L>
+static cudaError_t ypass_launch(const LoopArgs &a, bool inv, cudaStream_t s)
+{
+    using P = Plan<L>;
+    const size_t smem = fftl::smem_bytes<L>();
+    auto k = inv ? ypass_kernel<L, true> : ypass_kernel<L, false>;
+    cudaError_t e = prep_launch<L>(k, smem);
+    if (e != cudaSuccess) return e;
+    k<<<(unsigned)((long)L * L / P::B), P::THREADS, smem, s>>>(a, twiddles(L)); note_launch();
+    return cudaGetLastError();
+}
+
+template <int L>
+static cudaError_t zpass_launch(const LoopArgs &a, int mode, cudaStream_t s)
+{
+    using P = Plan<L>;
+    const size_t smem = fftl::smem_bytes<L>();
+    auto k = mode ? zpass_kernel<L, 1> : zpass_kernel<L, 0>;
+    cudaError_t e = prep_launch<L>(k, smem);
+    if (e != cudaSuccess) return e;
+    k<<<(unsigned)((long)L * L / P::B), P::THREADS, smem, s>>>(a, twiddles(L)); note_launch();
+    return cudaGetLastError();
+}
+
+// Volume sides supported by the reconstruction passes.
+#define CTDM_DISPATCH_R(Rrt, FN, ...)                  \
+    switch (Rrt) {                                     \
+    case 32: return FN<32>(__VA_ARGS__);               \
+    case 64: return FN<64>(__VA_ARGS__);               \
+    case 128: return FN<128>(__VA_ARGS__);             \
+    case 256: return FN<256>(__VA_ARGS__);             \
+    case 384: return FN<384>(__VA_ARGS__);             \
+    case 512: return FN<512>(__VA_ARGS__);             \
+    case 768: return FN<768>(__VA_ARGS__);             \
+    default: return cudaErrorInvalidValue;             \
+    }
+
+cudaError_t launch_xpass(const LoopArgs &a, bool final_pass, cudaStream_t s)
+{
+    CTDM_DISPATCH_R(a.R, xpass_launch, a, final_pass, s)
+}
+cudaError_t launch_ypass(const LoopArgs &a, bool inverse, cudaStream_t s)
+{
+    CTDM_DISPATCH_R(a.R, ypass_launch, a, inverse, s)
+}
+cudaError_t launch_zpass(const LoopArgs &a, int check_mode, cudaStream_t s)
+{
+    CTDM_DISPATCH_R(a.R, zpass_launch, a, check_mode, s)
+}
+
+// ------------------------------------------------------------ Ewald mapping
+template <int L>
+__global__ void __launch_bounds__(Plan<L>::THREADS) ewald_kernel(EwaldArgs a, const float2 *__restrict__ tw)
+{
+    using P = Plan<L>;
+    constexpr int R = L;
+    extern __shared__ float4 smem4[];
+    float2 *buf = reinterpret_cast<float2 *>(smem4);
+    uint32_t *cnt = reinterpret_cast<uint32_t *>(buf + P::B * P::LP);
+    AngleGeom *geo = reinterpret_cast<AngleGeom *>(cnt + P::B * L);
+    const long line0 = (long)blockIdx.x * P::B;   // line = x + R*y, B consecutive x
+    for (int e = threadIdx.x; e < P::B * P::LP; e += P::THREADS) buf[e] = make_float2(0.f, 0.f);
+    for (int e = threadIdx.x; e < P::B * L; e += P::THREADS) cnt[e] = 0u;
+    for (int e = threadIdx.x; e < a.A; e += P::THREADS) geo[e] = a.geom[e];
+    __syncthreads();
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = P::THREADS >> 5;
+    const long rr = (long)R * R;
+    const float four_pi = 4.0f * CTDM_PI_F;
+    for (int b = warp; b < P::B; b += nwarps) {
+        const long l = line0 + b;
+        const int x = (int)(l % R), y = (int)(l / R);
+        const int ii = x < R / 2 ? x : x - R;
+        const int jj = y < R / 2 ? y : y - R;
+        const float2 *ucol = a.U + x + (long)R * y;
+        float2 *col = buf + b * P::LP;
+        uint32_t *ccol = cnt + b * L;
+        for (int a0 = 0; a0 < a.A; a0 += 32) {
+            const int ang = a0 + lane;
+            int nz = -1;
+            float2 val = make_float2(0.f, 0.f);
+            if (ang < a.A && geo[ang].valid) {
+                float fz;
+                nz = ewald_nz(ii, jj, geo[ang], a.df, a.fm02, a.fm02s, R, fz);
+                if (nz >= 0) {
+                    const float2 u = __ldg(&ucol[ang * rr]);
+                    val = make_float2(-fz * four_pi * u.y, fz * four_pi * u.x);
+                }
+            }
+            // angle order per voxel: lanes are applied one after another
+            unsigned pending = __ballot_sync(0xffffffffu, nz >= 0);
+            while (pending) {
+                const int q = __ffs(pending) - 1;
+                if (lane == q) {
+                    float2 c = col[nz];
+                    col[nz] = make_float2(c.x + val.x, c.y + val.y);
+                    ccol[nz] += 1u;
+                }
+                __syncwarp();
+                pending &= pending - 1;
+            }
+        }
+    }
+    __syncthreads();
+    // Initial_F_F2 (cTDM/Recon_kernel.cu:253-276): F2 = (F / C where C != 0) / dx
+    {
+        const int b = threadIdx.x % P::B, t = threadIdx.x / P::B;
+        const long l = line0 + b;
+        const long base = l;   // (x + R*y)
+        for (int p = t; p < L; p += P::T) {
+            float2 v = buf[b * P::LP + p];
+            const uint32_t c = cnt[b * L + p];
+            if (c != 0u) v = make_float2(v.x / (float)c, v.y / (float)c);
+            v = make_float2(v.x / a.dx, v.y / a.dx);
+            buf[b * P::LP + p] = v;
+            const long idx = base + (long)p * rr;
+            a.F2[idx] = v;
+            if (a.counts) a.counts[idx] = c;
+            if (a.mask) a.mask[idx] = c != 0u;
+        }
+    }
+    __syncthreads();
+    P::template run<true>(buf, tw);
+    {
+        const int b = threadIdx.x % P::B, t = threadIdx.x / P::B;
+        const long base = line0 + b;
+        for (int p = t; p < L; p += P::T) a.G[base + (long)p * rr] = buf[b * P::LP + p];
+    }
+}
+
+template <int L>
+static cudaError_t ewald_launch(const EwaldArgs &a, cudaStream_t s)
+{
+    using P = Plan<L>;
+    const size_t smem = fftl::smem_bytes<L>() + sizeof(uint32_t) * P::B * L + sizeof(AngleGeom) * a.A;
+    auto k = ewald_kernel<L>;
+    cudaError_t e = prep_launch<L>(k, smem);
+    if (e != cudaSuccess) return e;
+    k<<<(unsigned)((long)L * L / P::B), P::THREADS, smem, s>>>(a, twiddles(L)); note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ewald(const EwaldArgs &a, cudaStream_t s)
+{
+    CTDM_DISPATCH_R(a.R, ewald_launch, a, s)
+}
+
+}  // namespace ctdm

@@ -1,0 +1,157 @@
+// Per-angle preparation of the Rytov data for the Fourier mapping.
+//
+// Reference chain (y-h-Lin/cTDM): bilinear_interpolation_kernel M -> N
+// (cTDM/HilbertTransform.cu:3658-3723), Combine2Stack centre crop N -> R with the
+// NaN/inf scrub (:1394-1427), MedianFilter_gpu + checkMaps per slice
+// (cTDM/Recon_kernel.cu:7-27,65-142), cuCopyArray u = log A + i phi transposed
+// (:154-169) and cuFFT2Dshift (cTDM/FFT.cu:220).  One kernel per 32 x 32 tile:
+// only the R x R window of the upsampled map is interpolated (into shared
+// memory with a one-pixel halo), the median is taken out of place (the
+// reference filters in place and races), and the transposed, quadrant-swapped
+// complex value is written coalesced.
+#include <cmath>
+
+#include "kernels_front.cuh"
+
+namespace ctdm {
+
+// bilinear_interpolation_kernel tap rule; taps past the input edge read 0 (the
+// reference leaves d10_2 unset there; it is defined as 0).
+__device__ __forceinline__ float resize_at(const float *__restrict__ d, int M1, float xr, int i, int j)
+{
+    const int ix = (int)(xr * (float)i);
+    const float a = xr * (float)i - (float)ix;
+    const int iy = (int)(xr * (float)j);
+    const float b = xr * (float)j - (float)iy;
+    const float d00 = (ix < M1 && iy < M1) ? d[iy * M1 + ix] : 0.f;
+    const float d10 = (ix + 1 < M1 && iy < M1) ? d[iy * M1 + ix + 1] : 0.f;
+    const float d01 = (ix < M1 && iy + 1 < M1) ? d[(iy + 1) * M1 + ix] : 0.f;
+    const float d11 = (ix + 1 < M1 && iy + 1 < M1) ? d[(iy + 1) * M1 + ix + 1] : 0.f;
+    const float t1 = a * d10 + (-d00 * a + d00);
+    const float t2 = a * d11 + (-d01 * a + d01);
+    return b * t2 + (-t1 * b + t1);
+}
+
+#define CTDM_SORT2(a, b)               \
+    {                                  \
+        const float lo_ = fminf(a, b); \
+        b = fmaxf(a, b);               \
+        a = lo_;                       \
+    }
+
+// Median of nine by the 19-exchange network published by Paeth (Graphics Gems).
+__device__ __forceinline__ float median9(float p0, float p1, float p2, float p3, float p4, float p5, float p6,
+                                         float p7, float p8)
+{
+    CTDM_SORT2(p1, p2); CTDM_SORT2(p4, p5); CTDM_SORT2(p7, p8);
+    CTDM_SORT2(p0, p1); CTDM_SORT2(p3, p4); CTDM_SORT2(p6, p7);
+    CTDM_SORT2(p1, p2); CTDM_SORT2(p4, p5); CTDM_SORT2(p7, p8);
+    CTDM_SORT2(p0, p3); CTDM_SORT2(p5, p8); CTDM_SORT2(p4, p7);
+    CTDM_SORT2(p3, p6); CTDM_SORT2(p1, p4); CTDM_SORT2(p2, p5);
+    CTDM_SORT2(p4, p7); CTDM_SORT2(p4, p2); CTDM_SORT2(p6, p4);
+    CTDM_SORT2(p4, p2);
+    return p4;
+}
+
+__device__ __forceinline__ float tile_median(float (*s)[35], int ly, int lx)
+{
+    return median9(s[ly - 1][lx - 1], s[ly - 1][lx], s[ly - 1][lx + 1], s[ly][lx - 1], s[ly][lx], s[ly][lx + 1],
+                   s[ly + 1][lx - 1], s[ly + 1][lx], s[ly + 1][lx + 1]);
+}
+
+// MODE 0: resize+crop from M x M maps.  MODE 1: input is already an R x R stack.
+// OUT 0: Rytov complex (transposed, swapped).  OUT 1: phase/amp stack.
+template <int MODE, int OUT>
+__global__ void __launch_bounds__(256) prep_kernel(const float *__restrict__ phase, const float *__restrict__ amp,
+                                                  int M, int N, int R, float2 *U0, float *ph_out, float *am_out)
+{
+    __shared__ float sp[34][35], sa[34][35];
+    const int a = blockIdx.z;
+    const int tx0 = blockIdx.x * 32, ty0 = blockIdx.y * 32;
+    const long in_sz = MODE == 0 ? (long)M * M : (long)R * R;
+    const float *P = phase + a * in_sz;
+    const float *Am = amp + a * in_sz;
+    const float xr = (float)(M - 1) / (float)N;
+    const int off = (N - R) / 2;
+    const int tid = threadIdx.y * 32 + threadIdx.x;
+    for (int e = tid; e < 34 * 34; e += 256) {
+        const int lx = e % 34, ly = e / 34;
+        const int i = tx0 - 1 + lx, j = ty0 - 1 + ly;
+        float pv = 0.f, av = 1.f;
+        if (i >= 0 && i < R && j >= 0 && j < R) {
+            if (MODE == 0) {
+                pv = resize_at(P, M, xr, i + off, j + off);
+                av = resize_at(Am, M, xr, i + off, j + off);
+                if (isnan(pv) || isinf(pv)) pv = 0.f;   // Combine2Stack scrub
+                if (isnan(av) || isinf(av)) av = 1.f;
+            } else {
+                pv = P[i + (long)R * j];
+                av = Am[i + (long)R * j];
+            }
+        }
+        sp[ly][lx] = pv;
+        sa[ly][lx] = av;
+    }
+    __syncthreads();
+    const long rr = (long)R * R;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const int li = threadIdx.y + 8 * k, lj = threadIdx.x;
+        const int i = tx0 + li, j = ty0 + lj;
+        if (i >= R || j >= R) continue;
+        float pv, av;
+        if (i == 0 || i == R - 1 || j == 0 || j == R - 1) {
+            pv = sp[lj + 1][li + 1];
+            av = sa[lj + 1][li + 1];
+        } else {
+            pv = tile_median(sp, lj + 1, li + 1);
+            av = tile_median(sa, lj + 1, li + 1);
+        }
+        // checkMaps (cTDM/Recon_kernel.cu:122-142)
+        if (isnan(pv) || isinf(pv)) pv = 0.f;
+        if (isnan(av) || isinf(av)) av = 1.0f;
+        else if (av == 0.f) av = 0.01f;
+        else av = fabsf(av);
+        if (OUT == 0) {
+            const int xs = (j + R / 2) % R, ys = (i + R / 2) % R;
+            U0[a * rr + xs + (long)R * ys] = make_float2(logf(av), pv);
+        } else {
+            ph_out[a * rr + i + (long)R * j] = pv;
+            am_out[a * rr + i + (long)R * j] = av;
+        }
+    }
+}
+
+cudaError_t prep_rytov(const float *phase, const float *amp, int A, int M, int N, int R, float2 *U0, cudaStream_t s)
+{
+    dim3 grid((R + 31) / 32, (R + 31) / 32, A), block(32, 8);
+    prep_kernel<0, 0><<<grid, block, 0, s>>>(phase, amp, M, N, R, U0, nullptr, nullptr); note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t prep_stack(const float *phase, const float *amp, int A, int M, int N, int R, float *ph_out,
+                       float *am_out, cudaStream_t s)
+{
+    dim3 grid((R + 31) / 32, (R + 31) / 32, A), block(32, 8);
+    prep_kernel<0, 1><<<grid, block, 0, s>>>(phase, amp, M, N, R, nullptr, ph_out, am_out); note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t stack_to_rytov(const float *ph, const float *am, int A, int R, float2 *U0, cudaStream_t s)
+{
+    dim3 grid((R + 31) / 32, (R + 31) / 32, A), block(32, 8);
+    prep_kernel<1, 0><<<grid, block, 0, s>>>(ph, am, R, R, R, U0, nullptr, nullptr); note_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace ctdm
+
+namespace ctdm {
+// MedianFilter on R x R stacks (stack in, stack out).
+cudaError_t median_stack(const float *ph, const float *am, int A, int R, float *ph_out, float *am_out, cudaStream_t s)
+{
+    dim3 grid((R + 31) / 32, (R + 31) / 32, A), block(32, 8);
+    prep_kernel<1, 1><<<grid, block, 0, s>>>(ph, am, R, R, R, nullptr, ph_out, am_out); note_launch();
+    return cudaGetLastError();
+}
+}  // namespace ctdm

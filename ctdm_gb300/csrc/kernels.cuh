@@ -1,0 +1,63 @@
+// Declarations of the kernel launchers shared between translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "ctdm_common.cuh"
+
+namespace ctdm {
+
+// Counts kernel launches issued by the library (process-wide, for instrumentation).
+void note_launch();
+
+// Twiddle table for an FFT length (exp(-2 pi i e / L), e < L), device resident.
+const float2 *twiddles(int L);
+// DCT helper tables for crop side M: dct_tw[k] = (cos(k pi/2M), sin(k pi/2M)),
+// k = 0..2M; eig[k] = 4 sin^2(2 pi k/(4M-1)).
+const float2 *dct_twiddles(int M);
+const float *dct_eigen(int M);
+
+// ---- per-angle Ewald geometry (host computed, FP64 rule inputs)
+struct AngleGeom {
+    double fx0, fy0, fz0;  // illumination frequency (1/m); fx0 = fm0 sin(AngY), fy0 = fm0 sin(AngX)
+    float fx0s, fy0s, fz0s;  // the same divided by df (FP32 fast path)
+    int valid;             // 0 when fm0^2 - fx0^2 - fy0^2 < 0 (the whole angle is skipped)
+};
+
+struct EwaldArgs {
+    const float2 *U;        // A spectra, R*R each, [a][Ny][Nx]
+    const AngleGeom *geom;  // A entries
+    int A, R;
+    double fm0, df, fm02;
+    float fm02s;            // (fm0/df)^2
+    float dx;
+    float2 *F2;             // R^3 out (k-space data, F/C/dx)
+    float2 *G;              // R^3 out (F2 after the z inverse transform)
+    uint32_t *counts;       // optional R^3 hit counts
+    uint8_t *mask;          // optional R^3 hit mask (1 where counts > 0)
+};
+
+struct LoopArgs {
+    float2 *G;
+    const float2 *F2;
+    const uint8_t *mask;
+    float2 *out;            // final RI volume (octant shifted), only for the final pass
+    int R;
+    float inv_n3, k2, n_med, n_med2;
+};
+
+cudaError_t launch_ewald(const EwaldArgs &a, cudaStream_t s);
+cudaError_t launch_xpass(const LoopArgs &a, bool final_pass, cudaStream_t s);
+cudaError_t launch_ypass(const LoopArgs &a, bool inverse, cudaStream_t s);
+cudaError_t launch_zpass(const LoopArgs &a, int check_mode, cudaStream_t s);
+
+// Generic batched transforms.  rows: nlines contiguous lines of length L.
+// cols: lines of length L with element p at (l % nx) + (l / nx) * plane + p * ld.
+cudaError_t fft_rows(float2 *data, int L, long nlines, bool inverse, cudaStream_t s);
+cudaError_t fft_cols(float2 *data, int L, long nlines, int nx, long plane, long ld, bool inverse,
+                     cudaStream_t s);
+// 3-D transform in place (cuFFT3D semantics: inverse scaled by 1/(R^3)).
+cudaError_t fft3d(float2 *data, int R, bool inverse, cudaStream_t s);
+cudaError_t scale_complex(float2 *data, long n, float s, bool conjugate, cudaStream_t st);
+
+}  // namespace ctdm

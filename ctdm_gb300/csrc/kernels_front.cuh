@@ -1,0 +1,47 @@
+// Declarations of the per-angle (2-D) stage launchers.
+#pragma once
+#include "kernels.cuh"
+
+namespace ctdm {
+
+// QPI Algorithm A --------------------------------------------------------
+// Carrier of one background hologram (N x N float): carrier = {r, c, radius}
+// on the device.  scratch: N*N complex; key: one 64-bit word.
+cudaError_t qpi_find_carrier(const float *bg, int N, float2 *scratch, unsigned long long *key, int *carrier,
+                             cudaStream_t s);
+// Pruned forward transform of A holograms into their M x M window spectra S
+// (ifftshifted, masked).  T1: A*N*M complex scratch.
+cudaError_t qpi_forward_window(const float *holo, int A, int N, int M, const int *carrier, float2 *T1, float2 *S,
+                               cudaStream_t s);
+// Inverse M x M transform of S (destroyed) and the epilogue: field_out != NULL
+// stores the complex field, otherwise phase/amp against bgf[a * bg_stride].
+cudaError_t qpi_inverse_window(float2 *S, int A, int M, float2 *field_out, const float2 *bgf, long bg_stride,
+                               float *phase, float *amp, cudaStream_t s);
+
+// DCT least-squares unwrap -----------------------------------------------
+// A phase maps M x M (float) -> unwrapped maps.  T: A*M*M float scratch.
+// mode 0 = reference IDCT twiddle, 1 = exact DCT-III.
+cudaError_t dct_unwrap(const float *phi, float *out, float *T, int A, int M, int mode, cudaStream_t s);
+
+// FFT-based unwrap (FastUnwrapping) ---------------------------------------
+cudaError_t fast_unwrap(float *phi, float *out, float2 *work, int A, int M, cudaStream_t s);
+
+// Resize + centre crop + median + checkMaps + log/complex + transpose + shift
+// into the per-angle Rytov arrays U0 (A x R x R complex), ready for FFT2.
+cudaError_t prep_rytov(const float *phase, const float *amp, int A, int M, int N, int R, float2 *U0,
+                       cudaStream_t s);
+// Same stage, writing the phase/amp stack instead (for inspection / tests):
+// resized+cropped then median+checkMaps, A x R x R each.
+cudaError_t prep_stack(const float *phase, const float *amp, int A, int M, int N, int R, float *ph_out,
+                       float *am_out, cudaStream_t s);
+// Median + checkMaps on an existing R x R stack, then Rytov arrays.
+cudaError_t stack_to_rytov(const float *ph, const float *am, int A, int R, float2 *U0, cudaStream_t s);
+
+// Goldstein ---------------------------------------------------------------
+cudaError_t goldstein_residues(const float *phi, int A, int W, int H, int8_t *charges, cudaStream_t s);
+cudaError_t goldstein_cuts(const int8_t *charges, int A, int W, int H, uint8_t *cuts, int8_t *work,
+                           cudaStream_t s);
+cudaError_t goldstein_floodfill(const uint8_t *cuts, const float *phi, int A, int W, int H, float *out,
+                                uint8_t *state, int *lists, int *status, cudaStream_t s);
+
+}  // namespace ctdm

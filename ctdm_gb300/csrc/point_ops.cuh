@@ -1,0 +1,80 @@
+// Point operators of the reconstruction shared by the fused passes and the
+// reference-compatible single-stage kernels.
+#pragma once
+#include "ctdm_common.cuh"
+#include "kernels.cuh"
+
+namespace ctdm {
+
+// calculate_n3D (cTDM/Recon_kernel.cu:305-342): n = n_med sqrt(1 + F/(-k^2)), the
+// principal root, then Re n >= n_med and Im n >= 0.  The root is evaluated in the
+// cancellation-free form (the larger of a, |b| from the half-sum formula, the
+// other from d / 2x); it is the same function as the reference's expression.
+__device__ __forceinline__ float2 est_n(float2 F, float k2, float nm)
+{
+    const float c = F.x / (-k2) + 1.0f, d = F.y / (-k2);
+    const float mod = hypotf(c, d);
+    float a, b;
+    if (d == 0.0f) {
+        a = sqrtf(fmaxf(c, 0.0f));
+        b = 0.0f;
+    } else if (c >= 0.0f) {
+        a = sqrtf((mod + c) * 0.5f);
+        b = d / (2.0f * a);
+    } else {
+        b = sqrtf((mod - c) * 0.5f);
+        a = fabsf(d) / (2.0f * b);
+        if (d < 0.0f) b = -b;
+    }
+    float nr = a * nm, ni = b * nm;
+    if (nr < nm) nr = nm;
+    if (ni < 0.0f) ni = 0.0f;
+    return make_float2(nr, ni);
+}
+
+// Modify_F3D (cTDM/Recon_kernel.cu:370-383), called with n_med^2.
+__device__ __forceinline__ float2 modify_f(float2 n, float k2, float nm2)
+{
+    return make_float2(((n.x * n.x - n.y * n.y) / nm2 - 1.0f) * (-k2), (n.x * n.y * 2.0f) / nm2 * (-k2));
+}
+
+// Voxel z index of fillEdwardSphere (cTDM/Recon_kernel.cu:187-229, cuRound :236):
+// nz = mod(round_half_away((f_z - f_z0)/df), R) with
+// f_z = sqrt(fm0^2 - (fx^2 + fy^2)), fx = ii df + fx0, fy = jj df + fy0; no sample
+// where the radicand is negative.  The rule is defined in IEEE double without
+// contraction.  A float evaluation in units of df decides it whenever the result
+// is farther from a decision boundary than 20x its worst-case rounding error
+// (radicand >= 4 df^2, fraction more than 0.02 away from one half); otherwise the
+// double rule runs.  Returns -1 for no sample; fz (1/m) for the value.
+__device__ __forceinline__ int ewald_nz(int ii, int jj, const AngleGeom &g, double df, double fm02, float fm02s,
+                                        int R, float &fz)
+{
+    const float fxs = (float)ii + g.fx0s, fys = (float)jj + g.fy0s;
+    const float rads = fm02s - (fxs * fxs + fys * fys);
+    if (rads < -1.0f) return -1;
+    if (rads >= 4.0f) {
+        const float fzs = sqrtf(rads);
+        const float t = fzs - g.fz0s;
+        const float fl = floorf(t);
+        const float fr = t - fl;
+        if (fabsf(fr - 0.5f) > 0.02f) {
+            const int nz = (fr > 0.5f) ? (int)fl + 1 : (int)fl;
+            fz = fzs * (float)df;
+            return imod(nz, R);
+        }
+    }
+    const double fx = __dadd_rn(__dmul_rn((double)ii, df), g.fx0);
+    const double fy = __dadd_rn(__dmul_rn((double)jj, df), g.fy0);
+    const double s = __dadd_rn(__dmul_rn(fx, fx), __dmul_rn(fy, fy));
+    const double rad = __dsub_rn(fm02, s);
+    if (rad < 0.0) return -1;
+    const double fzd = __dsqrt_rn(rad);
+    const double t = __ddiv_rn(__dsub_rn(fzd, g.fz0), df);
+    const double rn = t > 0.0 ? floor(__dadd_rn(t, 0.5)) : ceil(__dsub_rn(t, 0.5));
+    fz = (float)fzd;
+    long nz = (long)rn % R;
+    if (nz < 0) nz += R;
+    return (int)nz;
+}
+
+}  // namespace ctdm

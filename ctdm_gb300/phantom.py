@@ -1,0 +1,183 @@
+"""Seeded synthetic cTDM acquisitions (FP64 numpy).
+
+No public dataset exists for this path; these generators stand in for the BMP
+stacks the reference reads (cTDM/HilbertTransform.cu:613-771).  A phantom is a sum
+of uniform ellipsoids in a medium of index n_med.  Its scattering potential
+f = -k0^2 (n^2 - n_med^2) has the closed-form 3-D Fourier transform of an affine
+image of the unit ball, V * 3 (sin x - x cos x) / x^3.  For each illumination
+angle the first-order Rytov field is built from the Fourier diffraction relation
+that the reference's mapping inverts (cTDM/Recon_kernel.cu:187-229,
+cTDM/HilbertTransform.cu:1839-1862):
+
+    DFT2(u)[nu] * dx^2 = f_hat(nu_x, nu_y, f_z - f_z0) / (i 4 pi f_z),
+    f_z = sqrt(fm0^2 - (nu_x + f_x0)^2 - (nu_y + f_y0)^2),
+
+with f_x0 = fm0 sin(AngY), f_y0 = fm0 sin(AngX) and the transpose/ifftshift
+convention of CopyDataArray + cuFFT2Dshift, so that the reference algorithm maps
+it back onto the phantom.  Holograms are I = I0 |exp(-i 2 pi f_R . r) + exp(u)|^2
+with the carrier f_R at a quarter of Nyquist on both axes; the sign makes the
+order the reference selects (rows past 600/1024 of the shifted spectrum) carry
+exp(u), so the phase arg BG - arg SP equals Im u.  Poisson noise at a mean of
+`photons` counts per pixel.
+"""
+from dataclasses import dataclass, field
+from typing import List, Tuple
+
+import numpy as np
+
+
+@dataclass
+class Ellipsoid:
+    center: Tuple[float, float, float]   # (x, y, z) in metres, volume frame
+    semi: Tuple[float, float, float]     # semi-axes (a, b, c) in metres
+    n: float                             # refractive index inside
+    rot: float = 0.0                     # rotation about z (radians)
+
+
+@dataclass
+class Acquisition:
+    holograms: np.ndarray                # (A, N, N) float32, [angle, y, x]
+    background: np.ndarray               # (N, N) float32
+    ang_x: np.ndarray                    # (A,) float32 radians (reference AngX)
+    ang_y: np.ndarray                    # (A,) float32 radians (reference AngY)
+    n_holo: int
+    m_crop: int
+    r_vol: int
+    pixel: float                         # hologram pixel (m) = reconstruction dx
+    wavelength: float
+    n_med: float
+    ellipsoids: List[Ellipsoid] = field(default_factory=list)
+
+    @property
+    def fm0(self):
+        return self.n_med / self.wavelength
+
+    @property
+    def dx(self):
+        return self.pixel
+
+    @property
+    def df(self):
+        return 1.0 / (self.r_vol * self.dx)
+
+    @property
+    def k2(self):
+        k = 2 * np.pi * self.n_med / self.wavelength
+        return k * k
+
+
+def cone_angles(count, na, n_med):
+    """Illumination on a circular cone with n_med sin(theta) = na, azimuths
+    2 pi a / count.  Returns (AngX, AngY) in the reference's convention."""
+    s = na / n_med
+    phi = 2 * np.pi * np.arange(count) / count
+    ang_y = np.arcsin(s * np.cos(phi))   # f_x0 = fm0 sin(AngY)
+    ang_x = np.arcsin(s * np.sin(phi))   # f_y0 = fm0 sin(AngX)
+    return ang_x.astype(np.float32), ang_y.astype(np.float32)
+
+
+def potential_hat(ells, n_med, wavelength, kx, ky, kz):
+    """Analytic 3-D FT (exp(-i 2 pi k.r)) of f = -k0^2 (n^2 - n_med^2) for nested
+    ellipsoids: each ellipsoid contributes its index step over the previous
+    (enclosing) one."""
+    k0 = 2 * np.pi / wavelength
+    out = np.zeros(np.broadcast(kx, ky, kz).shape, np.complex128)
+    for idx, e in enumerate(ells):
+        base = n_med if idx == 0 else ells[0].n
+        df_step = -k0 * k0 * (e.n ** 2 - base ** 2)
+        c, s = np.cos(e.rot), np.sin(e.rot)
+        ux = c * kx + s * ky
+        uy = -s * kx + c * ky
+        a, b, cc = e.semi
+        q = 2 * np.pi * np.sqrt((a * ux) ** 2 + (b * uy) ** 2 + (cc * kz) ** 2)
+        vol = 4.0 / 3.0 * np.pi * a * b * cc
+        with np.errstate(divide="ignore", invalid="ignore"):
+            shape = np.where(q < 1e-6, 1.0 - q * q / 10.0, 3.0 * (np.sin(q) - q * np.cos(q)) / q ** 3)
+        phase = np.exp(-2j * np.pi * (kx * e.center[0] + ky * e.center[1] + kz * e.center[2]))
+        out += df_step * vol * shape * phase
+    return out
+
+
+def rytov_field(ells, n_med, wavelength, n, pixel, ang_x, ang_y):
+    """Complex Rytov phase u on the N x N hologram grid, [y, x] layout."""
+    fm0 = n_med / wavelength
+    fx0 = fm0 * np.sin(float(ang_y))
+    fy0 = fm0 * np.sin(float(ang_x))
+    fz0 = np.sqrt(fm0 * fm0 - fx0 * fx0 - fy0 * fy0)
+    dfh = 1.0 / (n * pixel)
+    sgn = np.fft.fftfreq(n, 1.0 / n)           # signed bin index
+    nx = sgn[None, :] * dfh                    # volume-frame x frequency (fast DFT index)
+    ny = sgn[:, None] * dfh
+    rad = fm0 * fm0 - (nx + fx0) ** 2 - (ny + fy0) ** 2
+    ok = rad > 0
+    fz = np.sqrt(np.where(ok, rad, 1.0))
+    fhat = potential_hat(ells, n_med, wavelength, nx, ny, np.where(ok, fz - fz0, 0.0))
+    spec = np.where(ok, fhat / (1j * 4 * np.pi * fz) / (pixel * pixel), 0.0)
+    ut_shift = np.fft.ifft2(spec)              # DFT2(u_shifted) = spec, [Ny, Nx] layout
+    ut = np.fft.fftshift(ut_shift)             # undo the quadrant swap
+    return ut.T                                # CopyDataArray transposes: hologram [y, x]
+
+
+def holograms_from_fields(fields, photons, rng):
+    n = fields.shape[-1]
+    yy, xx = np.mgrid[0:n, 0:n]
+    ref = np.exp(-2j * np.pi * (xx / 8.0 + yy / 8.0))   # carrier at a quarter Nyquist
+    i0 = photons / 2.0
+    out = []
+    for u in fields:
+        inten = i0 * np.abs(ref + np.exp(u)) ** 2
+        out.append(rng.poisson(inten).astype(np.float32) if photons > 0 else inten.astype(np.float32))
+    return np.stack(out)
+
+
+def cell_phantom(rng, scale=1.0, n_cell=1.37, n_nuc=1.39, semi=(4e-6, 3e-6, 2.5e-6), nucleoli=3):
+    ells = [Ellipsoid((0.0, 0.0, 0.0), tuple(s * scale for s in semi), n_cell, rot=0.3)]
+    for _ in range(nucleoli):
+        r = rng.uniform(0.5e-6, 1.0e-6) * scale
+        lim = [max(s * scale - r, 0) * 0.5 for s in semi]
+        c = tuple(rng.uniform(-l, l) for l in lim)
+        ells.append(Ellipsoid(c, (r, r, r), n_nuc))
+    return ells
+
+
+def random_cell(rng, fov):
+    """2-6 ellipsoids with RI U[1.35, 1.40] inside an envelope ellipsoid."""
+    k = int(rng.integers(2, 7))
+    env = (rng.uniform(0.12, 0.18) * fov, rng.uniform(0.1, 0.15) * fov, rng.uniform(0.08, 0.12) * fov)
+    ells = [Ellipsoid((0.0, 0.0, 0.0), env, float(rng.uniform(1.35, 1.40)), rot=float(rng.uniform(0, np.pi)))]
+    for _ in range(k - 1):
+        r = rng.uniform(0.1, 0.3) * min(env)
+        c = tuple(float(rng.uniform(-0.4, 0.4) * e) for e in env)
+        ells.append(Ellipsoid(c, (r, r * rng.uniform(0.7, 1.0), r * rng.uniform(0.7, 1.0)),
+                              float(rng.uniform(1.35, 1.40))))
+    return ells
+
+
+def acquisition(n, r, angles, na=0.9, seed=0, pixel=0.1e-6, wavelength=532e-9, n_med=1.337,
+                photons=1000.0, ells=None, scale=1.0, **cell):
+    """One tomogram: `angles` SP holograms of N x N plus one background."""
+    rng = np.random.default_rng(seed)
+    if ells is None:
+        ells = cell_phantom(rng, scale=scale, **cell)
+    ax, ay = cone_angles(angles, na, n_med)
+    fields = np.stack([rytov_field(ells, n_med, wavelength, n, pixel, ax[a], ay[a]) for a in range(angles)])
+    holo = holograms_from_fields(fields, photons, rng)
+    bg = holograms_from_fields(np.zeros((1, n, n), np.complex128), photons, rng)[0]
+    return Acquisition(holo, bg, ax, ay, n, n // 4, r, pixel, wavelength, n_med, ells)
+
+
+# Workloads with the shapes of the benchmark configurations ------------------
+def config_plain_small(seed=1000, angles=49):
+    """49 x 256^2 holograms -> 256^3, NA 0.9, pixel 0.1 um (the plain small case)."""
+    return acquisition(256, 256, angles, na=0.9, seed=seed)
+
+
+def config_wrap_heavy(seed=2000, angles=121):
+    """121 x 1024^2 holograms cropped to 256^2 spectra -> 256^3; RI 1.40, 10 um thick."""
+    return acquisition(1024, 256, angles, na=0.9, seed=seed, n_cell=1.40, n_nuc=1.40,
+                       semi=(7e-6, 5e-6, 5e-6), nucleoli=3)
+
+
+def small_case(seed=7, n=64, r=64, angles=6, na=0.9, pixel=0.4e-6, photons=1000.0):
+    """Tiny acquisition for parity tests: FOV 25.6 um at 0.4 um pixels."""
+    return acquisition(n, r, angles, na=na, seed=seed, pixel=pixel, photons=photons)

@@ -1,0 +1,195 @@
+/*
+ * ctdm.h -- C ABI of the GB300-native cTDM reconstruction library (libctdm_gb300.so).
+ *
+ * Two groups of entry points:
+ *
+ *  1. Drop-in symbols with the names and argument lists of the reference
+ *     (y-h-Lin/cTDM) functions on the hologram -> refractive-index path, so a
+ *     reference driver links against this library instead of its own .cu files.
+ *     Like the reference they return void; failures are reported through
+ *     ctdm_last_error() (thread-local, empty string when the last call succeeded).
+ *     They run on the legacy default stream and synchronise before returning.
+ *
+ *  2. The native API (ctdm_*): explicit context, explicit stream, status codes,
+ *     caller-owned buffers, no hidden global state.
+ *
+ * Complex data is interleaved float32 (re, im), layout-compatible with
+ * cufftComplex / float2.  2-D arrays are x-fastest (element (i, j) at i + W*j),
+ * volumes at i + W*j + W*H*k, as in the reference.
+ */
+#ifndef CTDM_H
+#define CTDM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(CTDM_BUILD) && defined(__GNUC__)
+#define CTDM_API __attribute__((visibility("default")))
+#else
+#define CTDM_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+    float x, y;
+} ctdm_cfloat;
+
+typedef enum {
+    CTDM_OK = 0,
+    CTDM_ERR_INVALID = 1,     /* bad argument or unsupported size */
+    CTDM_ERR_CUDA = 2,        /* CUDA runtime error (message in ctdm_last_error) */
+    CTDM_ERR_NOMEM = 3,       /* device or host allocation failed */
+    CTDM_ERR_IO = 4,          /* file could not be read or written */
+    CTDM_ERR_STALLED = 5,     /* Goldstein flood fill stopped early (see ctdm_goldstein) */
+    CTDM_ERR_TIMEOUT = 6      /* a bounded device-side wait ran out */
+} ctdm_status;
+
+typedef struct ctdm_ctx ctdm_ctx;
+
+/* Unwrap modes: the reference's inverse DCT twiddle (quirk kept) or the exact DCT-III. */
+#define CTDM_UNWRAP_REF 0
+#define CTDM_UNWRAP_EXACT 1
+/* Data-replacement predicate in the positivity loop: the reference's
+ * (F2.re != 0 && F2.im != 0) or the Ewald hit mask. */
+#define CTDM_CHECK_REF 0
+#define CTDM_CHECK_MASK 1
+/* Which unwrapped phase feeds the reconstruction. */
+#define CTDM_METHOD_DCT 0
+#define CTDM_METHOD_FAST 1
+#define CTDM_METHOD_GOLDSTEIN 2
+
+typedef struct {
+    int n_holo;          /* hologram side N (power of two, 64..2048) */
+    int m_crop;          /* window side M (0: N/4) */
+    int r_vol;           /* volume side R (32, 64, 128, 256, 384, 512, 768) */
+    int iterations;      /* positivity loop bodies (the reference runs IterTime + 1) */
+    int unwrap_mode;     /* CTDM_UNWRAP_REF / CTDM_UNWRAP_EXACT */
+    int check_mode;      /* CTDM_CHECK_REF / CTDM_CHECK_MASK */
+    int unwrap_method;   /* CTDM_METHOD_* */
+    int run_goldstein;   /* 1: also run Goldstein residues, cuts and flood fill per angle */
+    int bg_per_angle;    /* 1: one background hologram per angle, 0: one shared */
+    int carrier_r, carrier_c, carrier_radius; /* window centre row/col and radius; < 0: detect */
+    double n_med;        /* medium refractive index */
+    double wavelength;   /* vacuum wavelength (m) */
+    double dx;           /* reconstruction voxel (m) */
+} ctdm_params;
+
+/* Default parameters (reference defaults where they exist). */
+CTDM_API void ctdm_params_default(ctdm_params *p);
+
+CTDM_API const char *ctdm_last_error(void);
+CTDM_API const char *ctdm_version(void);
+
+CTDM_API ctdm_status ctdm_ctx_create(int device, ctdm_ctx **out);
+CTDM_API void ctdm_ctx_destroy(ctdm_ctx *ctx);
+/* Carrier {row, col, radius} used by the last pipeline / ctdm_qpi call. */
+CTDM_API ctdm_status ctdm_ctx_carrier(ctdm_ctx *ctx, int *carrier3);
+/* Device buffers of the last pipeline call (valid until the next call or destroy):
+ * which = 0 phase (A*M*M f32), 1 amp, 2 unwrapped phase, 3 Goldstein charges (i8),
+ * 4 Goldstein cuts (u8), 5 Goldstein unwrapped (f32), 6 spectra U (A*R*R c64),
+ * 7 F2 (R^3 c64), 8 hit counts (R^3 u32, only with CTDM_CHECK_MASK). */
+CTDM_API ctdm_status ctdm_ctx_buffer(ctdm_ctx *ctx, int which, void **dptr, size_t *bytes);
+/* Stage timing with CUDA events on the call's stream (off by default).  Stages:
+ * 0 QPI, 1 unwrap, 2 Goldstein, 3 spectra (prep + FFT2), 4 Ewald mapping,
+ * 5 y inverse pass, 6 x pass (loop), 7 y forward pass, 8 z pass, 9 final x pass.
+ * ms[i]: summed device time of stage i in the last pipeline call; counts[i]: number
+ * of launches of that stage (may be NULL). */
+CTDM_API ctdm_status ctdm_ctx_set_timing(ctdm_ctx *ctx, int on);
+CTDM_API ctdm_status ctdm_ctx_stage_times(ctdm_ctx *ctx, double *ms, int *counts, int n);
+/* Number of kernels this library has launched in the process so far. */
+CTDM_API unsigned long long ctdm_launch_count(void);
+
+/* --- whole path (replaces HilbertTransform's per-frame loop + BatchRecon) --- */
+/* Device-resident inputs: d_holo (A*N*N f32), d_bg (N*N or A*N*N f32), angles on
+ * the host (A f32 each, radians).  d_ri: R^3 complex RI volume, octant-shifted like
+ * the reference's output.  stream: cudaStream_t (NULL = legacy default). */
+CTDM_API ctdm_status ctdm_reconstruct_device(ctdm_ctx *ctx, const ctdm_params *p, int n_angles, const float *d_holo,
+                                    const float *d_bg, const float *h_angx, const float *h_angy,
+                                    ctdm_cfloat *d_ri, void *stream);
+/* Same with host buffers: copies in, reconstructs, copies the volume out, syncs. */
+CTDM_API ctdm_status ctdm_reconstruct(ctdm_ctx *ctx, const ctdm_params *p, int n_angles, const float *h_holo,
+                             const float *h_bg, const float *h_angx, const float *h_angy, ctdm_cfloat *h_ri);
+
+/* --- stages (device pointers) --- */
+/* QPI Algorithm A.  carrier3: in {row, col, radius} (any < 0: detect from the first
+ * background), out: the carrier used. */
+CTDM_API ctdm_status ctdm_qpi(ctdm_ctx *ctx, int N, int M, int A, const float *d_holo, const float *d_bg, int bg_per_angle,
+                     int *carrier3, float *d_phase, float *d_amp, void *stream);
+CTDM_API ctdm_status ctdm_unwrap_dct(ctdm_ctx *ctx, int A, int M, int mode, const float *d_phi, float *d_out, void *stream);
+/* FastUnwrapping: d_phi is normalised in place like the reference. */
+CTDM_API ctdm_status ctdm_unwrap_fast(ctdm_ctx *ctx, int A, int M, float *d_phi, float *d_out, void *stream);
+/* Goldstein: residue charges (-1/0/+1), branch-cut mask (0/1), flood-filled phase.
+ * h_status (A ints, may be NULL): 0 done, 1 sweep limit reached, 2 stalled. */
+CTDM_API ctdm_status ctdm_goldstein(ctdm_ctx *ctx, int A, int W, int H, const float *d_phi, int8_t *d_charges,
+                           uint8_t *d_cuts, float *d_out, int *h_status, void *stream);
+/* Resize M -> N, centre crop R, median + checkMaps, u = log A + i phi (transposed,
+ * quadrant-swapped), forward FFT2: d_U (A*R*R complex). */
+CTDM_API ctdm_status ctdm_prepare_spectra(ctdm_ctx *ctx, int A, int M, int N, int R, const float *d_phase,
+                                 const float *d_amp, ctdm_cfloat *d_U, void *stream);
+/* The same from R x R phase/amp stacks (BatchRecon's input). */
+CTDM_API ctdm_status ctdm_stack_spectra(ctdm_ctx *ctx, int A, int R, const float *d_ph, const float *d_am,
+                               ctdm_cfloat *d_U, void *stream);
+/* Resize + crop + median + checkMaps only (phase/amp stacks out). */
+CTDM_API ctdm_status ctdm_prepare_stack(ctdm_ctx *ctx, int A, int M, int N, int R, const float *d_phase, const float *d_amp,
+                               float *d_ph_out, float *d_am_out, void *stream);
+/* Ewald-cap mapping of all angles + F2 = F/C/dx.  d_counts may be NULL. */
+CTDM_API ctdm_status ctdm_map_ewald(ctdm_ctx *ctx, int A, int R, const ctdm_cfloat *d_U, const float *h_angx,
+                           const float *h_angy, double fm0, double df, double dx, ctdm_cfloat *d_F2,
+                           uint32_t *d_counts, void *stream);
+/* Positivity loop from F2: iterations loop bodies, octant-shifted RI out.
+ * d_counts required for CTDM_CHECK_MASK (else may be NULL). */
+CTDM_API ctdm_status ctdm_positivity(ctdm_ctx *ctx, int R, int iterations, int check_mode, double k2, double n_med,
+                            const ctdm_cfloat *d_F2, const uint32_t *d_counts, ctdm_cfloat *d_ri, void *stream);
+/* Unnormalised batched FFT of the library's line lengths.  rank 1..3, dims
+ * fastest-first; inverse = 1 uses exp(+i), no scaling. */
+CTDM_API ctdm_status ctdm_fft(ctdm_cfloat *d_data, int rank, const int *dims, int batch, int inverse, void *stream);
+
+/* ------------------------------------------------------------------------- */
+/* Drop-in replacements for the reference entry points (void, default stream) */
+/* ------------------------------------------------------------------------- */
+/* Reference globals consumed by BatchRecon / HilbertTransform
+ * (cTDM/HilbertTransform.cu:11-35): ReconX=Y=Z, Nmed, wavelength (nm),
+ * CameraPixelSize (um), Mag, IterTime, ReconSave, SaveDir. */
+CTDM_API void ctdm_set_recon_globals(int recon_size, double n_med, double wavelength_nm, double camera_pixel_um, double mag,
+                            int iter_time, int recon_save, const char *save_dir);
+
+/* cTDM/DCT_Unwrapping.cuh:106 -- device pointers, sizeX == sizeY. */
+CTDM_API void DCT_UWLS_Unwrapped(float *ImgDst, float *ImgSrc, int sizeX, int sizeY);
+/* cTDM/FastUnwrapping.cuh:12 -- (src, dst) order; src is normalised in place. */
+CTDM_API void FastUnwrapping(float *ImgSrc, float *ImgDst, int sizeX, int sizeY);
+/* cTDM/Goldstein.cuh:41 */
+CTDM_API void cudaGoldsteinUnwrap2D(float *cu_phi, float *cu_UnWrapPhase, int sizeX, int sizeY, int frameNumber);
+/* cTDM/Recon_kernel.cuh:31 -- host stacks in, filtered device stacks out. */
+CTDM_API void MedianFilter(float *PhaseData, float *AmpData, float *Phase_img, float *Amp_img, int nx, int ny, int nz);
+/* cTDM/Recon_kernel.cuh:37 */
+CTDM_API void CopyDataArray(ctdm_cfloat *u_sp, float *phase, float *amp, int sizeX, int sizeY, int sizeZ, int numZ);
+/* cTDM/Recon_kernel.cuh:41 */
+CTDM_API void EdwardSphere(ctdm_cfloat *u_sp, ctdm_cfloat *F, float *C, float fm0, float df, float AngX, float AngY, int sizeX,
+                  int sizeY, int sizeZ);
+/* cTDM/Recon_kernel.cuh:51 */
+CTDM_API void initial_F_and_F2(float *C, ctdm_cfloat *cuF, ctdm_cfloat *cuF2, float recon_dx, int Image_Width,
+                      int Image_Height, int Image_Slice);
+/* cTDM/Recon_kernel.cuh:56 (device n; the reference's host mode 1 is not kept) */
+CTDM_API void est_n_3D(ctdm_cfloat *n, ctdm_cfloat *F, float recon_k2, float recon_med, int Image_Width, int Image_Height,
+              int Image_Slice);
+/* cTDM/Recon_kernel.cuh:63 */
+CTDM_API void modify_F_3D(ctdm_cfloat *n, ctdm_cfloat *F, float recon_k2, float recon_med, int Image_Width, int Image_Height,
+                 int Image_Slice);
+/* cTDM/Recon_kernel.cuh:70 */
+CTDM_API void check_F_3D(ctdm_cfloat *F, ctdm_cfloat *F2, int Image_Width, int Image_Height, int Image_Slice);
+/* cTDM/FFT.cuh:29 -- dir -1 forward, +1 inverse scaled by 1/(XYZ). */
+CTDM_API void cuFFT3D(ctdm_cfloat *ImgArray, int sizeX, int sizeY, int sizeZ, int dir);
+/* cTDM/FFT.cuh:25 -- dir -1 forward, +1 inverse scaled by 1/(XY) and conjugated. */
+CTDM_API void cuFFT2D(ctdm_cfloat *ImgArray, int sizeX, int sizeY, int dir);
+/* cTDM/HilbertTransform.cuh:132 -- host stacks (R*R*frames) and angles (radians);
+ * reconstructs with the globals above and writes 3D-RI-*.rimap into SaveDir. */
+CTDM_API void BatchRecon(float *PhaseStack, float *AmpStack, float *sampleAngleRadX, float *sampleAngleRadY, int ReconFrame);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CTDM_H */

@@ -1,0 +1,271 @@
+"""ctypes wrapper around the FP64 oracle (oracle/_build/libctdm_oracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by the smoke check and by the
+CPU-baseline leg of bench.py.  The product package never imports this module.
+
+Arrays are numpy, x-fastest like the reference: a 2-D image of width W and
+height H is an (H, W) array; a volume is (R, R, R) indexed [z, y, x].
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_SO = os.path.join(_HERE, "_build", "libctdm_oracle.so")
+_lib = None
+
+
+def build(force=False):
+    """Compile the oracle with its Makefile (gcc, OpenMP)."""
+    src = os.path.join(_HERE, "ctdm_oracle.c")
+    if force or not os.path.exists(_SO) or os.path.getmtime(_SO) < os.path.getmtime(src):
+        subprocess.check_call(["make", "-s", "-C", _HERE], stdout=subprocess.DEVNULL)
+    return _SO
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        _lib = ctypes.CDLL(_SO)
+        _lib.or_carrier_start_row.restype = ctypes.c_int
+        _lib.or_goldstein_floodfill.restype = ctypes.c_int
+        _lib.or_get_threads.restype = ctypes.c_int
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _c128(a):
+    return np.ascontiguousarray(a, dtype=np.complex128)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+class Params(ctypes.Structure):
+    _fields_ = [
+        ("n", ctypes.c_int), ("m", ctypes.c_int), ("r", ctypes.c_int), ("iters", ctypes.c_int),
+        ("unwrap_mode", ctypes.c_int), ("check_mode", ctypes.c_int),
+        ("carrier_r", ctypes.c_int), ("carrier_c", ctypes.c_int), ("carrier_radius", ctypes.c_int),
+        ("fm0", ctypes.c_double), ("df", ctypes.c_double), ("dx", ctypes.c_double),
+        ("k2", ctypes.c_double), ("n_med", ctypes.c_double),
+    ]
+
+
+def set_threads(n):
+    lib().or_set_threads(int(n))
+
+
+def get_threads():
+    return lib().or_get_threads()
+
+
+# ---- FFT -------------------------------------------------------------------
+def fft2(a, sign=-1):
+    a = _c128(a).copy()
+    h, w = a.shape
+    lib().or_fft2d(_p(a), w, h, int(sign))
+    return a
+
+
+def fft3(a, direction):
+    a = _c128(a).copy()
+    r = a.shape[0]
+    lib().or_fft3d(_p(a), a.shape[2], a.shape[1], a.shape[0], int(direction))
+    return a
+
+
+# ---- QPI -------------------------------------------------------------------
+def carrier_start_row(n):
+    return lib().or_carrier_start_row(int(n))
+
+
+def qpi_carrier(bg):
+    bg = _f32(bg)
+    r, c, rad = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    lib().or_qpi_carrier(_p(bg), bg.shape[0], ctypes.byref(r), ctypes.byref(c), ctypes.byref(rad))
+    return r.value, c.value, rad.value
+
+
+def qpi_field(holo, m, r, c, radius):
+    holo = _f32(holo)
+    out = np.zeros((m, m), np.complex128)
+    lib().or_qpi_field(_p(holo), holo.shape[0], int(m), int(r), int(c), int(radius), _p(out))
+    return out
+
+
+def wrap_phase(sp, bg):
+    sp, bg = _c128(sp), _c128(bg)
+    ph = np.zeros(sp.shape, np.float64)
+    am = np.zeros(sp.shape, np.float64)
+    lib().or_wrap_phase(_p(sp), _p(bg), sp.size, _p(ph), _p(am))
+    return ph, am
+
+
+# ---- DCT unwrap ------------------------------------------------------------
+def wrapped_laplacian(phi):
+    phi = _f64(phi)
+    out = np.zeros_like(phi)
+    lib().or_wrapped_laplacian(_p(phi), phi.shape[1], phi.shape[0], _p(out))
+    return out
+
+
+def dct2d(a):
+    a = _f64(a).copy()
+    lib().or_dct2d(_p(a), a.shape[1], a.shape[0])
+    return a
+
+
+def idct2d(a, mode):
+    a = _f64(a).copy()
+    lib().or_idct2d(_p(a), a.shape[1], a.shape[0], int(mode))
+    return a
+
+
+def poisson_divide(a):
+    a = _f64(a).copy()
+    lib().or_poisson_divide(_p(a), a.shape[1], a.shape[0])
+    return a
+
+
+def dct_unwrap(phi, mode):
+    phi = _f64(phi)
+    out = np.zeros_like(phi)
+    lib().or_dct_unwrap(_p(phi), phi.shape[1], phi.shape[0], int(mode), _p(out))
+    return out
+
+
+def fast_unwrap(phi):
+    """Returns (unwrapped, normalised_input) -- the input is rescaled in place like
+    the reference's PhaseNormalize."""
+    phi = _f64(phi).copy()
+    out = np.zeros_like(phi)
+    lib().or_fast_unwrap(_p(phi), phi.shape[1], phi.shape[0], _p(out))
+    return out, phi
+
+
+# ---- Goldstein -------------------------------------------------------------
+def goldstein_residues(phi):
+    phi = _f32(phi)
+    out = np.zeros(phi.shape, np.int8)
+    lib().or_goldstein_residues(_p(phi), phi.shape[1], phi.shape[0], _p(out))
+    return out
+
+
+def goldstein_cuts(charges):
+    charges = np.ascontiguousarray(charges, np.int8)
+    out = np.zeros(charges.shape, np.uint8)
+    lib().or_goldstein_cuts(_p(charges), charges.shape[1], charges.shape[0], _p(out))
+    return out
+
+
+def goldstein_floodfill(cuts, phi):
+    cuts = np.ascontiguousarray(cuts, np.uint8)
+    phi = _f32(phi)
+    out = np.zeros(phi.shape, np.float32)
+    ub = np.zeros(phi.shape, np.uint8)
+    st = lib().or_goldstein_floodfill(_p(cuts), _p(phi), phi.shape[1], phi.shape[0], _p(out), _p(ub))
+    return out, ub, st
+
+
+def goldstein(phi):
+    q = goldstein_residues(phi)
+    cuts = goldstein_cuts(q)
+    out, ub, st = goldstein_floodfill(cuts, phi)
+    return q, cuts, out, st
+
+
+# ---- stack / spectra / mapping / loop --------------------------------------
+def resize_crop(ph, am, n2, r):
+    ph, am = _f64(ph), _f64(am)
+    m1 = ph.shape[1]
+    po = np.zeros((r, r), np.float64)
+    ao = np.zeros((r, r), np.float64)
+    lib().or_resize_crop(_p(ph), _p(am), m1, ph.shape[0], int(n2), int(n2), int(r), _p(po), _p(ao))
+    return po, ao
+
+
+def median_check(ph, am):
+    ph, am = _f64(ph), _f64(am)
+    po, ao = np.zeros_like(ph), np.zeros_like(am)
+    lib().or_median_check(_p(ph), _p(am), ph.shape[1], ph.shape[0], _p(po), _p(ao))
+    return po, ao
+
+
+def rytov_spectrum(ph, am):
+    ph, am = _f64(ph), _f64(am)
+    u = np.zeros(ph.shape, np.complex128)
+    lib().or_rytov_spectrum(_p(ph), _p(am), ph.shape[0], _p(u))
+    return u
+
+
+def ewald_index(r, fm0, df, angx, angy):
+    vox = np.zeros(r * r, np.int64)
+    fz = np.zeros(r * r, np.float64)
+    lib().or_ewald_index(int(r), ctypes.c_double(fm0), ctypes.c_double(df), ctypes.c_double(angx),
+                         ctypes.c_double(angy), _p(vox), _p(fz))
+    return vox, fz
+
+
+def ewald_map(U, angx, angy, fm0, df, dx):
+    U = _c128(U)
+    na, r = U.shape[0], U.shape[1]
+    F2 = np.zeros((r, r, r), np.complex128)
+    C = np.zeros((r, r, r), np.uint32)
+    angx, angy = _f32(angx), _f32(angy)
+    lib().or_ewald_map(_p(U), _p(angx), _p(angy), na, r, ctypes.c_double(fm0), ctypes.c_double(df),
+                       ctypes.c_double(dx), _p(F2), _p(C))
+    return F2, C
+
+
+def positivity(F2, counts, iters, k2, n_med, check_mode=0):
+    F2 = _c128(F2)
+    r = F2.shape[0]
+    counts = np.ascontiguousarray(counts, np.uint32)
+    out = np.zeros_like(F2)
+    lib().or_positivity(_p(F2), _p(counts), r, int(iters), ctypes.c_double(k2), ctypes.c_double(n_med),
+                        int(check_mode), _p(out))
+    return out
+
+
+def make_params(n, m, r, iters, fm0, df, dx, k2, n_med, unwrap_mode=0, check_mode=0, carrier=None):
+    p = Params()
+    p.n, p.m, p.r, p.iters = n, m, r, iters
+    p.unwrap_mode, p.check_mode = unwrap_mode, check_mode
+    cr, cc, rad = carrier if carrier is not None else (-1, -1, -1)
+    p.carrier_r, p.carrier_c, p.carrier_radius = cr, cc, rad
+    p.fm0, p.df, p.dx, p.k2, p.n_med = fm0, df, dx, k2, n_med
+    return p
+
+
+def front_end(params, sp, bg, bg_per_angle=False):
+    sp, bg = _f32(sp), _f32(bg)
+    na = sp.shape[0]
+    r = params.r
+    ph = np.zeros((na, r, r), np.float64)
+    am = np.zeros((na, r, r), np.float64)
+    car = (ctypes.c_int * 3)()
+    lib().or_front_end(ctypes.byref(params), _p(sp), _p(bg), na, int(bg_per_angle), _p(ph), _p(am), car)
+    return ph, am, tuple(car)
+
+
+def pipeline(params, sp, bg, angx, angy, bg_per_angle=False):
+    sp, bg = _f32(sp), _f32(bg)
+    angx, angy = _f32(angx), _f32(angy)
+    na = sp.shape[0]
+    r = params.r
+    out = np.zeros((r, r, r), np.complex128)
+    car = (ctypes.c_int * 3)()
+    lib().or_pipeline(ctypes.byref(params), _p(sp), _p(bg), na, int(bg_per_angle), _p(angx), _p(angy),
+                      _p(out), car)
+    return out, tuple(car)

@@ -1,0 +1,62 @@
+"""The C-ABI library loads on a CPU-only machine and exports every function that
+include/ctdm.h declares (no compute calls)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_functions():
+    text = open(os.path.join(ROOT, "include", "ctdm.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = re.findall(r"^\s*(?:CTDM_API\s+)?(?:const\s+)?[A-Za-z_][A-Za-z0-9_]*\s*\*?\s*([A-Za-z_][A-Za-z0-9_]*)\s*\(",
+                       text, re.M)
+    return sorted(set(n for n in names if n not in ("if", "while")))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from ctdm_gb300 import build
+    path = build.build()
+    return ctypes.CDLL(path)
+
+
+def test_header_parsed():
+    names = header_functions()
+    for n in ("ctdm_reconstruct_device", "DCT_UWLS_Unwrapped", "BatchRecon", "cuFFT3D", "EdwardSphere"):
+        assert n in names
+
+
+def test_every_declared_symbol_exported(lib):
+    missing = [n for n in header_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_python_binding_covers_header():
+    from ctdm_gb300 import _lib
+    assert set(header_functions()) <= set(_lib.EXPORTED)
+
+
+def test_params_struct_layout(lib):
+    from ctdm_gb300 import _lib
+    _lib.load()
+    p = _lib.Params()
+    _lib.load().ctdm_params_default(ctypes.byref(p))
+    assert p.n_holo == 1024 and p.r_vol == 256 and p.iterations == 101
+    assert p.carrier_r == -1 and abs(p.n_med - 1.333) < 1e-12
+    assert ctypes.sizeof(_lib.Params) == 12 * 4 + 3 * 8
+
+
+def test_version_and_error_without_gpu(lib):
+    from ctdm_gb300 import _lib
+    L = _lib.load()
+    assert b"sm_103a" in L.ctdm_version()
+    # invalid arguments are rejected on the host before any CUDA call
+    p = _lib.Params()
+    L.ctdm_params_default(ctypes.byref(p))
+    p.n_holo = 100
+    rc = L.ctdm_reconstruct_device(ctypes.c_void_p(1), ctypes.byref(p), 4, 1, 1, 1, 1, 1, None)
+    assert rc == 1 and b"unsupported" in L.ctdm_last_error()
