@@ -116,9 +116,10 @@ def ncu_traffic(kernel, workload):
 
 
 # ---------------------------------------------------------------- CPU baseline (oracle)
-def cpu_sample(acq, iters, threads=None):
-    """FP64 oracle on a bounded sample of one tomogram: the per-angle front end on
-    two angles and the positivity loop with 0 and 1 iterations at full volume size;
+def cpu_sample(acq, iters, goldstein=False, threads=None):
+    """FP64 oracle on a bounded sample of one tomogram: the per-angle chain (QPI,
+    DCT unwrap, Goldstein when configured, resize/median, Rytov spectrum) on two
+    angles and the positivity loop with 0 and 1 iterations at full volume size,
     extrapolated to the whole tomogram.  Returns (seconds per tomogram, threads, text)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
@@ -126,17 +127,25 @@ def cpu_sample(acq, iters, threads=None):
     if threads:
         O.set_threads(threads)
     nthr = O.get_threads()
-    A = len(acq.ang_x)
+    A, m, n, r = len(acq.ang_x), acq.m_crop, acq.n_holo, acq.r_vol
     s = 2
-    par = O.make_params(acq.n_holo, acq.m_crop, acq.r_vol, 0, acq.fm0, acq.df, acq.dx, acq.k2, acq.n_med)
     t0 = time.perf_counter()
-    ph, am, _ = O.front_end(par, acq.holograms[:s], acq.background)
-    t_front = (time.perf_counter() - t0) / s
+    car = O.qpi_carrier(acq.background)
+    bgf = O.qpi_field(acq.background, m, *car)
+    t_fixed = time.perf_counter() - t0
     t0 = time.perf_counter()
-    U = np.stack([O.rytov_spectrum(ph[a], am[a]) for a in range(s)])
-    t_spec = (time.perf_counter() - t0) / s
+    U = []
+    for a in range(s):
+        ph, am = O.wrap_phase(O.qpi_field(acq.holograms[a], m, *car), bgf)
+        if goldstein:
+            O.goldstein(ph.astype(np.float32))
+        uw = O.dct_unwrap(ph, 0)
+        p1, a1 = O.resize_crop(uw, am, n, r)
+        p2, a2 = O.median_check(p1, a1)
+        U.append(O.rytov_spectrum(p2, a2))
+    t_angle = (time.perf_counter() - t0) / s
     t0 = time.perf_counter()
-    F2, C = O.ewald_map(U, acq.ang_x[:s], acq.ang_y[:s], acq.fm0, acq.df, acq.dx)
+    F2, C = O.ewald_map(np.stack(U), acq.ang_x[:s], acq.ang_y[:s], acq.fm0, acq.df, acq.dx)
     t_map = time.perf_counter() - t0
     t0 = time.perf_counter()
     O.positivity(F2, C, 0, acq.k2, acq.n_med)
@@ -145,9 +154,10 @@ def cpu_sample(acq, iters, threads=None):
     O.positivity(F2, C, 1, acq.k2, acq.n_med)
     t_p1 = time.perf_counter() - t0
     t_iter = max(t_p1 - t_p0, 0.0)
-    total = A * (t_front + t_spec) + t_map + t_p0 + iters * t_iter
-    text = (f"oracle on {s} of {A} angles + positivity loop with 0 and 1 iterations at {acq.r_vol}^3, "
-            f"extrapolated: {A}x{t_front + t_spec:.3f}s/angle + {t_map + t_p0:.2f}s + {iters}x{t_iter:.2f}s/iter")
+    total = t_fixed + A * t_angle + t_map + t_p0 + iters * t_iter
+    text = (f"oracle on {s} of {A} angles{' incl. Goldstein' if goldstein else ''} + positivity loop with 0 and 1 "
+            f"iterations at {r}^3, extrapolated: {A}x{t_angle:.3f}s/angle + {t_fixed + t_map + t_p0:.2f}s + "
+            f"{iters}x{t_iter:.2f}s/iter")
     return total, nthr, text
 
 
@@ -255,7 +265,7 @@ def run_ours(args):
     achieved = bytes_per[best] / (avg_ms * 1e-3) / 1e9
     peak, peak_kind = measured_peaks()
     traffic = ncu_traffic(best, args.config)
-    cpu_s, cores, text = cpu_sample(acq, cfg["iterations"])
+    cpu_s, cores, text = cpu_sample(acq, cfg["iterations"], cfg["goldstein"])
     tomos = world * args.steps
     line = {
         "metric": "tomograms/s (hologram->RI)",
@@ -298,7 +308,7 @@ def run_reference(args):
     acq = make_workload(args.config, seed=1000)
     times = []
     for k in range(args.warmup + args.steps):
-        s, cores, text = cpu_sample(acq, cfg["iterations"])
+        s, cores, text = cpu_sample(acq, cfg["iterations"], cfg["goldstein"])
         if k >= args.warmup:
             times.append(s)
     per = sum(times) / len(times)
@@ -328,10 +338,10 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="plain_small", choices=sorted(CONFIGS))
+    ap.add_argument("--config", default="wrap_heavy", choices=sorted(CONFIGS))
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

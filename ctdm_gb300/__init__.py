@@ -119,6 +119,14 @@ class Context:
         check(self.lib.ctdm_ctx_buffer(self.handle, int(which), ctypes.byref(p), ctypes.byref(n)), "ctdm_ctx_buffer")
         return p.value, n.value
 
+    def read_buffer(self, which, dtype):
+        """Host copy of a context buffer (see ctdm_ctx_buffer) as a flat numpy array."""
+        _, n = self.buffer(which)
+        out = np.empty(n // np.dtype(dtype).itemsize, dtype)
+        check(self.lib.ctdm_ctx_read_buffer(self.handle, int(which), out.ctypes.data, out.nbytes),
+              "ctdm_ctx_read_buffer")
+        return out
+
     # -- stages (device pointers) ----------------------------------------------
     def qpi(self, n, m, holo, bg, phase, amp, n_angles, bg_per_angle=False, carrier=(-1, -1, -1), stream=None):
         c = (ctypes.c_int * 3)(*carrier)
@@ -140,6 +148,12 @@ class Context:
                                      _stream(stream))
         if rc not in (0, 5):
             check(rc, "ctdm_goldstein")
+        return list(st)
+
+    def goldstein_fill(self, cuts, phi, out, n_maps, w, h, stream=None):
+        st = (ctypes.c_int * n_maps)()
+        check(self.lib.ctdm_goldstein_fill(self.handle, n_maps, w, h, _ptr(cuts), _ptr(phi), _ptr(out), st,
+                                           _stream(stream)), "ctdm_goldstein_fill")
         return list(st)
 
     def prepare_spectra(self, phase, amp, U, n_angles, m, n, r, stream=None):

@@ -32,6 +32,8 @@ _SIGS = {
     "ctdm_ctx_destroy": (None, [c_void_p]),
     "ctdm_ctx_carrier": (c_int, [c_void_p, P_int]),
     "ctdm_ctx_buffer": (c_int, [c_void_p, c_int, ctypes.POINTER(c_void_p), ctypes.POINTER(c_size_t)]),
+    "ctdm_ctx_read_buffer": (c_int, [c_void_p, c_int, c_void_p, c_size_t]),
+    "ctdm_goldstein_fill": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, P_int, c_void_p]),
     "ctdm_ctx_set_timing": (c_int, [c_void_p, c_int]),
     "ctdm_ctx_stage_times": (c_int, [c_void_p, ctypes.POINTER(c_double), P_int, c_int]),
     "ctdm_launch_count": (ctypes.c_ulonglong, []),

@@ -315,6 +315,19 @@ extern "C" ctdm_status ctdm_ctx_carrier(ctdm_ctx *c, int *carrier3)
     return CTDM_OK;
 }
 
+extern "C" ctdm_status ctdm_ctx_read_buffer(ctdm_ctx *c, int which, void *host, size_t bytes)
+{
+    void *d = nullptr;
+    size_t n = 0;
+    ctdm_status st = ctdm_ctx_buffer(c, which, &d, &n);
+    if (st != CTDM_OK) return st;
+    if (!host || !d) return invalid("ctdm_ctx_read_buffer: buffer %d not allocated", which);
+    CK(cudaSetDevice(c->device), "cudaSetDevice");
+    CK(cudaDeviceSynchronize(), "synchronise");
+    CK(cudaMemcpy(host, d, bytes < n ? bytes : n, cudaMemcpyDeviceToHost), "read buffer");
+    return CTDM_OK;
+}
+
 extern "C" ctdm_status ctdm_ctx_buffer(ctdm_ctx *c, int which, void **dptr, size_t *bytes)
 {
     static const int map[] = {B_PHASE, B_AMP, B_PHU, B_CHG, B_CUT, B_GOLD, B_U, B_F2, B_COUNTS};
@@ -491,7 +504,7 @@ extern "C" ctdm_status ctdm_reconstruct_device(ctdm_ctx *c, const ctdm_params *p
         CK(ensure(c, B_CUT, A * mm), "alloc cuts");
         CK(ensure(c, B_GOLD, sizeof(float) * A * mm), "alloc goldstein out");
         CK(ensure(c, B_GSTATE, A * mm), "alloc goldstein state");
-        CK(ensure(c, B_GLIST, sizeof(int) * 2 * A * mm), "alloc goldstein lists");
+        CK(ensure(c, B_GLIST, sizeof(int) * 3 * A * mm), "alloc goldstein lists");
         CK(ensure(c, B_GSTATUS, sizeof(int) * A), "alloc goldstein status");
         CK(goldstein_residues(B<float>(c, B_PHASE), A, M, M, B<int8_t>(c, B_CHG), s), "goldstein residues");
         CK(goldstein_cuts(B<int8_t>(c, B_CHG), A, M, M, B<uint8_t>(c, B_CUT), reinterpret_cast<int8_t *>(B<float>(c, B_DCT)),
@@ -620,7 +633,7 @@ extern "C" ctdm_status ctdm_goldstein(ctdm_ctx *c, int A, int W, int H, const fl
     cudaStream_t s = (cudaStream_t)stream;
     const long n = (long)W * H;
     CK(ensure(c, B_GSTATE, A * n), "alloc state");
-    CK(ensure(c, B_GLIST, sizeof(int) * 2 * A * n), "alloc lists");
+    CK(ensure(c, B_GLIST, sizeof(int) * 3 * A * n), "alloc lists");
     CK(ensure(c, B_GSTATUS, sizeof(int) * A), "alloc status");
     CK(ensure(c, B_TMP, A * n), "alloc work");
     CK(goldstein_residues(d_phi, A, W, H, d_charges, s), "residues");
@@ -638,6 +651,27 @@ extern "C" ctdm_status ctdm_goldstein(ctdm_ctx *c, int A, int W, int H, const fl
         set_err("ctdm_goldstein: flood fill stopped early on at least one map");
         return CTDM_ERR_STALLED;
     }
+    return CTDM_OK;
+}
+
+extern "C" ctdm_status ctdm_goldstein_fill(ctdm_ctx *c, int A, int W, int H, const uint8_t *d_cuts,
+                                           const float *d_phi, float *d_out, int *h_status, void *stream)
+{
+    if (!c || !d_cuts || !d_phi || !d_out) return invalid("ctdm_goldstein_fill: NULL argument");
+    if (W < 4 || H < 4 || W > 1024 || H > 1024 || A < 1) return invalid("ctdm_goldstein_fill: size unsupported");
+    CK(cudaSetDevice(c->device), "cudaSetDevice");
+    cudaStream_t s = (cudaStream_t)stream;
+    const long n = (long)W * H;
+    CK(ensure(c, B_GSTATE, A * n), "alloc state");
+    CK(ensure(c, B_GLIST, sizeof(int) * 3 * A * n), "alloc lists");
+    CK(ensure(c, B_GSTATUS, sizeof(int) * A), "alloc status");
+    CK(goldstein_floodfill(d_cuts, d_phi, A, W, H, d_out, B<uint8_t>(c, B_GSTATE), B<int>(c, B_GLIST),
+                           B<int>(c, B_GSTATUS), s),
+       "flood fill");
+    std::vector<int> stv(A);
+    CK(cudaMemcpyAsync(stv.data(), c->buf[B_GSTATUS], sizeof(int) * A, cudaMemcpyDeviceToHost, s), "status");
+    CK(cudaStreamSynchronize(s), "synchronise");
+    if (h_status) std::memcpy(h_status, stv.data(), sizeof(int) * A);
     return CTDM_OK;
 }
 

@@ -110,9 +110,12 @@ def rytov_field(ells, n_med, wavelength, n, pixel, ang_x, ang_y):
     ny = sgn[:, None] * dfh
     rad = fm0 * fm0 - (nx + fx0) ** 2 - (ny + fy0) ** 2
     ok = rad > 0
-    fz = np.sqrt(np.where(ok, rad, 1.0))
-    fhat = potential_hat(ells, n_med, wavelength, nx, ny, np.where(ok, fz - fz0, 0.0))
-    spec = np.where(ok, fhat / (1j * 4 * np.pi * fz) / (pixel * pixel), 0.0)
+    iy, ix = np.nonzero(ok)                    # the field spectrum lives on the Ewald cap only
+    kx, ky = nx[0, ix], ny[iy, 0]
+    fz = np.sqrt(rad[iy, ix])
+    fhat = potential_hat(ells, n_med, wavelength, kx, ky, fz - fz0)
+    spec = np.zeros((n, n), np.complex128)
+    spec[iy, ix] = fhat / (1j * 4 * np.pi * fz) / (pixel * pixel)
     ut_shift = np.fft.ifft2(spec)              # DFT2(u_shifted) = spec, [Ny, Nx] layout
     ut = np.fft.fftshift(ut_shift)             # undo the quadrant swap
     return ut.T                                # CopyDataArray transposes: hologram [y, x]

@@ -92,6 +92,8 @@ CTDM_API ctdm_status ctdm_ctx_carrier(ctdm_ctx *ctx, int *carrier3);
  * 4 Goldstein cuts (u8), 5 Goldstein unwrapped (f32), 6 spectra U (A*R*R c64),
  * 7 F2 (R^3 c64), 8 hit counts (R^3 u32, only with CTDM_CHECK_MASK). */
 CTDM_API ctdm_status ctdm_ctx_buffer(ctdm_ctx *ctx, int which, void **dptr, size_t *bytes);
+/* Copies min(bytes, size) of buffer `which` (see ctdm_ctx_buffer) to host memory (synchronous). */
+CTDM_API ctdm_status ctdm_ctx_read_buffer(ctdm_ctx *ctx, int which, void *host, size_t bytes);
 /* Stage timing with CUDA events on the call's stream (off by default).  Stages:
  * 0 QPI, 1 unwrap, 2 Goldstein, 3 spectra (prep + FFT2), 4 Ewald mapping,
  * 5 y inverse pass, 6 x pass (loop), 7 y forward pass, 8 z pass, 9 final x pass.
@@ -125,6 +127,9 @@ CTDM_API ctdm_status ctdm_unwrap_fast(ctdm_ctx *ctx, int A, int M, float *d_phi,
  * h_status (A ints, may be NULL): 0 done, 1 sweep limit reached, 2 stalled. */
 CTDM_API ctdm_status ctdm_goldstein(ctdm_ctx *ctx, int A, int W, int H, const float *d_phi, int8_t *d_charges,
                            uint8_t *d_cuts, float *d_out, int *h_status, void *stream);
+/* Flood fill alone with caller-provided branch cuts (0/1 per pixel). */
+CTDM_API ctdm_status ctdm_goldstein_fill(ctdm_ctx *ctx, int A, int W, int H, const uint8_t *d_cuts, const float *d_phi,
+                                         float *d_out, int *h_status, void *stream);
 /* Resize M -> N, centre crop R, median + checkMaps, u = log A + i phi (transposed,
  * quadrant-swapped), forward FFT2: d_U (A*R*R complex). */
 CTDM_API ctdm_status ctdm_prepare_spectra(ctdm_ctx *ctx, int A, int M, int N, int R, const float *d_phase,
