@@ -504,7 +504,7 @@ extern "C" ctdm_status ctdm_reconstruct_device(ctdm_ctx *c, const ctdm_params *p
         CK(ensure(c, B_CUT, A * mm), "alloc cuts");
         CK(ensure(c, B_GOLD, sizeof(float) * A * mm), "alloc goldstein out");
         CK(ensure(c, B_GSTATE, A * mm), "alloc goldstein state");
-        CK(ensure(c, B_GLIST, sizeof(int) * 3 * A * mm), "alloc goldstein lists");
+        CK(ensure(c, B_GLIST, sizeof(int) * 5 * A * mm), "alloc goldstein lists");
         CK(ensure(c, B_GSTATUS, sizeof(int) * A), "alloc goldstein status");
         CK(goldstein_residues(B<float>(c, B_PHASE), A, M, M, B<int8_t>(c, B_CHG), s), "goldstein residues");
         CK(goldstein_cuts(B<int8_t>(c, B_CHG), A, M, M, B<uint8_t>(c, B_CUT), reinterpret_cast<int8_t *>(B<float>(c, B_DCT)),
@@ -633,7 +633,7 @@ extern "C" ctdm_status ctdm_goldstein(ctdm_ctx *c, int A, int W, int H, const fl
     cudaStream_t s = (cudaStream_t)stream;
     const long n = (long)W * H;
     CK(ensure(c, B_GSTATE, A * n), "alloc state");
-    CK(ensure(c, B_GLIST, sizeof(int) * 3 * A * n), "alloc lists");
+    CK(ensure(c, B_GLIST, sizeof(int) * 5 * A * n), "alloc lists");
     CK(ensure(c, B_GSTATUS, sizeof(int) * A), "alloc status");
     CK(ensure(c, B_TMP, A * n), "alloc work");
     CK(goldstein_residues(d_phi, A, W, H, d_charges, s), "residues");
@@ -663,7 +663,7 @@ extern "C" ctdm_status ctdm_goldstein_fill(ctdm_ctx *c, int A, int W, int H, con
     cudaStream_t s = (cudaStream_t)stream;
     const long n = (long)W * H;
     CK(ensure(c, B_GSTATE, A * n), "alloc state");
-    CK(ensure(c, B_GLIST, sizeof(int) * 3 * A * n), "alloc lists");
+    CK(ensure(c, B_GLIST, sizeof(int) * 5 * A * n), "alloc lists");
     CK(ensure(c, B_GSTATUS, sizeof(int) * A), "alloc status");
     CK(goldstein_floodfill(d_cuts, d_phi, A, W, H, d_out, B<uint8_t>(c, B_GSTATE), B<int>(c, B_GLIST),
                            B<int>(c, B_GSTATUS), s),

@@ -202,16 +202,21 @@ cudaError_t goldstein_cuts(const int8_t *charges, int A, int W, int H, uint8_t *
 }
 
 // ------------------------------------------------------------ flood fill
+// State bits per pixel.  The active ("adjoin") set of each sweep is an unsorted
+// list: the visiting order matters only through index comparisons, and two
+// consecutive lists are identical exactly when they have the same length and
+// every entry of the new one was in the old one (F_PREV).
 enum : unsigned {
-    F_CUT = 1u, F_UB = 2u, F_ADJ = 4u, F_LIST = 8u, F_NEW = 16u, F_CAND = 32u, F_READY = 64u, F_MARK = 128u
+    F_CUT = 1u, F_UB = 2u, F_PREV = 4u, F_LIST = 8u, F_NEW = 16u, F_CAND = 32u, F_READY = 64u, F_MARK = 128u
 };
 constexpr int FF_THREADS = 512;
 
-__device__ __forceinline__ void byte_or(uint8_t *p, unsigned bits)
+__device__ __forceinline__ unsigned byte_or(uint8_t *p, unsigned bits)
 {
     const uintptr_t addr = reinterpret_cast<uintptr_t>(p);
     unsigned *w = reinterpret_cast<unsigned *>(addr & ~(uintptr_t)3);
-    atomicOr(w, bits << (8 * (addr & 3)));
+    const unsigned sh = 8u * (unsigned)(addr & 3);
+    return (atomicOr(w, bits << sh) >> sh) & 0xffu;
 }
 
 // neighbour k of p in the reference's order: below (p+1), above (p-1), right
@@ -247,41 +252,18 @@ __device__ __forceinline__ float unwrap_from(float ref, float ph)
     return __fadd_rn(ref, dp);
 }
 
-// Raster-ordered compaction of the pixels whose state has `bit`; sets F_LIST.
-__device__ int compact(uint8_t *st, long n, int *list, int *scan)
-{
-    const int t = threadIdx.x;
-    const long seg = (n + FF_THREADS - 1) / FF_THREADS;
-    const long b0 = t * seg, b1 = min(n, b0 + seg);
-    int c = 0;
-    for (long p = b0; p < b1; p++) c += (st[p] & F_ADJ) != 0;
-    scan[t] = c;
-    __syncthreads();
-    for (int off = 1; off < FF_THREADS; off <<= 1) {
-        const int v = t >= off ? scan[t - off] : 0;
-        __syncthreads();
-        scan[t] += v;
-        __syncthreads();
-    }
-    int pos = scan[t] - c;
-    const int total = scan[FF_THREADS - 1];
-    for (long p = b0; p < b1; p++) {
-        const unsigned s = st[p];
-        if (s & F_ADJ) {
-            list[pos++] = (int)p;
-            st[p] = (uint8_t)(s | F_LIST);
-        }
-    }
-    __syncthreads();
-    return total;
-}
+struct FFLists {
+    int *cur, *nxt, *prev, *ref;
+    float *nv;
+};
 
-// One sweep over the raster-ordered list (use_cuts: main loop; else the final
-// cut-pixel fill, which ignores cuts and makes no marks).
-__device__ void sweep(uint8_t *st, const int *list, int L, int *ref, const float *ph, float *o, float *nv, int W, int H,
+// One sweep over the list (use_cuts: main loop; else the final cut-pixel fill,
+// which ignores cuts and makes no marks).  Marks append to lists.nxt.
+__device__ void sweep(uint8_t *st, const FFLists &ls, int L, int *nnext, const float *ph, float *o, int W, int H,
                       bool use_cuts)
 {
     const int t = threadIdx.x;
+    const int *list = ls.cur;
     // candidates from states that cannot change before the visit
     for (int e = t; e < L; e += FF_THREADS) {
         const int p = list[e];
@@ -321,8 +303,8 @@ __device__ void sweep(uint8_t *st, const int *list, int L, int *ref, const float
         }
         if (!__syncthreads_or(changed)) break;
     }
-    // reference neighbour (first unwrapped in visiting order), values of the
-    // pixels whose reference is not recomputed in this sweep
+    // reference neighbour (first unwrapped in visiting order) and the values whose
+    // reference is not recomputed in this sweep
     for (int e = t; e < L; e += FF_THREADS) {
         const int p = list[e];
         const unsigned s = st[p];
@@ -334,18 +316,18 @@ __device__ void sweep(uint8_t *st, const int *list, int L, int *ref, const float
             if (use_cuts && (st[nb] & F_CUT)) continue;
             if (ub_at_visit(st, nb, p)) chosen = nb;
         }
-        ref[e] = chosen;
+        ls.ref[e] = chosen;
     }
     __syncthreads();
     for (int e = t; e < L; e += FF_THREADS) {
         const int p = list[e];
         const unsigned s = st[p];
         if (!(s & F_CAND)) continue;
-        const int nb = ref[e];
+        const int nb = ls.ref[e];
         const unsigned sn = st[nb];
         const bool dep = (sn & F_LIST) && nb < p && (sn & F_CAND);
         if (!dep) {
-            nv[p] = unwrap_from(o[nb], ph[p]);
+            ls.nv[p] = unwrap_from(o[nb], ph[p]);
             st[p] = (uint8_t)(s | F_READY);
         }
     }
@@ -356,9 +338,9 @@ __device__ void sweep(uint8_t *st, const int *list, int L, int *ref, const float
             const int p = list[e];
             const unsigned s = st[p];
             if (!(s & F_CAND) || (s & F_READY)) continue;
-            const int nb = ref[e];
+            const int nb = ls.ref[e];
             if (st[nb] & F_READY) {
-                nv[p] = unwrap_from(nv[nb], ph[p]);
+                ls.nv[p] = unwrap_from(ls.nv[nb], ph[p]);
                 st[p] = (uint8_t)(s | F_READY);
             } else {
                 pending = true;
@@ -368,7 +350,7 @@ __device__ void sweep(uint8_t *st, const int *list, int L, int *ref, const float
     }
     // adjoin marks for the next sweep: a visit marks each usable neighbour that is
     // not unwrapped at that time; a list pixel keeps only the marks made after its
-    // own visit
+    // own visit.  The first mark of a pixel appends it to the next list.
     if (use_cuts) {
         for (int e = t; e < L; e += FF_THREADS) {
             const int p = list[e];
@@ -378,7 +360,9 @@ __device__ void sweep(uint8_t *st, const int *list, int L, int *ref, const float
                 const unsigned sn = st[nb];
                 if (sn & F_CUT) continue;
                 if (ub_at_visit(st, nb, p)) continue;
-                if (!(sn & F_LIST) || nb < p) byte_or(st + nb, F_MARK);
+                if (!(sn & F_LIST) || nb < p) {
+                    if (!(byte_or(st + nb, F_MARK) & F_MARK)) ls.nxt[atomicAdd(nnext, 1)] = nb;
+                }
             }
         }
     }
@@ -386,22 +370,10 @@ __device__ void sweep(uint8_t *st, const int *list, int L, int *ref, const float
     for (int e = t; e < L; e += FF_THREADS) {
         const int p = list[e];
         const unsigned s = st[p];
-        if (s & F_CAND) o[p] = nv[p];
-        st[p] = (uint8_t)((s & (F_CUT | F_MARK)) | ((s & F_NEW) ? F_UB : 0u));
+        if (s & F_CAND) o[p] = ls.nv[p];
+        st[p] = (uint8_t)((s & (F_CUT | F_MARK)) | ((s & F_NEW) ? F_UB : 0u) | F_PREV);
     }
     __syncthreads();
-    if (use_cuts) {
-        for (int e = t; e < L; e += FF_THREADS) {
-            const int p = list[e];
-            for (int k = 0; k < 4; k++) {
-                int nb;
-                if (!neighbour(p, k, W, H, nb)) continue;
-                const unsigned sn = st[nb];
-                if (sn & F_MARK) st[nb] = (uint8_t)((sn & ~F_MARK) | F_ADJ);
-            }
-        }
-        __syncthreads();
-    }
 }
 
 template <bool SMEM>
@@ -410,17 +382,20 @@ __global__ void __launch_bounds__(FF_THREADS) floodfill_kernel(const uint8_t *__
                                                               uint8_t *gstate, int *lists, int *status)
 {
     extern __shared__ uint8_t sstate[];
-    __shared__ int scan[FF_THREADS];
-    __shared__ int s_ok, s_sum;
+    __shared__ int s_ok, s_nnext;
     const int a = blockIdx.x, t = threadIdx.x;
     const long n = (long)W * H;
     uint8_t *st = SMEM ? sstate : gstate + a * n;
     const uint8_t *cut = cuts + a * n;
     const float *ph = phi + a * n;
     float *o = out + a * n;
-    int *listA = lists + a * 3 * n;
-    int *listB = listA + n;
-    float *nv = reinterpret_cast<float *>(listB + n);
+    int *base = lists + a * 5 * n;
+    FFLists ls;
+    ls.cur = base;
+    ls.nxt = base + n;
+    ls.prev = base + 2 * n;
+    ls.ref = base + 3 * n;
+    ls.nv = reinterpret_cast<float *>(base + 4 * n);
     int nbc_local = 0;
     for (long p = t; p < n; p += FF_THREADS) {
         st[p] = cut[p] ? (uint8_t)F_CUT : (uint8_t)0;
@@ -440,65 +415,99 @@ __global__ void __launch_bounds__(FF_THREADS) floodfill_kernel(const uint8_t *__
         }
         const int rowRef = yr, colRef = xr;
         if (ok && (rowRef >= W || colRef >= H)) ok = 0;
+        int cnt = 0;
         if (ok) {
             const long seed = rowRef + (long)W * colRef;
-            if (rowRef > 0) st[seed - 1] |= F_ADJ;
-            if (rowRef < W - 1) st[seed + 1] |= F_ADJ;
-            if (colRef > 0) st[seed - W] |= F_ADJ;
-            if (colRef < H - 1) st[seed + W] |= F_ADJ;
+            const long nbs[4] = {seed - 1, seed + 1, seed - W, seed + W};
+            const bool okn[4] = {rowRef > 0, rowRef < W - 1, colRef > 0, colRef < H - 1};
+            for (int k = 0; k < 4; k++)
+                if (okn[k]) {
+                    st[nbs[k]] |= F_MARK;
+                    ls.nxt[cnt++] = (int)nbs[k];
+                }
             st[seed] |= F_UB;
             o[seed] = ph[seed];
         }
         s_ok = ok;
+        s_nnext = cnt;
     }
     __syncthreads();
     if (!s_ok) {
         if (t == 0) status[a] = 2;
         return;
     }
-    int *list = listA, *prev = listB;
-    int L1 = 0, countLimit = 0, stat = 0;
+    int L1 = 0, Lprev = 0, countLimit = 0, stat = 0;
     bool abort_fill = false;
     for (int outer = 0; outer < 4; outer++) {
-        int c = 0;
-        for (long p = t; p < n; p += FF_THREADS) c += (st[p] & F_ADJ) != 0;
-        if (t == 0) s_sum = 0;
         __syncthreads();
-        if (c) atomicAdd(&s_sum, c);
-        __syncthreads();
-        if (s_sum == 0) break;
+        if (s_nnext == 0) break;
         if (countLimit >= 2) { stat = 2; break; }
         int term = 0;
         while (countLimit < 2) {
             if (++term > 5000) { stat = 1; abort_fill = true; break; }
-            const int L2 = compact(st, n, list, scan);
+            // the marked pixels become this sweep's list
+            int *tmp = ls.prev;
+            ls.prev = ls.cur;
+            ls.cur = ls.nxt;
+            ls.nxt = tmp;
+            __syncthreads();
+            const int L2 = s_nnext;
+            __syncthreads();
+            if (t == 0) s_nnext = 0;
+            bool all_prev = true;
+            for (int e = t; e < L2; e += FF_THREADS) {
+                const int p = ls.cur[e];
+                const unsigned s = st[p];
+                all_prev &= (s & F_PREV) != 0;
+                st[p] = (uint8_t)((s & ~F_MARK) | F_LIST);
+            }
+            const bool same = __syncthreads_and(all_prev);
             if (L1 == L2) {
-                bool diff = false;
-                for (int e = t; e < L2; e += FF_THREADS) diff |= prev[e] != list[e];
-                if (!__syncthreads_or(diff)) countLimit++;
+                if (same) countLimit++;
             } else {
                 countLimit = 0;
             }
-            // prev is free from here on: it holds the reference neighbours
-            sweep(st, list, L2, prev, ph, o, nv, W, H, true);
-            int *tmp = prev;
-            prev = list;
-            list = tmp;
+            for (int e = t; e < Lprev; e += FF_THREADS) {
+                const int p = ls.prev[e];
+                st[p] = (uint8_t)(st[p] & ~F_PREV);
+            }
+            __syncthreads();
+            sweep(st, ls, L2, &s_nnext, ph, o, W, H, true);
             L1 = L2;
+            Lprev = L2;
         }
         if (abort_fill) break;
     }
     if (!abort_fill && nbc > 0) {
-        for (long p = t; p < n; p += FF_THREADS) {
-            const int rr = (int)(p % W), cc = (int)(p / W);
-            if (rr < 1 || rr > W - 2 || cc < 1 || cc > H - 2) continue;
-            if ((st[p] & F_CUT) && (!(st[p + 1] & F_CUT) || !(st[p - 1] & F_CUT) || !(st[p - W] & F_CUT) ||
-                                    !(st[p + W] & F_CUT)))
-                byte_or(st + p, F_ADJ);
+        // final fill of the cut pixels that adjoin unwrapped ones, plus any pixel still
+        // marked (only when the sweeps stalled)
+        __syncthreads();
+        for (int e = t; e < Lprev; e += FF_THREADS) {
+            const int p = ls.cur[e];
+            st[p] = (uint8_t)(st[p] & ~F_PREV);
         }
         __syncthreads();
-        const int L2 = compact(st, n, list, scan);
-        sweep(st, list, L2, prev, ph, o, nv, W, H, false);
+        if (t == 0) s_nnext = 0;
+        __syncthreads();
+        for (long p = t; p < n; p += FF_THREADS) {
+            const unsigned s = st[p];
+            const int rr = (int)(p % W), cc = (int)(p / W);
+            bool add = (s & F_MARK) != 0;
+            if (!add && (s & F_CUT) && rr >= 1 && rr <= W - 2 && cc >= 1 && cc <= H - 2)
+                add = !(st[p + 1] & F_CUT) || !(st[p - 1] & F_CUT) || !(st[p - W] & F_CUT) || !(st[p + W] & F_CUT);
+            if (add) ls.nxt[atomicAdd(&s_nnext, 1)] = (int)p;
+        }
+        __syncthreads();
+        const int L2 = s_nnext;
+        for (int e = t; e < L2; e += FF_THREADS) {
+            const int p = ls.nxt[e];
+            st[p] = (uint8_t)((st[p] & ~F_MARK) | F_LIST);
+        }
+        int *tmp = ls.cur;
+        ls.cur = ls.nxt;
+        ls.nxt = tmp;
+        __syncthreads();
+        sweep(st, ls, L2, &s_nnext, ph, o, W, H, false);
     }
     if (t == 0) status[a] = stat;
 }
