@@ -434,6 +434,8 @@ static ctdm_status do_positivity(ctdm_ctx *c, int R, int iters, int check_mode, 
     la.k2 = (float)k2;
     la.n_med = (float)n_med;
     la.n_med2 = (float)(n_med * n_med);
+    la.s1 = (float)(-1.0 / ((double)R * R * R * k2));
+    la.s2 = (float)(-k2 / (n_med * n_med));
     StageTimer &tm = c->timer;
     CK(launch_ypass(la, true, s), "y inverse pass");
     tm.mark(S_YINV, s);

@@ -2,11 +2,20 @@
 //
 // A CTA holds B lines of length L in shared memory, element p of line b at
 // buf[b * LP + p] (LP = L plus a pad that keeps 64-bit accesses of a half-warp
-// on distinct banks).  Each radix stage loads R strided points per butterfly
+// on distinct banks).  Each radix stage gathers R strided points per butterfly
 // into registers, applies the stage twiddles, runs an in-register radix-R DFT
-// and writes back in Stockham (self-sorting) order, so the output is in natural
-// order without a bit-reversal pass.  Threads are mapped b-fastest: tid -> (b =
-// tid % B, t = tid / B), T threads per line.
+// and scatters back in Stockham (self-sorting) order, so the output is in
+// natural order without a bit-reversal pass.  Threads are mapped b-fastest:
+// tid -> (b = tid % B, t = tid / B), T threads per line, and every thread keeps
+// a register tile of E = L / T points through all stages.
+//
+// Register-resident ends: the first stage of a transform reads points
+// j + r * (L / R0) and the last stage writes points j + r * (L / Rlast) for the
+// butterflies j = t + T q of the thread.  A kernel may therefore load the first
+// stage straight from global memory and store the last one straight back
+// (skipping shared memory), and when a transform is followed by another one
+// whose radix order is reversed, the second starts from the registers the first
+// ended in.
 //
 // Conventions (cuFFT C2C as used by the reference, cTDM/FFT.cu:697-838):
 // forward exp(-2 pi i k n / L), inverse exp(+2 pi i k n / L), both unnormalised.
@@ -41,7 +50,6 @@ template <bool INV>
 __device__ __forceinline__ float2 w8(float2 a, int k)
 {
     const float h = 0.70710678118654752440f;
-    // forward W8^1 = (h, -h), W8^3 = (-h, -h); inverse conjugates
     float2 w = (k == 1) ? make_float2(h, INV ? h : -h) : make_float2(-h, INV ? h : -h);
     return cmul(a, w);
 }
@@ -109,92 +117,138 @@ __device__ __forceinline__ void dftR(float2 *a)
     else if constexpr (R == 16) dft16<INV>(a);
 }
 
-// ---------------------------------------------------------------- plans
-// Per length: radix sequence, lines per CTA (B) and threads per line (T).
-template <int L> struct Plan;
-#define FFTL_PLAN(LL, BB, TT, ...)                                       \
-    template <> struct Plan<LL> {                                       \
-        static constexpr int B = BB, T = TT;                            \
-        static constexpr int PAD = (BB >= 16) ? 1 : (16 / BB);          \
-        static constexpr int LP = LL + PAD;                             \
-        static constexpr int THREADS = BB * TT;                         \
-        template <bool INV>                                             \
-        __device__ static void run(float2 *buf, const float2 *tw);      \
-    };
-FFTL_PLAN(16, 64, 4, 4, 4)
-FFTL_PLAN(32, 64, 4, 8, 4)
-FFTL_PLAN(64, 32, 8, 8, 8)
-FFTL_PLAN(128, 32, 8, 16, 8)
-FFTL_PLAN(256, 16, 16, 16, 16)
-FFTL_PLAN(384, 32, 8, 16, 8, 3)
-FFTL_PLAN(512, 16, 16, 8, 8, 8)
-FFTL_PLAN(768, 16, 16, 16, 16, 3)
-FFTL_PLAN(1024, 8, 32, 16, 16, 4)
-FFTL_PLAN(1536, 8, 32, 16, 16, 3, 2)
-FFTL_PLAN(2048, 4, 64, 16, 16, 8)
-#undef FFTL_PLAN
-
-// One Stockham stage of radix R with span NS (product of the earlier radices).
-template <int L, int B, int T, int LP, bool INV, int NS, int R>
-__device__ __forceinline__ void stage(float2 *buf, const float2 *__restrict__ tw, int b, int t)
+// ---------------------------------------------------------------- one stage
+// Register tile v[E], E = L / T, viewed as PER butterflies of R points.
+template <int L, int T, int LP, int R>
+__device__ __forceinline__ void gather(const float2 *buf, float2 *v, int b, int t)
 {
-    constexpr int NB = L / R;       // butterflies per line
-    constexpr int PER = NB / T;     // butterflies per thread
+    constexpr int NB = L / R, PER = NB / T;
+    const float2 *line = buf + b * LP;
+#pragma unroll
+    for (int q = 0; q < PER; q++)
+#pragma unroll
+        for (int r = 0; r < R; r++) v[q * R + r] = line[t + T * q + r * NB];
+}
+
+template <int L, int T, bool INV, int NS, int R>
+__device__ __forceinline__ void compute(float2 *v, const float2 *__restrict__ tw, int t)
+{
+    constexpr int NB = L / R, PER = NB / T;
     static_assert(NB % T == 0, "threads per line must divide the butterfly count");
-    float2 v[PER][R];
+#pragma unroll
+    for (int q = 0; q < PER; q++) {
+        if constexpr (NS > 1) {
+            const int k = (t + T * q) % NS;
+#pragma unroll
+            for (int r = 1; r < R; r++) {
+                const float2 w = __ldg(&tw[r * k * (L / (NS * R))]);
+                v[q * R + r] = INV ? cmulc(v[q * R + r], w) : cmul(v[q * R + r], w);
+            }
+        }
+        dftR<R, INV>(v + q * R);
+    }
+}
+
+template <int L, int T, int LP, int NS, int R>
+__device__ __forceinline__ void scatter(float2 *buf, const float2 *v, int b, int t)
+{
+    constexpr int NB = L / R, PER = NB / T;
     float2 *line = buf + b * LP;
 #pragma unroll
     for (int q = 0; q < PER; q++) {
         const int j = t + T * q;
+        const int base = (j / NS) * NS * R + (j % NS);
 #pragma unroll
-        for (int r = 0; r < R; r++) v[q][r] = line[j + r * NB];
+        for (int r = 0; r < R; r++) line[base + r * NS] = v[q * R + r];
     }
-    __syncthreads();
-#pragma unroll
-    for (int q = 0; q < PER; q++) {
-        const int j = t + T * q;
-        const int k = j % NS;
-        if constexpr (NS > 1) {
-#pragma unroll
-            for (int r = 1; r < R; r++) {
-                float2 w = __ldg(&tw[r * k * (L / (NS * R))]);
-                v[q][r] = INV ? cmulc(v[q][r], w) : cmul(v[q][r], w);
-            }
-        }
-        dftR<R, INV>(v[q]);
-        const int base = (j / NS) * NS * R + k;
-#pragma unroll
-        for (int r = 0; r < R; r++) line[base + r * NS] = v[q][r];
-    }
-    __syncthreads();
 }
 
-template <int L, int B, int T, int LP, bool INV, int NS, int R, int... REST>
-__device__ __forceinline__ void stages(float2 *buf, const float2 *__restrict__ tw, int b, int t)
+// Stages in the order given.  GATHER0: the first stage reads shared memory
+// (else its inputs are already in v).  SCATTER_LAST: the last stage writes shared
+// memory (else its outputs stay in v).
+template <int L, int T, int LP, bool INV, bool GATHER0, bool SCATTER_LAST, int NS, int R, int... REST>
+__device__ __forceinline__ void stages(float2 *buf, float2 *v, const float2 *__restrict__ tw, int b, int t)
 {
-    stage<L, B, T, LP, INV, NS, R>(buf, tw, b, t);
-    if constexpr (sizeof...(REST) > 0) stages<L, B, T, LP, INV, NS * R, REST...>(buf, tw, b, t);
+    constexpr bool first = (NS == 1);
+    constexpr bool last = (sizeof...(REST) == 0);
+    if constexpr (!first || GATHER0) {
+        gather<L, T, LP, R>(buf, v, b, t);
+        __syncthreads();
+    }
+    compute<L, T, INV, NS, R>(v, tw, t);
+    if constexpr (!last || SCATTER_LAST) {
+        scatter<L, T, LP, NS, R>(buf, v, b, t);
+        __syncthreads();
+    }
+    if constexpr (!last) stages<L, T, LP, INV, GATHER0, SCATTER_LAST, NS * R, REST...>(buf, v, tw, b, t);
 }
 
-#define FFTL_RUN(LL, ...)                                                                  \
-    template <bool INV>                                                                   \
-    __device__ __forceinline__ void Plan<LL>::run(float2 *buf, const float2 *tw)          \
-    {                                                                                     \
-        const int b = threadIdx.x % B, t = threadIdx.x / B;                              \
-        stages<LL, B, T, LP, INV, 1, __VA_ARGS__>(buf, tw, b, t);                         \
-    }
-FFTL_RUN(16, 4, 4)
-FFTL_RUN(32, 8, 4)
-FFTL_RUN(64, 8, 8)
-FFTL_RUN(128, 16, 8)
-FFTL_RUN(256, 16, 16)
-FFTL_RUN(384, 16, 8, 3)
-FFTL_RUN(512, 8, 8, 8)
-FFTL_RUN(768, 16, 16, 3)
-FFTL_RUN(1024, 16, 16, 4)
-FFTL_RUN(1536, 16, 16, 3, 2)
-FFTL_RUN(2048, 16, 16, 8)
-#undef FFTL_RUN
+// ---------------------------------------------------------------- plans
+// Per length: lines per CTA (B), threads per line (T), radix sequence.  run()
+// uses the sequence as listed, runr() the reversed one.
+template <int L> struct Plan;
+#define FFTL_PLAN(LL, BB, TT, FWD, REV)                                                             \
+    template <> struct Plan<LL> {                                                                   \
+        static constexpr int B = BB, T = TT;                                                        \
+        static constexpr int PAD = (BB >= 16) ? 1 : (16 / BB);                                      \
+        static constexpr int LP = LL + PAD;                                                         \
+        static constexpr int THREADS = BB * TT;                                                     \
+        static constexpr int E = LL / TT;                                                           \
+        /* first / last radix of the listed order (the reversed order swaps them) */                \
+        template <bool INV, bool GATHER0, bool SCATTER_LAST>                                        \
+        __device__ static __forceinline__ void seq(float2 *buf, float2 *v, const float2 *tw)        \
+        {                                                                                           \
+            stages<LL, TT, LP, INV, GATHER0, SCATTER_LAST, 1, FWD>(buf, v, tw, threadIdx.x % BB,    \
+                                                                   threadIdx.x / BB);               \
+        }                                                                                           \
+        template <bool INV, bool GATHER0, bool SCATTER_LAST>                                        \
+        __device__ static __forceinline__ void seqr(float2 *buf, float2 *v, const float2 *tw)       \
+        {                                                                                           \
+            stages<LL, TT, LP, INV, GATHER0, SCATTER_LAST, 1, REV>(buf, v, tw, threadIdx.x % BB,    \
+                                                                   threadIdx.x / BB);               \
+        }                                                                                           \
+        template <bool INV>                                                                         \
+        __device__ static __forceinline__ void run(float2 *buf, const float2 *tw)                   \
+        {                                                                                           \
+            float2 v[E];                                                                            \
+            seq<INV, true, true>(buf, v, tw);                                                       \
+        }                                                                                           \
+    };
+#define FFTL_LIST(...) __VA_ARGS__
+FFTL_PLAN(16, 64, 4, FFTL_LIST(4, 4), FFTL_LIST(4, 4))
+FFTL_PLAN(32, 64, 4, FFTL_LIST(8, 4), FFTL_LIST(4, 8))
+FFTL_PLAN(64, 32, 8, FFTL_LIST(8, 8), FFTL_LIST(8, 8))
+FFTL_PLAN(128, 32, 8, FFTL_LIST(16, 8), FFTL_LIST(8, 16))
+FFTL_PLAN(256, 16, 16, FFTL_LIST(16, 16), FFTL_LIST(16, 16))
+FFTL_PLAN(384, 32, 8, FFTL_LIST(16, 8, 3), FFTL_LIST(3, 8, 16))
+FFTL_PLAN(512, 16, 16, FFTL_LIST(8, 8, 8), FFTL_LIST(8, 8, 8))
+FFTL_PLAN(768, 16, 16, FFTL_LIST(16, 16, 3), FFTL_LIST(3, 16, 16))
+FFTL_PLAN(1024, 8, 32, FFTL_LIST(16, 16, 4), FFTL_LIST(4, 16, 16))
+FFTL_PLAN(1536, 8, 32, FFTL_LIST(16, 16, 3, 2), FFTL_LIST(2, 3, 16, 16))
+FFTL_PLAN(2048, 4, 64, FFTL_LIST(16, 16, 8), FFTL_LIST(8, 16, 16))
+#undef FFTL_PLAN
+
+// First radix of the listed (forward) sequence and of the reversed one.
+template <int L> struct Ends;
+template <> struct Ends<16> { static constexpr int F = 4, Rv = 4; };
+template <> struct Ends<32> { static constexpr int F = 8, Rv = 4; };
+template <> struct Ends<64> { static constexpr int F = 8, Rv = 8; };
+template <> struct Ends<128> { static constexpr int F = 16, Rv = 8; };
+template <> struct Ends<256> { static constexpr int F = 16, Rv = 16; };
+template <> struct Ends<384> { static constexpr int F = 16, Rv = 3; };
+template <> struct Ends<512> { static constexpr int F = 8, Rv = 8; };
+template <> struct Ends<768> { static constexpr int F = 16, Rv = 3; };
+template <> struct Ends<1024> { static constexpr int F = 16, Rv = 4; };
+template <> struct Ends<1536> { static constexpr int F = 16, Rv = 2; };
+template <> struct Ends<2048> { static constexpr int F = 16, Rv = 8; };
+
+// Point index of register slot i (butterfly q = i / R, point r = i % R) at the
+// register-resident end of a sequence whose end radix is R: j + r * (L / R).
+template <int L, int T, int R>
+__device__ __forceinline__ int slot_pos(int i, int t)
+{
+    return (t + T * (i / R)) + (i % R) * (L / R);
+}
 
 template <int L>
 __host__ __device__ constexpr size_t smem_bytes()

@@ -332,6 +332,9 @@ __device__ void sweep(uint8_t *st, const FFLists &ls, int L, int *nnext, const f
         }
     }
     __syncthreads();
+    // dependency rounds: a value computed in a round is published (F_READY) only
+    // after the round's barrier, so a reader never sees the flag before the value.
+    // F_PREV is unused during a sweep and marks "computed in this round".
     for (int guard = 0; guard <= L; guard++) {
         bool pending = false;
         for (int e = t; e < L; e += FF_THREADS) {
@@ -341,10 +344,16 @@ __device__ void sweep(uint8_t *st, const FFLists &ls, int L, int *nnext, const f
             const int nb = ls.ref[e];
             if (st[nb] & F_READY) {
                 ls.nv[p] = unwrap_from(ls.nv[nb], ph[p]);
-                st[p] = (uint8_t)(s | F_READY);
+                st[p] = (uint8_t)(s | F_PREV);
             } else {
                 pending = true;
             }
+        }
+        __syncthreads();
+        for (int e = t; e < L; e += FF_THREADS) {
+            const int p = list[e];
+            const unsigned s = st[p];
+            if (s & F_PREV) st[p] = (uint8_t)((s & ~F_PREV) | F_READY);
         }
         if (!__syncthreads_or(pending)) break;
     }

@@ -105,15 +105,22 @@ template <int L, bool INV>
 __global__ void __launch_bounds__(Plan<L>::THREADS) cols_kernel(float2 *data, const float2 *__restrict__ tw, long nlines,
                                                                 int nx, long plane, long ld)
 {
+    using P = Plan<L>;
+    using En = fftl::Ends<L>;
     extern __shared__ float4 smem4[];
     float2 *buf = reinterpret_cast<float2 *>(smem4);
-    const long line0 = (long)blockIdx.x * Plan<L>::B;
+    const long line0 = (long)blockIdx.x * P::B;
     bool ok;
     const long base = col_base<L>(line0, nx, plane, nlines, ok);
-    load_cols<L>(buf, data, base, ok, ld);
-    __syncthreads();
-    Plan<L>::template run<INV>(buf, tw);
-    store_cols<L>(data, buf, base, ok, ld);
+    const int t = threadIdx.x / P::B;
+    float2 v[P::E];
+#pragma unroll
+    for (int i = 0; i < P::E; i++)
+        v[i] = ok ? __ldcs(&data[base + (long)fftl::slot_pos<L, P::T, En::F>(i, t) * ld]) : make_float2(0.f, 0.f);
+    P::template seq<INV, false, false>(buf, v, tw);
+    if (!ok) return;
+#pragma unroll
+    for (int i = 0; i < P::E; i++) __stcs(&data[base + (long)fftl::slot_pos<L, P::T, En::Rv>(i, t) * ld], v[i]);
 }
 
 template <int L, class K>
@@ -199,25 +206,24 @@ __global__ void __launch_bounds__(Plan<L>::THREADS) xpass_kernel(LoopArgs a, con
     const long line0 = (long)blockIdx.x * P::B;
     load_rows<L>(buf, a.G, line0, nl);
     __syncthreads();
-    P::template run<true>(buf, tw);
     if constexpr (FINAL) {
+        P::template run<true>(buf, tw);
         // est_n then the octant shift (cuFFT3Dshift, cTDM/FFT.cu:324-350) on the write
         for (int e = threadIdx.x; e < P::B * L; e += P::THREADS) {
             const int b = e / L, p = e - b * L;
             const long l = line0 + b;
             const int y = (int)(l % L), z = (int)(l / L);
-            float2 v = cscale(buf[b * P::LP + p], a.inv_n3);
             const long o = (long)((p + L / 2) % L) + (long)L * ((y + L / 2) % L) + (long)L * L * ((z + L / 2) % L);
-            a.out[o] = est_n(v, a.k2, a.n_med);
+            a.out[o] = est_n_scaled(buf[b * P::LP + p], a.s1, a.n_med);
         }
     } else {
-        for (int e = threadIdx.x; e < P::B * L; e += P::THREADS) {
-            const int b = e / L, p = e - b * L;
-            float2 v = cscale(buf[b * P::LP + p], a.inv_n3);
-            buf[b * P::LP + p] = modify_f(est_n(v, a.k2, a.n_med), a.k2, a.n_med2);
-        }
-        __syncthreads();
-        P::template run<false>(buf, tw);
+        // IFFT_x ending in registers, the real-space operators on the registers, and
+        // the forward transform in the reversed radix order starting from them
+        float2 v[P::E];
+        P::template seq<true, true, false>(buf, v, tw);
+#pragma unroll
+        for (int i = 0; i < P::E; i++) v[i] = modify_f_scaled(est_n_scaled(v[i], a.s1, a.n_med), a.s2, a.k2);
+        P::template seqr<false, false, true>(buf, v, tw);
         store_rows<L>(a.G, buf, line0, nl);
     }
 }
@@ -227,16 +233,20 @@ template <int L, bool INV>
 __global__ void __launch_bounds__(Plan<L>::THREADS) ypass_kernel(LoopArgs a, const float2 *__restrict__ tw)
 {
     using P = Plan<L>;
+    using En = fftl::Ends<L>;
     extern __shared__ float4 smem4[];
     float2 *buf = reinterpret_cast<float2 *>(smem4);
     const long nl = (long)L * L;
     const long line0 = (long)blockIdx.x * P::B;
     bool ok;
     const long base = col_base<L>(line0, L, (long)L * L, nl, ok);
-    load_cols<L>(buf, a.G, base, ok, L);
-    __syncthreads();
-    P::template run<INV>(buf, tw);
-    store_cols<L>(a.G, buf, base, ok, L);
+    const int t = threadIdx.x / P::B;
+    float2 v[P::E];
+#pragma unroll
+    for (int i = 0; i < P::E; i++) v[i] = __ldcs(&a.G[base + (long)fftl::slot_pos<L, P::T, En::F>(i, t) * L]);
+    P::template seq<INV, false, false>(buf, v, tw);
+#pragma unroll
+    for (int i = 0; i < P::E; i++) __stcs(&a.G[base + (long)fftl::slot_pos<L, P::T, En::Rv>(i, t) * L], v[i]);
 }
 
 // ------------------------------------------------------------ z pass
@@ -246,31 +256,30 @@ template <int L, int MODE>
 __global__ void __launch_bounds__(Plan<L>::THREADS) zpass_kernel(LoopArgs a, const float2 *__restrict__ tw)
 {
     using P = Plan<L>;
+    using En = fftl::Ends<L>;
     extern __shared__ float4 smem4[];
     float2 *buf = reinterpret_cast<float2 *>(smem4);
     const long nl = (long)L * L;
     const long line0 = (long)blockIdx.x * P::B;
     bool ok;
     const long base = col_base<L>(line0, L, L, nl, ok);
-    load_cols<L>(buf, a.G, base, ok, nl);
-    __syncthreads();
-    P::template run<false>(buf, tw);
-    {
-        const int b = threadIdx.x % P::B, t = threadIdx.x / P::B;
-        if (ok) {
-            for (int p = t; p < L; p += P::T) {
-                const long idx = base + p * nl;
-                const float2 f2 = __ldcs(&a.F2[idx]);
-                bool keep;
-                if (MODE == 0) keep = (f2.x != 0.0f && f2.y != 0.0f);
-                else keep = a.mask[idx] != 0;
-                if (keep) buf[b * P::LP + p] = f2;
-            }
-        }
+    const int t = threadIdx.x / P::B;
+    float2 v[P::E];
+#pragma unroll
+    for (int i = 0; i < P::E; i++) v[i] = __ldcs(&a.G[base + (long)fftl::slot_pos<L, P::T, En::F>(i, t) * nl]);
+    P::template seq<false, false, false>(buf, v, tw);
+#pragma unroll
+    for (int i = 0; i < P::E; i++) {
+        const long idx = base + (long)fftl::slot_pos<L, P::T, En::Rv>(i, t) * nl;
+        const float2 f2 = __ldcs(&a.F2[idx]);
+        bool keep;
+        if (MODE == 0) keep = (f2.x != 0.0f && f2.y != 0.0f);
+        else keep = a.mask[idx] != 0;
+        if (keep) v[i] = f2;
     }
-    __syncthreads();
-    P::template run<true>(buf, tw);
-    store_cols<L>(a.G, buf, base, ok, nl);
+    P::template seqr<true, false, false>(buf, v, tw);
+#pragma unroll
+    for (int i = 0; i < P::E; i++) __stcs(&a.G[base + (long)fftl::slot_pos<L, P::T, En::F>(i, t) * nl], v[i]);
 }
 
 template <int L>
@@ -407,11 +416,13 @@ __global__ void __launch_bounds__(Plan<L>::THREADS) ewald_kernel(EwaldArgs a, co
         }
     }
     __syncthreads();
-    P::template run<true>(buf, tw);
     {
+        float2 v[P::E];
+        P::template seq<true, true, false>(buf, v, tw);
         const int b = threadIdx.x % P::B, t = threadIdx.x / P::B;
         const long base = line0 + b;
-        for (int p = t; p < L; p += P::T) a.G[base + (long)p * rr] = buf[b * P::LP + p];
+#pragma unroll
+        for (int i = 0; i < P::E; i++) a.G[base + (long)fftl::slot_pos<L, P::T, fftl::Ends<L>::Rv>(i, t) * rr] = v[i];
     }
 }
 

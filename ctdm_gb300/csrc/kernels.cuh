@@ -44,6 +44,8 @@ struct LoopArgs {
     float2 *out;            // final RI volume (octant shifted), only for the final pass
     int R;
     float inv_n3, k2, n_med, n_med2;
+    float s1;   // -1 / (R^3 k^2)
+    float s2;   // -k^2 / n_med^2
 };
 
 cudaError_t launch_ewald(const EwaldArgs &a, cudaStream_t s);

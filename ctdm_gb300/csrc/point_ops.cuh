@@ -32,6 +32,37 @@ __device__ __forceinline__ float2 est_n(float2 F, float k2, float nm)
     return make_float2(nr, ni);
 }
 
+// The same root for an unscaled inverse-transform value v: c = 1 + v s1 with
+// s1 = -1/(R^3 k^2) folding the 1/R^3 normalisation and the division by -k^2.
+__device__ __forceinline__ float2 est_n_scaled(float2 v, float s1, float nm)
+{
+    const float c = fmaf(v.x, s1, 1.0f), d = v.y * s1;
+    const float mod = sqrtf(fmaf(c, c, d * d));
+    float a, b;
+    if (d == 0.0f) {
+        a = sqrtf(fmaxf(c, 0.0f));
+        b = 0.0f;
+    } else if (c >= 0.0f) {
+        a = sqrtf((mod + c) * 0.5f);
+        b = d * __frcp_rn(2.0f * a);
+    } else {
+        b = sqrtf((mod - c) * 0.5f);
+        a = fabsf(d) * __frcp_rn(2.0f * b);
+        if (d < 0.0f) b = -b;
+    }
+    float nr = a * nm, ni = b * nm;
+    if (nr < nm) nr = nm;
+    if (ni < 0.0f) ni = 0.0f;
+    return make_float2(nr, ni);
+}
+
+// Modify_F3D with the constants folded: f = ((nr^2 - ni^2) s2 + k^2, 2 nr ni s2),
+// s2 = -k^2 / n_med^2.
+__device__ __forceinline__ float2 modify_f_scaled(float2 n, float s2, float k2)
+{
+    return make_float2(fmaf(n.x * n.x - n.y * n.y, s2, k2), 2.0f * n.x * n.y * s2);
+}
+
 // Modify_F3D (cTDM/Recon_kernel.cu:370-383), called with n_med^2.
 __device__ __forceinline__ float2 modify_f(float2 n, float k2, float nm2)
 {

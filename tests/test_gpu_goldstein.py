@@ -125,3 +125,13 @@ def test_pipeline_with_goldstein(ctx, dev, oracle):
         assert np.array_equal(cuts[a], oc)
         oo, ub, st = oracle.goldstein_floodfill(oc, phase[a])
         assert np.sqrt(np.mean((gold[a] - oo) ** 2)) < PHASE_TOL
+
+
+def test_goldstein_deterministic(ctx, dev):
+    """Repeated runs give identical bits (no ordering races in the parallel fill)."""
+    maps = np.stack([noisy_phase(256, s, 1.2) for s in range(4)])
+    first = run_gpu(ctx, dev, maps)
+    for _ in range(3):
+        again = run_gpu(ctx, dev, maps)
+        for x, y in zip(first[:3], again[:3]):
+            assert np.array_equal(x, y)
