@@ -187,7 +187,7 @@ const float *dct_eigen(int M)
 // ---------------------------------------------------------------- context
 enum BufId {
     B_PHASE, B_AMP, B_PHU, B_CHG, B_CUT, B_GOLD, B_U, B_F2, B_COUNTS, B_G, B_T1, B_S, B_BGF, B_DCT, B_MASK, B_GEOM,
-    B_CARRIER, B_KEY, B_SCRATCH, B_HOLO, B_BG, B_RI, B_GSTATE, B_GLIST, B_GSTATUS, B_FASTW, B_FASTIN, B_TMP, NBUF
+    B_CARRIER, B_KEY, B_SCRATCH, B_HOLO, B_BG, B_RI, B_GSTATE, B_GLIST, B_GSTATUS, B_FASTW, B_FASTIN, B_TMP, B_GWORK, NBUF
 };
 
 // Stage boundaries recorded with CUDA events when timing is enabled.
@@ -222,6 +222,10 @@ struct ctdm_ctx {
     size_t used[NBUF] = {};
     int carrier[3] = {-1, -1, -1};
     StageTimer timer;
+    // side stream for work whose result the reconstruction does not consume
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr, g0 = nullptr, g1 = nullptr;
+    bool side_timed = false;
 };
 
 static cudaError_t ensure(ctdm_ctx *c, int id, size_t bytes)
@@ -262,6 +266,15 @@ extern "C" ctdm_status ctdm_ctx_create(int device, ctdm_ctx **out)
     CK(ensure_tables(), "building twiddle tables");
     ctdm_ctx *c = new ctdm_ctx();
     c->device = device;
+    cudaError_t e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->g0);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->g1);
+    if (e != cudaSuccess) {
+        ctdm_ctx_destroy(c);
+        return cuda_fail(e, "creating the side stream");
+    }
     *out = c;
     g_err.clear();
     return CTDM_OK;
@@ -275,6 +288,9 @@ extern "C" void ctdm_ctx_destroy(ctdm_ctx *c)
         if (c->buf[i]) cudaFree(c->buf[i]);
     for (int i = 0; i < StageTimer::kMax; i++)
         if (c->timer.ev[i]) cudaEventDestroy(c->timer.ev[i]);
+    if (c->side) cudaStreamDestroy(c->side);
+    for (cudaEvent_t e : {c->fork, c->join, c->g0, c->g1})
+        if (e) cudaEventDestroy(e);
     delete c;
 }
 
@@ -304,6 +320,13 @@ extern "C" ctdm_status ctdm_ctx_stage_times(ctdm_ctx *c, double *ms, int *counts
             ms[t.tag[i]] += dt;
             if (counts) counts[t.tag[i]]++;
         }
+    }
+    if (c->side_timed && S_GOLD < n) {
+        float dt = 0;
+        CK(cudaEventSynchronize(c->g1), "stage timing");
+        CK(cudaEventElapsedTime(&dt, c->g0, c->g1), "stage timing");
+        ms[S_GOLD] += dt;
+        if (counts) counts[S_GOLD]++;
     }
     return CTDM_OK;
 }
@@ -501,21 +524,42 @@ extern "C" ctdm_status ctdm_reconstruct_device(ctdm_ctx *c, const ctdm_params *p
     tm.mark(S_QPI, s);
 
     const float *unwrapped = B<float>(c, B_PHU);
-    if (p->run_goldstein || p->unwrap_method == CTDM_METHOD_GOLDSTEIN) {
+    // Goldstein: when its phase does not feed the reconstruction it runs on the side
+    // stream (latency-bound, one CTA per map) beside the memory-bound passes, and the
+    // call's stream joins it at the end.
+    const bool run_gold = p->run_goldstein || p->unwrap_method == CTDM_METHOD_GOLDSTEIN;
+    const bool gold_side = run_gold && p->unwrap_method != CTDM_METHOD_GOLDSTEIN;
+    c->side_timed = false;
+    if (run_gold) {
         CK(ensure(c, B_CHG, A * mm), "alloc charges");
         CK(ensure(c, B_CUT, A * mm), "alloc cuts");
         CK(ensure(c, B_GOLD, sizeof(float) * A * mm), "alloc goldstein out");
         CK(ensure(c, B_GSTATE, A * mm), "alloc goldstein state");
         CK(ensure(c, B_GLIST, sizeof(int) * 5 * A * mm), "alloc goldstein lists");
         CK(ensure(c, B_GSTATUS, sizeof(int) * A), "alloc goldstein status");
-        CK(goldstein_residues(B<float>(c, B_PHASE), A, M, M, B<int8_t>(c, B_CHG), s), "goldstein residues");
-        CK(goldstein_cuts(B<int8_t>(c, B_CHG), A, M, M, B<uint8_t>(c, B_CUT), reinterpret_cast<int8_t *>(B<float>(c, B_DCT)),
-                          s),
+        CK(ensure(c, B_GWORK, A * mm), "alloc goldstein work");
+        cudaStream_t gs = s;
+        if (gold_side) {
+            CK(cudaEventRecord(c->fork, s), "fork");
+            CK(cudaStreamWaitEvent(c->side, c->fork, 0), "fork wait");
+            gs = c->side;
+            if (tm.on) {
+                CK(cudaEventRecord(c->g0, gs), "goldstein timing");
+                c->side_timed = true;
+            }
+        }
+        CK(goldstein_residues(B<float>(c, B_PHASE), A, M, M, B<int8_t>(c, B_CHG), gs), "goldstein residues");
+        CK(goldstein_cuts(B<int8_t>(c, B_CHG), A, M, M, B<uint8_t>(c, B_CUT), B<int8_t>(c, B_GWORK), gs),
            "goldstein cuts");
         CK(goldstein_floodfill(B<uint8_t>(c, B_CUT), B<float>(c, B_PHASE), A, M, M, B<float>(c, B_GOLD),
-                               B<uint8_t>(c, B_GSTATE), B<int>(c, B_GLIST), B<int>(c, B_GSTATUS), s),
+                               B<uint8_t>(c, B_GSTATE), B<int>(c, B_GLIST), B<int>(c, B_GSTATUS), gs),
            "goldstein flood fill");
-        tm.mark(S_GOLD, s);
+        if (gold_side) {
+            if (tm.on) CK(cudaEventRecord(c->g1, gs), "goldstein timing");
+            CK(cudaEventRecord(c->join, gs), "join");
+        } else {
+            tm.mark(S_GOLD, s);
+        }
     }
     if (p->unwrap_method == CTDM_METHOD_DCT) {
         CK(dct_unwrap(B<float>(c, B_PHASE), B<float>(c, B_PHU), B<float>(c, B_DCT), A, M, p->unwrap_mode, s),
@@ -560,6 +604,7 @@ extern "C" ctdm_status ctdm_reconstruct_device(ctdm_ctx *c, const ctdm_params *p
                        mask_mode ? B<uint8_t>(c, B_MASK) : nullptr, B<float2>(c, B_G),
                        reinterpret_cast<float2 *>(d_ri), s);
     if (st != CTDM_OK) return st;
+    if (gold_side) CK(cudaStreamWaitEvent(s, c->join, 0), "join wait");
     CK(cudaMemcpyAsync(c->carrier, c->buf[B_CARRIER], sizeof(int) * 3, cudaMemcpyDeviceToHost, s), "carrier readback");
     g_err.clear();
     return CTDM_OK;

@@ -123,6 +123,8 @@ __global__ void __launch_bounds__(Plan<L>::THREADS) cols_kernel(float2 *data, co
     for (int i = 0; i < P::E; i++) __stcs(&data[base + (long)fftl::slot_pos<L, P::T, En::Rv>(i, t) * ld], v[i]);
 }
 
+// Large dynamic shared memory opt-in and the largest shared-memory carveout, so
+// that several line-batch CTAs stay resident per SM.
 template <int L, class K>
 static cudaError_t prep_launch(K kernel, size_t smem)
 {
@@ -130,7 +132,8 @@ static cudaError_t prep_launch(K kernel, size_t smem)
         cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
-    return cudaSuccess;
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                (int)cudaSharedmemCarveoutMaxShared);
 }
 
 template <int L>
@@ -197,7 +200,7 @@ cudaError_t fft3d(float2 *data, int R, bool inverse, cudaStream_t s)
 
 // ------------------------------------------------------------ x pass
 template <int L, bool FINAL>
-__global__ void __launch_bounds__(Plan<L>::THREADS) xpass_kernel(LoopArgs a, const float2 *__restrict__ tw)
+__global__ void __launch_bounds__(Plan<L>::THREADS, 4) xpass_kernel(LoopArgs a, const float2 *__restrict__ tw)
 {
     using P = Plan<L>;
     extern __shared__ float4 smem4[];
@@ -253,7 +256,7 @@ __global__ void __launch_bounds__(Plan<L>::THREADS) ypass_kernel(LoopArgs a, con
 // check_F3D (cTDM/Recon_kernel.cu:396-412): F <- F2 where F2.re != 0 and F2.im != 0
 // (mode 0, the reference predicate) or where the voxel was hit (mode 1).
 template <int L, int MODE>
-__global__ void __launch_bounds__(Plan<L>::THREADS) zpass_kernel(LoopArgs a, const float2 *__restrict__ tw)
+__global__ void __launch_bounds__(Plan<L>::THREADS, 3) zpass_kernel(LoopArgs a, const float2 *__restrict__ tw)
 {
     using P = Plan<L>;
     using En = fftl::Ends<L>;
