@@ -56,6 +56,7 @@ _SIGS = {
     "ctdm_positivity": (c_int, [c_void_p, c_int, c_int, c_int, c_double, c_double, c_void_p, c_void_p, c_void_p,
                                 c_void_p]),
     "ctdm_fft": (c_int, [c_void_p, c_int, P_int, c_int, c_int, c_void_p]),
+    "ctdm_unwrap_dct_noalloc": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p]),
     "ctdm_set_recon_globals": (None, [c_int, c_double, c_double, c_double, c_double, c_int, c_int, ctypes.c_char_p]),
     "DCT_UWLS_Unwrapped": (None, [c_void_p, c_void_p, c_int, c_int]),
     "FastUnwrapping": (None, [c_void_p, c_void_p, c_int, c_int]),

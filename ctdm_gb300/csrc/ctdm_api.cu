@@ -69,6 +69,10 @@ static ctdm_status invalid(const char *fmt, ...)
 
 extern "C" const char *ctdm_last_error(void) { return g_err.c_str(); }
 
+namespace ctdm {
+void set_error_message(const char *msg) { g_err = msg ? msg : ""; }
+}  // namespace ctdm
+
 static std::atomic<unsigned long long> g_launches{0};
 namespace ctdm {
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }

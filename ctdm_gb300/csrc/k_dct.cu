@@ -224,3 +224,38 @@ cudaError_t dct_unwrap(const float *phi, float *out, float *T, int A, int M, int
 }
 
 }  // namespace ctdm
+
+namespace ctdm {
+
+// The same three passes with caller-supplied tables and scratch (no lookups in
+// the per-device table registry).
+template <int L2>
+static cudaError_t dct_launch_explicit(const float *phi, float *out, float *T, int A, int M, int mode,
+                                       const float2 *tw, const float2 *dtw, const float *eig, cudaStream_t s)
+{
+    using P = Plan<L2>;
+    const long nl = (long)A * M;
+    const unsigned grid = (unsigned)((nl + P::B - 1) / P::B);
+    const size_t smem1 = fftl::smem_bytes<L2>();
+    const size_t smem2 = smem1 + sizeof(float) * P::B * M;
+    cudaError_t e = set_smem2<L2>(dct_rows_kernel<L2>, smem1);
+    if (e != cudaSuccess) return e;
+    dct_rows_kernel<L2><<<grid, P::THREADS, smem1, s>>>(phi, T, nl, M, dtw, tw); note_launch();
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    e = set_smem2<L2>(dct_cols_kernel<L2>, smem2);
+    if (e != cudaSuccess) return e;
+    dct_cols_kernel<L2><<<grid, P::THREADS, smem2, s>>>(T, nl, M, mode, dtw, eig, tw); note_launch();
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    e = set_smem2<L2>(dct_rows_inv_kernel<L2>, smem2);
+    if (e != cudaSuccess) return e;
+    dct_rows_inv_kernel<L2><<<grid, P::THREADS, smem2, s>>>(T, out, nl, M, mode, dtw, tw); note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t dct_unwrap_explicit(const float *phi, float *out, float *T, int A, int M, int mode, const float2 *tw,
+                                const float2 *dtw, const float *eig, cudaStream_t s)
+{
+    CTDM_DISPATCH_L(2 * M, dct_launch_explicit, phi, out, T, A, M, mode, tw, dtw, eig, s)
+}
+
+}  // namespace ctdm

@@ -148,6 +148,18 @@ CTDM_API ctdm_status ctdm_map_ewald(ctdm_ctx *ctx, int A, int R, const ctdm_cflo
  * d_counts required for CTDM_CHECK_MASK (else may be NULL). */
 CTDM_API ctdm_status ctdm_positivity(ctdm_ctx *ctx, int R, int iterations, int check_mode, double k2, double n_med,
                             const ctdm_cfloat *d_F2, const uint32_t *d_counts, ctdm_cfloat *d_ri, void *stream);
+/* DCT least-squares unwrap that allocates nothing -- no counterpart in the reference.
+ * For callers that cannot allocate device memory: an acquisition loop that must not
+ * allocate once it runs, or a host that owns all GPU memory through its own pool.
+ * The scratch map and the transform tables are file-scope __device__ arrays of the
+ * library (about 16.1 MiB held on every GPU that loads it, until the process exits).
+ * Limits: M in {16, 32, 64, 128, 256} and A * M * M <= 4194304 points; larger
+ * requests return CTDM_ERR_INVALID with a message in ctdm_last_error().  The first
+ * call on a device resolves the arrays' device addresses and fills the tables with
+ * synchronous copies, so make it before any stream capture on that device.  All
+ * calls share one scratch array, which keeps the last call's contents (nothing in
+ * it needs clearing); calls that overlap on the GPU race on it. */
+CTDM_API ctdm_status ctdm_unwrap_dct_noalloc(int A, int M, int mode, const float *d_phi, float *d_out, void *stream);
 /* Unnormalised batched FFT of the library's line lengths.  rank 1..3, dims
  * fastest-first; inverse = 1 uses exp(+i), no scaling. */
 CTDM_API ctdm_status ctdm_fft(ctdm_cfloat *d_data, int rank, const int *dims, int batch, int inverse, void *stream);
