@@ -188,3 +188,61 @@ def fft(data, dims, batch=1, inverse=False, stream=None):
     """Unnormalised in-place FFT of a device buffer (dims fastest-first)."""
     d = (ctypes.c_int * len(dims))(*dims)
     check(load().ctdm_fft(_ptr(data), len(dims), d, batch, int(inverse), _stream(stream)), "ctdm_fft")
+
+
+class Tape:
+    """Measurement operator A = P F~ of one tomogram (ctdm_tape) with its adjoint,
+    shaped like a torch.autograd.Function: forward(V) -> y, backward(dL/dy) -> dL/dV."""
+
+    def __init__(self, F2, r, k2, counts=None, device=0):
+        self.lib = load()
+        h = ctypes.c_void_p()
+        check(self.lib.ctdm_tape_create(int(device), int(r), _ptr(F2), _ptr(counts), float(k2), ctypes.byref(h)),
+              "ctdm_tape_create")
+        self.handle = h
+        self.r = r
+
+    @property
+    def samples(self):
+        return int(self.lib.ctdm_tape_samples(self.handle))
+
+    def data(self):
+        """(y, indices) on the host."""
+        y = np.empty(self.samples, np.complex64)
+        idx = np.empty(self.samples, np.uint32)
+        check(self.lib.ctdm_tape_data(self.handle, y.ctypes.data, idx.ctypes.data), "ctdm_tape_data")
+        return y, idx
+
+    def forward(self, V, y, stream=None):
+        check(self.lib.ctdm_forward(self.handle, _ptr(V), _ptr(y), _stream(stream)), "ctdm_forward")
+
+    def backward(self, gy, gV, stream=None):
+        check(self.lib.ctdm_backward(self.handle, _ptr(gy), _ptr(gV), _stream(stream)), "ctdm_backward")
+
+    def loss_grad(self, V, grad, lam=0.0, eps=1e-4):
+        loss = ctypes.c_double()
+        check(self.lib.ctdm_loss_grad(self.handle, _ptr(V), float(lam), float(eps), _ptr(grad), ctypes.byref(loss)),
+              "ctdm_loss_grad")
+        return loss.value
+
+    def reconstruct(self, V, iterations, lam=1e-3, eps=1e-4, step=0.0, record_loss=False, stream=None):
+        hist = np.zeros(max(iterations, 1), np.float64) if record_loss else None
+        check(self.lib.ctdm_reconstruct_gradient(self.handle, int(iterations), float(lam), float(eps), float(step),
+                                                 _ptr(V), _ptr(hist), _stream(stream)), "ctdm_reconstruct_gradient")
+        return hist
+
+    def close(self):
+        if self.handle:
+            self.lib.ctdm_tape_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def contrast_to_ri(V, r, n_med, out, clamp=False, stream=None):
+    check(load().ctdm_contrast_to_ri(int(r), _ptr(V), float(n_med), int(clamp), _ptr(out), _stream(stream)),
+          "ctdm_contrast_to_ri")

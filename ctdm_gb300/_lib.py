@@ -57,6 +57,16 @@ _SIGS = {
                                 c_void_p]),
     "ctdm_fft": (c_int, [c_void_p, c_int, P_int, c_int, c_int, c_void_p]),
     "ctdm_unwrap_dct_noalloc": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p]),
+    "ctdm_tape_create": (c_int, [c_int, c_int, c_void_p, c_void_p, c_double, ctypes.POINTER(c_void_p)]),
+    "ctdm_tape_destroy": (None, [c_void_p]),
+    "ctdm_tape_samples": (ctypes.c_long, [c_void_p]),
+    "ctdm_tape_data": (c_int, [c_void_p, c_void_p, c_void_p]),
+    "ctdm_forward": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    "ctdm_backward": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    "ctdm_loss_grad": (c_int, [c_void_p, c_void_p, c_double, c_double, c_void_p, ctypes.POINTER(c_double)]),
+    "ctdm_reconstruct_gradient": (c_int, [c_void_p, c_int, c_double, c_double, c_double, c_void_p, c_void_p,
+                                          c_void_p]),
+    "ctdm_contrast_to_ri": (c_int, [c_int, c_void_p, c_double, c_int, c_void_p, c_void_p]),
     "ctdm_set_recon_globals": (None, [c_int, c_double, c_double, c_double, c_double, c_int, c_int, ctypes.c_char_p]),
     "DCT_UWLS_Unwrapped": (None, [c_void_p, c_void_p, c_int, c_int]),
     "FastUnwrapping": (None, [c_void_p, c_void_p, c_int, c_int]),

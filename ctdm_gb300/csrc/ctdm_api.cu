@@ -165,6 +165,8 @@ static DevTables *tables_here()
 }
 
 namespace ctdm {
+cudaError_t device_tables() { return ensure_tables(); }
+
 const float2 *twiddles(int L)
 {
     DevTables *t = tables_here();

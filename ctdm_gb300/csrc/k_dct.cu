@@ -204,6 +204,7 @@ static cudaError_t dct_launch(const float *phi, float *out, float *T, int A, int
     const size_t smem2 = smem1 + sizeof(float) * P::B * M;
     const float2 *dtw = dct_twiddles(M);
     const float2 *tw = twiddles(L2);
+    if (!dtw || !tw || !dct_eigen(M)) return cudaErrorInitializationError;   // device tables not built
     cudaError_t e = set_smem2<L2>(dct_rows_kernel<L2>, smem1);
     if (e != cudaSuccess) return e;
     dct_rows_kernel<L2><<<grid, P::THREADS, smem1, s>>>(phi, T, nl, M, dtw, tw); note_launch();

@@ -23,6 +23,7 @@ using fftl::Plan;
 template <int L, class K>
 static cudaError_t set_smem(K kernel, size_t smem)
 {
+    if (!twiddles(L)) return cudaErrorInitializationError;   // device tables not built on this device
     if (smem > 48 * 1024)
         return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     return cudaSuccess;

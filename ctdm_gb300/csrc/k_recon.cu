@@ -128,6 +128,7 @@ __global__ void __launch_bounds__(Plan<L>::THREADS) cols_kernel(float2 *data, co
 template <int L, class K>
 static cudaError_t prep_launch(K kernel, size_t smem)
 {
+    if (!twiddles(L)) return cudaErrorInitializationError;   // device tables not built on this device
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;

@@ -10,7 +10,10 @@ namespace ctdm {
 // Counts kernel launches issued by the library (process-wide, for instrumentation).
 void note_launch();
 
-// Twiddle table for an FFT length (exp(-2 pi i e / L), e < L), device resident.
+// Builds the current device's tables once (contexts and tapes call it at creation).
+cudaError_t device_tables();
+// Twiddle table for an FFT length (exp(-2 pi i e / L), e < L), device resident;
+// NULL until device_tables() has run on the current device.
 const float2 *twiddles(int L);
 // DCT helper tables for crop side M: dct_tw[k] = (cos(k pi/2M), sin(k pi/2M)),
 // k = 0..2M; eig[k] = 4 sin^2(2 pi k/(4M-1)).

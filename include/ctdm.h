@@ -148,6 +148,36 @@ CTDM_API ctdm_status ctdm_map_ewald(ctdm_ctx *ctx, int A, int R, const ctdm_cflo
  * d_counts required for CTDM_CHECK_MASK (else may be NULL). */
 CTDM_API ctdm_status ctdm_positivity(ctdm_ctx *ctx, int R, int iterations, int check_mode, double k2, double n_med,
                             const ctdm_cfloat *d_F2, const uint32_t *d_counts, ctdm_cfloat *d_ri, void *stream);
+/* --- differentiable form (no reference counterpart) ---------------------------------
+ * Measurement operator A = P F~: unitary 3-D FFT (F / R^{3/2}) then sampling at the
+ * measured voxels of the Ewald caps.  V is the contrast f / (-k^2) of the reference's
+ * scattering potential (n = n_med sqrt(1 + V)).  The tape keeps the sorted measured
+ * voxel indices and the data y = F2 / (-k^2 R^{3/2}); forward/backward are shaped like
+ * a torch.autograd.Function (backward = A^H, recomputing the transform).  Gradients
+ * use the conjugate-Wirtinger convention dL/dRe V + i dL/dIm V. */
+typedef struct ctdm_tape ctdm_tape;
+/* Measured voxels: d_counts > 0 when given, else the reference predicate on F2. */
+CTDM_API ctdm_status ctdm_tape_create(int device, int R, const ctdm_cfloat *d_F2, const uint32_t *d_counts, double k2,
+                                      ctdm_tape **out);
+CTDM_API void ctdm_tape_destroy(ctdm_tape *tape);
+CTDM_API long ctdm_tape_samples(const ctdm_tape *tape);
+CTDM_API ctdm_status ctdm_tape_data(const ctdm_tape *tape, ctdm_cfloat *h_y, uint32_t *h_idx);
+/* y (S complex) = A V */
+CTDM_API ctdm_status ctdm_forward(ctdm_tape *tape, const ctdm_cfloat *d_V, ctdm_cfloat *d_y, void *stream);
+/* dL/dV (R^3 complex) = A^H dL/dy */
+CTDM_API ctdm_status ctdm_backward(ctdm_tape *tape, const ctdm_cfloat *d_gy, ctdm_cfloat *d_gV, void *stream);
+/* L = 1/2 ||A V - y||^2 + lambda TV_eps(V) and its gradient (synchronous). */
+CTDM_API ctdm_status ctdm_loss_grad(ctdm_tape *tape, const ctdm_cfloat *d_V, double lambda, double eps,
+                                    ctdm_cfloat *d_grad, double *loss);
+/* Accelerated gradient descent (FISTA) on L from d_V (updated in place).  step <= 0
+ * picks 1 / (1 + 12 lambda / eps).  h_loss (iterations doubles, may be NULL) receives
+ * the objective per iteration (synchronises each iteration when given). */
+CTDM_API ctdm_status ctdm_reconstruct_gradient(ctdm_tape *tape, int iterations, double lambda, double eps, double step,
+                                               ctdm_cfloat *d_V, double *h_loss, void *stream);
+/* n = n_med sqrt(1 + V), optional positivity clamp, octant-shifted like the reference output. */
+CTDM_API ctdm_status ctdm_contrast_to_ri(int R, const ctdm_cfloat *d_V, double n_med, int clamp, ctdm_cfloat *d_ri,
+                                         void *stream);
+
 /* DCT least-squares unwrap that allocates nothing -- no counterpart in the reference.
  * For callers that cannot allocate device memory: an acquisition loop that must not
  * allocate once it runs, or a host that owns all GPU memory through its own pool.

@@ -1,0 +1,219 @@
+"""GPU checks of the differentiable form (ctdm_tape, ctdm_forward/ctdm_backward,
+ctdm_loss_grad, ctdm_reconstruct_gradient, ctdm_contrast_to_ri) through the C ABI
+against the FP64 oracle (oracle/adjoint.py), finite differences and the
+positivity path.
+
+Tolerances (float32 transforms vs FP64): forward / backward / gradient relative
+L2 error <= 1e-5; loss relative error <= 1e-5; central differences of the GPU loss
+(h = 1e-3, 64 voxels, real and imaginary perturbations) within 5e-3 of the
+largest gradient component; RI RMSE <= 1e-5."""
+import numpy as np
+import pytest
+
+import adjoint as AD
+
+pytestmark = pytest.mark.gpu
+
+REL = 1e-5
+
+
+def T(a, dev):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+
+def rel(a, b):
+    a = np.asarray(a, np.complex128).ravel()
+    b = np.asarray(b, np.complex128).ravel()
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def _random_tape(ctx, dev, r, frac=0.3, seed=0, with_counts=True, k2=4.0, scale=1.0):
+    import ctdm_gb300 as C
+    rng = np.random.default_rng(seed)
+    F2 = (rng.standard_normal((r, r, r)) + 1j * rng.standard_normal((r, r, r))).astype(np.complex64)
+    hit = rng.random((r, r, r)) < frac
+    F2[~hit] = 0
+    counts = (hit * rng.integers(1, 4, (r, r, r))).astype(np.int32)
+    F2 *= np.float32(-k2 * r ** 1.5 * scale)   # data y of the given scale
+    tape = C.Tape(T(F2, dev), r, k2, T(counts, dev) if with_counts else None)
+    return tape, F2, counts, rng
+
+
+@pytest.mark.parametrize("with_counts", [True, False])
+def test_tape_indices_and_data(ctx, dev, with_counts):
+    r, k2 = 32, 4.0
+    tape, F2, counts, _ = _random_tape(ctx, dev, r, with_counts=with_counts, k2=k2)
+    y, idx = tape.data()
+    ref_idx = AD.measured_indices(F2, counts if with_counts else None)
+    assert np.array_equal(idx, ref_idx)
+    np.testing.assert_allclose(y, AD.tape_data(F2, ref_idx, r, k2), rtol=1e-6)
+    tape.close()
+
+
+@pytest.mark.parametrize("r", [32, 64, 128])
+def test_forward_backward_match_fp64(ctx, dev, r):
+    import torch
+    tape, _, _, rng = _random_tape(ctx, dev, r, seed=r)
+    _, idx = tape.data()
+    V = (rng.standard_normal((r, r, r)) + 1j * rng.standard_normal((r, r, r))).astype(np.complex64)
+    g = (rng.standard_normal(idx.size) + 1j * rng.standard_normal(idx.size)).astype(np.complex64)
+    y = torch.zeros(idx.size, dtype=torch.complex64, device=dev)
+    gV = torch.zeros((r, r, r), dtype=torch.complex64, device=dev)
+    tape.forward(T(V, dev), y)
+    tape.backward(T(g, dev), gV)
+    torch.cuda.synchronize()
+    yh, gVh = y.cpu().numpy(), gV.cpu().numpy()
+    assert rel(yh, AD.forward(V, idx)) < REL
+    assert rel(gVh, AD.adjoint(g, idx, r)) < REL
+    # adjoint identity <A V, g> = <V, A^H g> on the GPU results themselves
+    lhs = np.vdot(g.astype(np.complex128), yh.astype(np.complex128))
+    rhs = np.vdot(gVh.astype(np.complex128), V.astype(np.complex128))
+    assert abs(lhs - rhs) <= 1e-5 * np.linalg.norm(g) * np.linalg.norm(V)
+    tape.close()
+
+
+def test_adjoint_identity_512(ctx, dev):
+    """Size-independent property at the full 512^3 volume (transform recomputed in
+    the backward): <A V, g> = <V, A^H g> and A A^H = I on the samples."""
+    import torch
+    r = 512
+    gen = torch.Generator(device=dev).manual_seed(3)
+    F2 = torch.zeros((r, r, r), dtype=torch.complex64, device=dev)
+    hit = torch.rand((r, r, r), generator=gen, device=dev) < 0.02
+    F2[hit] = torch.complex(torch.ones((), device=dev), torch.ones((), device=dev))
+    import ctdm_gb300 as C
+    tape = C.Tape(F2, r, 1.0)
+    S = tape.samples
+    assert S == int(hit.sum().item())
+    del F2, hit
+    V = torch.randn((r, r, r), dtype=torch.complex64, device=dev, generator=gen)
+    g = torch.randn(S, dtype=torch.complex64, device=dev, generator=gen)
+    y = torch.empty(S, dtype=torch.complex64, device=dev)
+    gV = torch.empty((r, r, r), dtype=torch.complex64, device=dev)
+    tape.forward(V, y)
+    tape.backward(g, gV)
+    y2 = torch.empty(S, dtype=torch.complex64, device=dev)
+    tape.forward(gV, y2)
+    torch.cuda.synchronize()
+    lhs = torch.vdot(g.to(torch.complex128), y.to(torch.complex128)).item()
+    rhs = torch.vdot(gV.to(torch.complex128).ravel(), V.to(torch.complex128).ravel()).item()
+    scale = (torch.linalg.vector_norm(g) * torch.linalg.vector_norm(V)).item()
+    assert abs(lhs - rhs) <= 1e-5 * scale
+    assert (torch.linalg.vector_norm(y2 - g) / torch.linalg.vector_norm(g)).item() < 1e-5
+    tape.close()
+
+
+@pytest.mark.parametrize("lam", [0.0, 0.05])
+def test_loss_grad_matches_fp64(ctx, dev, lam):
+    import torch
+    r, eps = 32, 1e-2
+    tape, _, _, rng = _random_tape(ctx, dev, r, seed=7)
+    y, idx = tape.data()
+    V = (0.1 * (rng.standard_normal((r, r, r)) + 1j * rng.standard_normal((r, r, r)))).astype(np.complex64)
+    grad = torch.zeros((r, r, r), dtype=torch.complex64, device=dev)
+    L = tape.loss_grad(T(V, dev), grad, lam, eps)
+    Lr, gr = AD.loss_grad(V, idx, y.astype(np.complex128), lam, eps)
+    assert abs(L - Lr) <= REL * Lr
+    assert rel(grad.cpu().numpy(), gr) < REL
+    tape.close()
+
+
+@pytest.mark.parametrize("lam", [0.0, 0.05])
+def test_gradient_finite_differences(ctx, dev, lam):
+    """Central differences of the GPU loss itself, h = 1e-3, on 64 voxels, against
+    the GPU gradient (real part <- Re perturbation, imaginary <- Im perturbation).
+    Contrast and data of physical scale (~0.02) keep the float32 loss noise / 2h
+    small against the gradient."""
+    import torch
+    r, eps, h = 32, 1e-2, 1e-3
+    tape, F2, _, rng = _random_tape(ctx, dev, r, seed=11, scale=0.02)
+    V = (0.02 * (rng.standard_normal((r, r, r)) + 1j * rng.standard_normal((r, r, r)))).astype(np.complex64)
+    grad = torch.zeros((r, r, r), dtype=torch.complex64, device=dev)
+    Vd = T(V, dev)
+    tape.loss_grad(Vd, grad, lam, eps)
+    g = grad.cpu().numpy().ravel()
+    picks = rng.choice(r ** 3, 64, replace=False)
+    err = []
+    for p in picks:
+        z, yy, x = np.unravel_index(p, (r, r, r))
+        for unit, comp in ((1.0, g[p].real), (1j, g[p].imag)):
+            base = Vd[z, yy, x].item()
+            Vd[z, yy, x] = base + h * unit
+            Lp = tape.loss_grad(Vd, grad, lam, eps)
+            Vd[z, yy, x] = base - h * unit
+            Lm = tape.loss_grad(Vd, grad, lam, eps)
+            Vd[z, yy, x] = base
+            err.append((Lp - Lm) / (2 * h) - comp)
+    err = np.abs(np.array(err))
+    assert err.max() <= 5e-3 * np.abs(g).max()
+    tape.close()
+
+
+def test_fista_matches_fp64(ctx, dev):
+    import torch
+    r, lam, eps, iters = 32, 1e-3, 1e-2, 10
+    tape, _, _, rng = _random_tape(ctx, dev, r, seed=5)
+    y, idx = tape.data()
+    V0 = np.zeros((r, r, r), np.complex64)
+    V = T(V0, dev)
+    hist = tape.reconstruct(V, iters, lam, eps, record_loss=True)
+    torch.cuda.synchronize()
+    Vr, hr = AD.fista(V0, idx, y.astype(np.complex128), iters, lam, eps)
+    assert rel(V.cpu().numpy(), Vr) < 1e-4
+    np.testing.assert_allclose(hist, hr, rtol=1e-4)
+    assert hist[-1] < 0.2 * hist[0]
+    tape.close()
+
+
+def test_contrast_to_ri(ctx, dev):
+    import torch
+    import ctdm_gb300 as C
+    r, nm = 32, 1.337
+    rng = np.random.default_rng(9)
+    V = (0.05 * rng.standard_normal((r, r, r)) + 0.01j * rng.standard_normal((r, r, r))).astype(np.complex64)
+    V[0, 0, :4] = [-2.0, -2.0 - 0.0j, 0.0, -1.0]
+    for clamp in (False, True):
+        out = torch.zeros((r, r, r), dtype=torch.complex64, device=dev)
+        C.contrast_to_ri(T(V, dev), r, nm, out, clamp=clamp)
+        torch.cuda.synchronize()
+        ref = AD.contrast_to_ri(V, nm, clamp)
+        assert np.sqrt(np.mean(np.abs(out.cpu().numpy() - ref) ** 2)) < 1e-6
+
+
+def test_gradient_recon_ties_to_positivity_path(ctx, dev, oracle):
+    """One plain gradient step from V = 0 (lambda 0, step 1) is A^H y, the
+    zero-filled inverse -- the RI the positivity path returns with no loop bodies.
+    Then TV-regularised FISTA on the same phantom data lowers the objective."""
+    import torch
+    import ctdm_gb300 as C
+    from ctdm_gb300 import phantom
+    acq = phantom.small_case(seed=5, n=64, r=64, angles=8)
+    r = acq.r_vol
+    ph, am, _ = oracle.front_end(oracle.make_params(acq.n_holo, acq.m_crop, r, 0, acq.fm0, acq.df, acq.dx, acq.k2,
+                                                    acq.n_med), acq.holograms, acq.background)
+    U = np.stack([oracle.rytov_spectrum(ph[a], am[a]) for a in range(len(ph))])
+    oF2, oC = oracle.ewald_map(U, acq.ang_x, acq.ang_y, acq.fm0, acq.df, acq.dx)
+    ref = oracle.positivity(oF2, oC, 0, acq.k2, acq.n_med, 0)
+    F2 = T(oF2.astype(np.complex64), dev)
+    tape = C.Tape(F2, r, acq.k2, T(oC.astype(np.int32), dev))
+    V = torch.zeros((r, r, r), dtype=torch.complex64, device=dev)
+    tape.reconstruct(V, 1, 0.0, 1.0, step=1.0)
+    n = torch.zeros_like(V)
+    C.contrast_to_ri(V, r, acq.n_med, n, clamp=True)   # est_n clamps (cTDM/Recon_kernel.cu:est_n_3D)
+    torch.cuda.synchronize()
+    assert np.sqrt(np.mean(np.abs(n.cpu().numpy() - ref) ** 2)) < 1e-5
+    V.zero_()
+    hist = tape.reconstruct(V, 30, 1e-4, 1e-3, record_loss=True)
+    assert np.all(np.isfinite(hist)) and hist[-1] < hist[0]
+    tape.close()
+
+
+def test_tape_rejects_bad_arguments(ctx, dev):
+    import torch
+    import ctdm_gb300 as C
+    F2 = torch.zeros((32, 32, 32), dtype=torch.complex64, device=dev)
+    with pytest.raises(RuntimeError, match="no measured voxels"):
+        C.Tape(F2, 32, 1.0)
+    with pytest.raises(RuntimeError, match="unsupported"):
+        C.Tape(F2, 48, 1.0)
