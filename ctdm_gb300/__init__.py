@@ -107,7 +107,7 @@ class Context:
         check(self.lib.ctdm_ctx_set_timing(self.handle, int(on)), "ctdm_ctx_set_timing")
 
     def stage_times(self):
-        """{stage: (ms, launches)} of the last timed pipeline call."""
+        """{stage: (ms, launches)} summed over the pipeline calls made since set_timing(True)."""
         n = len(self.STAGES)
         ms = (ctypes.c_double * n)()
         cnt = (ctypes.c_int * n)()

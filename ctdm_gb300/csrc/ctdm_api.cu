@@ -199,18 +199,24 @@ enum BufId {
 // Stage boundaries recorded with CUDA events when timing is enabled.
 enum StageTag { S_QPI, S_UNWRAP, S_GOLD, S_SPECTRA, S_EWALD, S_YINV, S_XPASS, S_YFWD, S_ZPASS, S_XFINAL, S_COUNT };
 
+// Stage timing accumulates over every reconstruction between ctdm_ctx_set_timing(on)
+// and the read, so a caller can time the stages of a whole timed loop.  Marks on the
+// call's stream attribute the interval since the previous mark to a stage; work on
+// the side stream is bracketed by its own event pairs.
 struct StageTimer {
-    static const int kMax = 1024;
+    static const int kMax = 16384, kSide = 1024;
     cudaEvent_t ev[kMax] = {};
     int tag[kMax] = {};
     int n = 0;
+    cudaEvent_t side[2 * kSide] = {};
+    int ns = 0;   // side events recorded (pairs: begin, end)
     bool on = false;
-    void start(cudaStream_t s)
+    void reset()
     {
-        if (!on) return;
         n = 0;
-        mark(-1, s);
+        ns = 0;
     }
+    void start(cudaStream_t s) { mark(-1, s); }
     void mark(int t, cudaStream_t s)
     {
         if (!on || n >= kMax) return;
@@ -218,6 +224,14 @@ struct StageTimer {
         tag[n] = t;
         cudaEventRecord(ev[n], s);
         n++;
+    }
+    // begin (even ns) or end (odd ns) of a side-stream interval
+    void side_mark(cudaStream_t s)
+    {
+        if (!on || ns >= 2 * kSide) return;
+        if (!side[ns]) cudaEventCreate(&side[ns]);
+        cudaEventRecord(side[ns], s);
+        ns++;
     }
 };
 
@@ -230,8 +244,7 @@ struct ctdm_ctx {
     StageTimer timer;
     // side stream for work whose result the reconstruction does not consume
     cudaStream_t side = nullptr;
-    cudaEvent_t fork = nullptr, join = nullptr, g0 = nullptr, g1 = nullptr;
-    bool side_timed = false;
+    cudaEvent_t fork = nullptr, join = nullptr;
 };
 
 static cudaError_t ensure(ctdm_ctx *c, int id, size_t bytes)
@@ -275,8 +288,6 @@ extern "C" ctdm_status ctdm_ctx_create(int device, ctdm_ctx **out)
     cudaError_t e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreate(&c->g0);
-    if (e == cudaSuccess) e = cudaEventCreate(&c->g1);
     if (e != cudaSuccess) {
         ctdm_ctx_destroy(c);
         return cuda_fail(e, "creating the side stream");
@@ -294,8 +305,10 @@ extern "C" void ctdm_ctx_destroy(ctdm_ctx *c)
         if (c->buf[i]) cudaFree(c->buf[i]);
     for (int i = 0; i < StageTimer::kMax; i++)
         if (c->timer.ev[i]) cudaEventDestroy(c->timer.ev[i]);
+    for (int i = 0; i < 2 * StageTimer::kSide; i++)
+        if (c->timer.side[i]) cudaEventDestroy(c->timer.side[i]);
     if (c->side) cudaStreamDestroy(c->side);
-    for (cudaEvent_t e : {c->fork, c->join, c->g0, c->g1})
+    for (cudaEvent_t e : {c->fork, c->join})
         if (e) cudaEventDestroy(e);
     delete c;
 }
@@ -304,11 +317,12 @@ extern "C" ctdm_status ctdm_ctx_set_timing(ctdm_ctx *c, int on)
 {
     if (!c) return invalid("ctdm_ctx_set_timing: NULL context");
     c->timer.on = on != 0;
-    c->timer.n = 0;
+    c->timer.reset();
     return CTDM_OK;
 }
 
-// Per-stage device time (ms) and launch-group count of the last timed pipeline call.
+// Per-stage device time (ms) and launch-group count summed over the pipeline calls
+// made since timing was switched on.
 extern "C" ctdm_status ctdm_ctx_stage_times(ctdm_ctx *c, double *ms, int *counts, int n)
 {
     if (!c || !ms || n < 1) return invalid("ctdm_ctx_stage_times: bad argument");
@@ -317,8 +331,7 @@ extern "C" ctdm_status ctdm_ctx_stage_times(ctdm_ctx *c, double *ms, int *counts
         if (counts) counts[i] = 0;
     }
     StageTimer &t = c->timer;
-    if (t.n < 2) return CTDM_OK;
-    CK(cudaEventSynchronize(t.ev[t.n - 1]), "stage timing");
+    if (t.n >= 2) CK(cudaEventSynchronize(t.ev[t.n - 1]), "stage timing");
     for (int i = 1; i < t.n; i++) {
         float dt = 0;
         CK(cudaEventElapsedTime(&dt, t.ev[i - 1], t.ev[i]), "stage timing");
@@ -327,10 +340,10 @@ extern "C" ctdm_status ctdm_ctx_stage_times(ctdm_ctx *c, double *ms, int *counts
             if (counts) counts[t.tag[i]]++;
         }
     }
-    if (c->side_timed && S_GOLD < n) {
+    for (int i = 0; i + 1 < t.ns && S_GOLD < n; i += 2) {
         float dt = 0;
-        CK(cudaEventSynchronize(c->g1), "stage timing");
-        CK(cudaEventElapsedTime(&dt, c->g0, c->g1), "stage timing");
+        CK(cudaEventSynchronize(t.side[i + 1]), "stage timing");
+        CK(cudaEventElapsedTime(&dt, t.side[i], t.side[i + 1]), "stage timing");
         ms[S_GOLD] += dt;
         if (counts) counts[S_GOLD]++;
     }
@@ -535,7 +548,6 @@ extern "C" ctdm_status ctdm_reconstruct_device(ctdm_ctx *c, const ctdm_params *p
     // call's stream joins it at the end.
     const bool run_gold = p->run_goldstein || p->unwrap_method == CTDM_METHOD_GOLDSTEIN;
     const bool gold_side = run_gold && p->unwrap_method != CTDM_METHOD_GOLDSTEIN;
-    c->side_timed = false;
     if (run_gold) {
         CK(ensure(c, B_CHG, A * mm), "alloc charges");
         CK(ensure(c, B_CUT, A * mm), "alloc cuts");
@@ -549,10 +561,7 @@ extern "C" ctdm_status ctdm_reconstruct_device(ctdm_ctx *c, const ctdm_params *p
             CK(cudaEventRecord(c->fork, s), "fork");
             CK(cudaStreamWaitEvent(c->side, c->fork, 0), "fork wait");
             gs = c->side;
-            if (tm.on) {
-                CK(cudaEventRecord(c->g0, gs), "goldstein timing");
-                c->side_timed = true;
-            }
+            tm.side_mark(gs);
         }
         CK(goldstein_residues(B<float>(c, B_PHASE), A, M, M, B<int8_t>(c, B_CHG), gs), "goldstein residues");
         CK(goldstein_cuts(B<int8_t>(c, B_CHG), A, M, M, B<uint8_t>(c, B_CUT), B<int8_t>(c, B_GWORK), gs),
@@ -561,7 +570,7 @@ extern "C" ctdm_status ctdm_reconstruct_device(ctdm_ctx *c, const ctdm_params *p
                                B<uint8_t>(c, B_GSTATE), B<int>(c, B_GLIST), B<int>(c, B_GSTATUS), gs),
            "goldstein flood fill");
         if (gold_side) {
-            if (tm.on) CK(cudaEventRecord(c->g1, gs), "goldstein timing");
+            tm.side_mark(gs);
             CK(cudaEventRecord(c->join, gs), "join");
         } else {
             tm.mark(S_GOLD, s);

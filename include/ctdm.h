@@ -97,8 +97,10 @@ CTDM_API ctdm_status ctdm_ctx_read_buffer(ctdm_ctx *ctx, int which, void *host, 
 /* Stage timing with CUDA events on the call's stream (off by default).  Stages:
  * 0 QPI, 1 unwrap, 2 Goldstein, 3 spectra (prep + FFT2), 4 Ewald mapping,
  * 5 y inverse pass, 6 x pass (loop), 7 y forward pass, 8 z pass, 9 final x pass.
- * ms[i]: summed device time of stage i in the last pipeline call; counts[i]: number
- * of launches of that stage (may be NULL). */
+ * ms[i]: device time of stage i summed over the pipeline calls made since timing was
+ * switched on (set_timing(1) restarts the sums); counts[i]: number of launches of
+ * that stage (may be NULL).  Up to 16383 stage marks and 1024 side-stream intervals
+ * are kept; later ones are not recorded. */
 CTDM_API ctdm_status ctdm_ctx_set_timing(ctdm_ctx *ctx, int on);
 CTDM_API ctdm_status ctdm_ctx_stage_times(ctdm_ctx *ctx, double *ms, int *counts, int n);
 /* Number of kernels this library has launched in the process so far. */
