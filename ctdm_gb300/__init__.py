@@ -114,6 +114,12 @@ class Context:
         check(self.lib.ctdm_ctx_stage_times(self.handle, ms, cnt, n), "ctdm_ctx_stage_times")
         return {name: (ms[i], cnt[i]) for i, name in enumerate(self.STAGES)}
 
+    def device_status(self):
+        """Status word of the bounded device-side waits (0 = none ran out); clears it."""
+        st = ctypes.c_int()
+        check(self.lib.ctdm_ctx_device_status(self.handle, ctypes.byref(st)), "ctdm_ctx_device_status")
+        return st.value
+
     def buffer(self, which):
         p, n = ctypes.c_void_p(), ctypes.c_size_t()
         check(self.lib.ctdm_ctx_buffer(self.handle, int(which), ctypes.byref(p), ctypes.byref(n)), "ctdm_ctx_buffer")

@@ -36,6 +36,7 @@ _SIGS = {
     "ctdm_goldstein_fill": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, P_int, c_void_p]),
     "ctdm_ctx_set_timing": (c_int, [c_void_p, c_int]),
     "ctdm_ctx_stage_times": (c_int, [c_void_p, ctypes.POINTER(c_double), P_int, c_int]),
+    "ctdm_ctx_device_status": (c_int, [c_void_p, P_int]),
     "ctdm_launch_count": (ctypes.c_ulonglong, []),
     "ctdm_reconstruct_device": (c_int, [c_void_p, ctypes.POINTER(Params), c_int, c_void_p, c_void_p, c_void_p,
                                         c_void_p, c_void_p, c_void_p]),

@@ -245,6 +245,8 @@ struct ctdm_ctx {
     // side stream for work whose result the reconstruction does not consume
     cudaStream_t side = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr;
+    // device status word (bounded device-side waits record a code here)
+    int *d_err = nullptr;
 };
 
 static cudaError_t ensure(ctdm_ctx *c, int id, size_t bytes)
@@ -288,6 +290,8 @@ extern "C" ctdm_status ctdm_ctx_create(int device, ctdm_ctx **out)
     cudaError_t e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_err, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(c->d_err, 0, sizeof(int));
     if (e != cudaSuccess) {
         ctdm_ctx_destroy(c);
         return cuda_fail(e, "creating the side stream");
@@ -308,6 +312,7 @@ extern "C" void ctdm_ctx_destroy(ctdm_ctx *c)
     for (int i = 0; i < 2 * StageTimer::kSide; i++)
         if (c->timer.side[i]) cudaEventDestroy(c->timer.side[i]);
     if (c->side) cudaStreamDestroy(c->side);
+    if (c->d_err) cudaFree(c->d_err);
     for (cudaEvent_t e : {c->fork, c->join})
         if (e) cudaEventDestroy(e);
     delete c;
@@ -347,6 +352,20 @@ extern "C" ctdm_status ctdm_ctx_stage_times(ctdm_ctx *c, double *ms, int *counts
         ms[S_GOLD] += dt;
         if (counts) counts[S_GOLD]++;
     }
+    return CTDM_OK;
+}
+
+// Status word of the context's bounded device-side waits: 0, or the code of the
+// first wait that ran out since the last read (1: a TMA tile of the z pass).
+// Synchronises the device; reading clears it.
+extern "C" ctdm_status ctdm_ctx_device_status(ctdm_ctx *c, int *status)
+{
+    if (!c || !status) return invalid("ctdm_ctx_device_status: NULL argument");
+    CK(cudaSetDevice(c->device), "cudaSetDevice");
+    CK(cudaDeviceSynchronize(), "device status");
+    CK(cudaMemcpy(status, c->d_err, sizeof(int), cudaMemcpyDeviceToHost), "device status");
+    CK(cudaMemset(c->d_err, 0, sizeof(int)), "device status");
+    g_err.clear();
     return CTDM_OK;
 }
 
@@ -478,6 +497,7 @@ static ctdm_status do_positivity(ctdm_ctx *c, int R, int iters, int check_mode, 
     la.n_med2 = (float)(n_med * n_med);
     la.s1 = (float)(-1.0 / ((double)R * R * R * k2));
     la.s2 = (float)(-k2 / (n_med * n_med));
+    la.err = c->d_err;
     StageTimer &tm = c->timer;
     CK(launch_ypass(la, true, s), "y inverse pass");
     tm.mark(S_YINV, s);
@@ -646,7 +666,14 @@ extern "C" ctdm_status ctdm_reconstruct(ctdm_ctx *c, const ctdm_params *p, int A
                                  B<ctdm_cfloat>(c, B_RI), s);
     if (st != CTDM_OK) return st;
     CK(cudaMemcpyAsync(h_ri, c->buf[B_RI], sizeof(float2) * r3, cudaMemcpyDeviceToHost, s), "download volume");
+    int derr = 0;
+    CK(cudaMemcpyAsync(&derr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, s), "device status");
     CK(cudaStreamSynchronize(s), "synchronise");
+    if (derr != 0) {
+        cudaMemset(c->d_err, 0, sizeof(int));
+        g_err = "a bounded device-side wait ran out (code " + std::to_string(derr) + ")";
+        return CTDM_ERR_TIMEOUT;
+    }
     return CTDM_OK;
 }
 
@@ -825,6 +852,7 @@ extern "C" ctdm_status ctdm_positivity(ctdm_ctx *c, int R, int iterations, int c
         CK(counts_to_mask(d_counts, B<uint8_t>(c, B_MASK), r3, s), "mask");
         mask = B<uint8_t>(c, B_MASK);
     }
+    c->timer.start(s);
     return do_positivity(c, R, iterations, check_mode, k2, n_med, reinterpret_cast<const float2 *>(d_F2), mask, G,
                          reinterpret_cast<float2 *>(d_ri), s);
 }

@@ -17,6 +17,12 @@
 // whose radix order is reversed, the second starts from the registers the first
 // ended in.
 //
+// Row mapping (TF = true): tid -> (t = tid % T, b = tid / T), lanes spread along
+// one line, for lines that are contiguous in global memory (a warp's register-end
+// loads and stores are then unit-stride).  Point p of line b sits at
+// buf[b * (L + L/16) + p + p/16]: one pad slot per 16 points keeps the stride-R
+// scatters of the early stages on distinct banks.
+//
 // Conventions (cuFFT C2C as used by the reference, cTDM/FFT.cu:697-838):
 // forward exp(-2 pi i k n / L), inverse exp(+2 pi i k n / L), both unnormalised.
 // Twiddles come from a per-length table tw[e] = exp(-2 pi i e / L) computed in
@@ -118,16 +124,25 @@ __device__ __forceinline__ void dftR(float2 *a)
 }
 
 // ---------------------------------------------------------------- one stage
+// Shared-memory position of point p: padded line stride LP (column mapping) or
+// one pad slot per 16 points (row mapping).
+template <int L, int LP, bool TF>
+struct Lay {
+    static constexpr int LINE = TF ? L + L / 16 : LP;
+    __device__ static __forceinline__ int at(int p) { return TF ? p + (p >> 4) : p; }
+};
+
 // Register tile v[E], E = L / T, viewed as PER butterflies of R points.
-template <int L, int T, int LP, int R>
+template <int L, int T, int LP, int R, bool TF = false>
 __device__ __forceinline__ void gather(const float2 *buf, float2 *v, int b, int t)
 {
+    using Y = Lay<L, LP, TF>;
     constexpr int NB = L / R, PER = NB / T;
-    const float2 *line = buf + b * LP;
+    const float2 *line = buf + b * Y::LINE;
 #pragma unroll
     for (int q = 0; q < PER; q++)
 #pragma unroll
-        for (int r = 0; r < R; r++) v[q * R + r] = line[t + T * q + r * NB];
+        for (int r = 0; r < R; r++) v[q * R + r] = line[Y::at(t + T * q + r * NB)];
 }
 
 template <int L, int T, bool INV, int NS, int R>
@@ -149,38 +164,39 @@ __device__ __forceinline__ void compute(float2 *v, const float2 *__restrict__ tw
     }
 }
 
-template <int L, int T, int LP, int NS, int R>
+template <int L, int T, int LP, int NS, int R, bool TF = false>
 __device__ __forceinline__ void scatter(float2 *buf, const float2 *v, int b, int t)
 {
+    using Y = Lay<L, LP, TF>;
     constexpr int NB = L / R, PER = NB / T;
-    float2 *line = buf + b * LP;
+    float2 *line = buf + b * Y::LINE;
 #pragma unroll
     for (int q = 0; q < PER; q++) {
         const int j = t + T * q;
         const int base = (j / NS) * NS * R + (j % NS);
 #pragma unroll
-        for (int r = 0; r < R; r++) line[base + r * NS] = v[q * R + r];
+        for (int r = 0; r < R; r++) line[Y::at(base + r * NS)] = v[q * R + r];
     }
 }
 
 // Stages in the order given.  GATHER0: the first stage reads shared memory
 // (else its inputs are already in v).  SCATTER_LAST: the last stage writes shared
 // memory (else its outputs stay in v).
-template <int L, int T, int LP, bool INV, bool GATHER0, bool SCATTER_LAST, int NS, int R, int... REST>
+template <int L, int T, int LP, bool INV, bool GATHER0, bool SCATTER_LAST, bool TF, int NS, int R, int... REST>
 __device__ __forceinline__ void stages(float2 *buf, float2 *v, const float2 *__restrict__ tw, int b, int t)
 {
     constexpr bool first = (NS == 1);
     constexpr bool last = (sizeof...(REST) == 0);
     if constexpr (!first || GATHER0) {
-        gather<L, T, LP, R>(buf, v, b, t);
+        gather<L, T, LP, R, TF>(buf, v, b, t);
         __syncthreads();
     }
     compute<L, T, INV, NS, R>(v, tw, t);
     if constexpr (!last || SCATTER_LAST) {
-        scatter<L, T, LP, NS, R>(buf, v, b, t);
+        scatter<L, T, LP, NS, R, TF>(buf, v, b, t);
         __syncthreads();
     }
-    if constexpr (!last) stages<L, T, LP, INV, GATHER0, SCATTER_LAST, NS * R, REST...>(buf, v, tw, b, t);
+    if constexpr (!last) stages<L, T, LP, INV, GATHER0, SCATTER_LAST, TF, NS * R, REST...>(buf, v, tw, b, t);
 }
 
 // ---------------------------------------------------------------- plans
@@ -198,14 +214,29 @@ template <int L> struct Plan;
         template <bool INV, bool GATHER0, bool SCATTER_LAST>                                        \
         __device__ static __forceinline__ void seq(float2 *buf, float2 *v, const float2 *tw)        \
         {                                                                                           \
-            stages<LL, TT, LP, INV, GATHER0, SCATTER_LAST, 1, FWD>(buf, v, tw, threadIdx.x % BB,    \
+            stages<LL, TT, LP, INV, GATHER0, SCATTER_LAST, false, 1, FWD>(buf, v, tw,               \
+                                                                   threadIdx.x % BB,                \
                                                                    threadIdx.x / BB);               \
         }                                                                                           \
         template <bool INV, bool GATHER0, bool SCATTER_LAST>                                        \
         __device__ static __forceinline__ void seqr(float2 *buf, float2 *v, const float2 *tw)       \
         {                                                                                           \
-            stages<LL, TT, LP, INV, GATHER0, SCATTER_LAST, 1, REV>(buf, v, tw, threadIdx.x % BB,    \
+            stages<LL, TT, LP, INV, GATHER0, SCATTER_LAST, false, 1, REV>(buf, v, tw,               \
+                                                                   threadIdx.x % BB,                \
                                                                    threadIdx.x / BB);               \
+        }                                                                                           \
+        /* the same under the row mapping (t = tid % T, b = tid / T) */                             \
+        template <bool INV>                                                                         \
+        __device__ static __forceinline__ void seq_row(float2 *buf, float2 *v, const float2 *tw)    \
+        {                                                                                           \
+            stages<LL, TT, LP, INV, false, false, true, 1, FWD>(buf, v, tw, threadIdx.x / TT,       \
+                                                                threadIdx.x % TT);                  \
+        }                                                                                           \
+        template <bool INV>                                                                         \
+        __device__ static __forceinline__ void seqr_row(float2 *buf, float2 *v, const float2 *tw)   \
+        {                                                                                           \
+            stages<LL, TT, LP, INV, false, false, true, 1, REV>(buf, v, tw, threadIdx.x / TT,       \
+                                                                 threadIdx.x % TT);                 \
         }                                                                                           \
         template <bool INV>                                                                         \
         __device__ static __forceinline__ void run(float2 *buf, const float2 *tw)                   \
@@ -254,6 +285,21 @@ template <int L>
 __host__ __device__ constexpr size_t smem_bytes()
 {
     return sizeof(float2) * Plan<L>::B * Plan<L>::LP;
+}
+
+// Resident CTAs per SM to ask of the register allocator: `want` for register
+// tiles of up to 16 points, fewer for the longer tiles so they do not spill.
+template <int L>
+__host__ __device__ constexpr int min_ctas(int want)
+{
+    return Plan<L>::E <= 16 ? want : (Plan<L>::E <= 32 ? 2 : 1);
+}
+
+// Shared memory of the row mapping.
+template <int L>
+__host__ __device__ constexpr size_t smem_bytes_row()
+{
+    return sizeof(float2) * Plan<L>::B * (L + L / 16);
 }
 
 }  // namespace fftl

@@ -49,6 +49,8 @@ struct LoopArgs {
     float inv_n3, k2, n_med, n_med2;
     float s1;   // -1 / (R^3 k^2)
     float s2;   // -k^2 / n_med^2
+    int *err;   // device status word: a bounded wait that ran out records a nonzero code
+    int staged; // z pass: F2 / mask tiles staged by TMA (set by the launcher)
 };
 
 cudaError_t launch_ewald(const EwaldArgs &a, cudaStream_t s);

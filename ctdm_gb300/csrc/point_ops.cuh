@@ -34,26 +34,24 @@ __device__ __forceinline__ float2 est_n(float2 F, float k2, float nm)
 
 // The same root for an unscaled inverse-transform value v: c = 1 + v s1 with
 // s1 = -1/(R^3 k^2) folding the 1/R^3 normalisation and the division by -k^2.
+// Evaluated without division or branch: with h = (|z| + |c|) / 2, the parts of
+// the principal root are sqrt(h) and |d| / (2 sqrt(h)); the first is the real
+// part when c >= 0 and the imaginary part (sign of d) when c < 0.  Square roots
+// come from the hardware reciprocal square root (sqrt(h) = h rsqrt(h)); a few ulp
+// against the correctly rounded form, far inside the loop's float32 error.
 __device__ __forceinline__ float2 est_n_scaled(float2 v, float s1, float nm)
 {
     const float c = fmaf(v.x, s1, 1.0f), d = v.y * s1;
-    const float mod = sqrtf(fmaf(c, c, d * d));
-    float a, b;
-    if (d == 0.0f) {
-        a = sqrtf(fmaxf(c, 0.0f));
-        b = 0.0f;
-    } else if (c >= 0.0f) {
-        a = sqrtf((mod + c) * 0.5f);
-        b = d * __frcp_rn(2.0f * a);
-    } else {
-        b = sqrtf((mod - c) * 0.5f);
-        a = fabsf(d) * __frcp_rn(2.0f * b);
-        if (d < 0.0f) b = -b;
-    }
-    float nr = a * nm, ni = b * nm;
-    if (nr < nm) nr = nm;
-    if (ni < 0.0f) ni = 0.0f;
-    return make_float2(nr, ni);
+    const float m2 = fmaf(c, c, d * d);
+    const float mod = m2 > 0.0f ? m2 * rsqrtf(m2) : 0.0f;
+    const float h = 0.5f * (mod + fabsf(c));
+    const float rh = h > 0.0f ? rsqrtf(h) : 0.0f;
+    const float big = h * rh, small = 0.5f * fabsf(d) * rh;
+    const bool pos = c >= 0.0f;
+    const float a = pos ? big : small;
+    const float bm = pos ? small : (d == 0.0f ? 0.0f : big);
+    const float b = copysignf(bm, d);
+    return make_float2(fmaxf(a * nm, nm), fmaxf(b * nm, 0.0f));
 }
 
 // Modify_F3D with the constants folded: f = ((nr^2 - ni^2) s2 + k^2, 2 nr ni s2),

@@ -1,0 +1,94 @@
+// Tensor-memory-accelerator (TMA) staging: tensor maps built on the host, bulk
+// tensor loads into shared memory completed on an mbarrier, inline PTX only.
+//
+// A kernel that stages a tile:
+//   thread 0: mbar_init(bar, 1); fence; __syncthreads();
+//   thread 0: mbar_expect_tx(bar, bytes); tma_load_3d(...) for each box;
+//   ... independent work ...
+//   every thread: mbar_wait(bar, 0, err)   (bounded: gives up and flags after a
+//                                          fixed number of polls, never spins forever)
+//
+// Rules kept by the callers: the innermost box extent times the element size is a
+// multiple of 16 bytes, the innermost start coordinate times the element size is a
+// multiple of 16 bytes, the global base is 16-byte aligned and every global stride
+// a multiple of 16 bytes; the shared destination is 128-byte aligned.
+#pragma once
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace tma {
+
+// ---------------------------------------------------------------- device side
+__device__ __forceinline__ uint32_t smem_addr(const void *p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+// Makes the initialised barrier visible to the asynchronous (TMA) proxy.
+__device__ __forceinline__ void fence_barrier_init()
+{
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// 3-D tiled bulk tensor load global -> shared, completing `bytes` on `bar`.
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int c0, int c1, int c2, uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_addr(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_addr(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
+{
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+
+// Bounded wait for phase `parity` of `bar`.  Returns false (and records `code` in
+// *err when err is given) if the phase has not completed after kMaxPolls polls;
+// each poll is a hardware try_wait, so the bound is well above any real copy.
+constexpr int kMaxPolls = 1 << 22;
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err, int code)
+{
+    for (int i = 0; i < kMaxPolls; i++)
+        if (mbar_try_wait(bar, parity)) return true;
+    if (err) atomicExch(err, code);
+    return false;
+}
+
+// Prefetch a tensor map descriptor (a kernel parameter) into the descriptor cache.
+__device__ __forceinline__ void prefetch_map(const CUtensorMap *map)
+{
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
+}
+
+// ---------------------------------------------------------------- host side
+// Tiled 3-D map over a dense array of `elem_bytes`-sized elements (1 or 8) with
+// extents dims[0] (fastest) .. dims[2] and box extents box[0..2].  The element
+// type only fixes the size; the bits are copied unchanged.
+cudaError_t make_map_3d(CUtensorMap *map, const void *base, int elem_bytes, const uint64_t dims[3],
+                        const uint32_t box[3]);
+
+}  // namespace tma

@@ -103,6 +103,10 @@ CTDM_API ctdm_status ctdm_ctx_read_buffer(ctdm_ctx *ctx, int which, void *host, 
  * are kept; later ones are not recorded. */
 CTDM_API ctdm_status ctdm_ctx_set_timing(ctdm_ctx *ctx, int on);
 CTDM_API ctdm_status ctdm_ctx_stage_times(ctdm_ctx *ctx, double *ms, int *counts, int n);
+/* Status word of the context's bounded device-side waits: 0, or the code of the
+ * first wait that ran out since the last read (1: a TMA tile of the positivity
+ * loop's z pass did not arrive).  Synchronises the device; reading clears it. */
+CTDM_API ctdm_status ctdm_ctx_device_status(ctdm_ctx *ctx, int *status);
 /* Number of kernels this library has launched in the process so far. */
 CTDM_API unsigned long long ctdm_launch_count(void);
 
