@@ -285,7 +285,9 @@ __global__ void __launch_bounds__(Plan<L>::THREADS) ypass_kernel(LoopArgs a, con
     extern __shared__ float4 smem4[];
     float2 *buf = reinterpret_cast<float2 *>(smem4);
     const long nl = (long)L * L;
-    const long line0 = (long)blockIdx.x * P::B;
+    // planes in descending z: the x pass runs them ascending, so each pass starts on
+    // the planes the previous one wrote last (still in L2)
+    const long line0 = (long)(gridDim.x - 1 - blockIdx.x) * P::B;
     bool ok;
     const long base = col_base<L>(line0, L, (long)L * L, nl, ok);
     const int t = threadIdx.x / P::B;
