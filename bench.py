@@ -31,6 +31,7 @@ sys.path.insert(0, ROOT)
 CONFIGS = {
     "plain_small": dict(iterations=10, goldstein=False),
     "wrap_heavy": dict(iterations=20, goldstein=True),
+    "batched": dict(iterations=10, goldstein=False, tomograms=64, lanes=4),
 }
 
 
@@ -167,6 +168,111 @@ def cpu_sample(acq, iters, goldstein=False, threads=None):
             f"iterations at {r}^3, extrapolated: {A}x{t_angle:.3f}s/angle + {t_fixed + t_map + t_p0:.2f}s + "
             f"{iters}x{t_iter:.2f}s/iter")
     return total, nthr, text
+
+
+# ---------------------------------------------------------------- batched workload
+def batched_jobs(dev, seed=3000, count=64, iterations=10):
+    """`count` tomograms: angle counts uniform in [31, 181], holograms 512^2 or 1024^2,
+    volumes 256^3 or 384^3 (seeded).  Two seeded random multi-ellipsoid cells (2-6
+    ellipsoids, RI 1.35-1.40), one per hologram size, are acquired at 181 cone angles;
+    a tomogram with A angles takes A of them spread evenly over the cone, gathered on
+    the device."""
+    import torch
+    import ctdm_gb300 as C
+    from ctdm_gb300 import phantom
+    rng = np.random.default_rng(seed)
+    bases = {}
+    for n in (512, 1024):
+        cell = phantom.random_cell(np.random.default_rng(seed + n), n * 0.1e-6)
+        acq = phantom.acquisition(n, 256, 181, na=0.9, seed=seed + n, ells=cell)
+        bases[n] = (acq, torch.from_numpy(acq.holograms).to(dev), torch.from_numpy(acq.background).to(dev))
+    jobs, meta = [], []
+    for _ in range(count):
+        a = int(rng.integers(31, 182))
+        n = int(rng.choice([512, 1024]))
+        r = int(rng.choice([256, 384]))
+        acq, holo, bg = bases[n]
+        idx = np.round(np.linspace(0, 180, a)).astype(np.int64)
+        h = holo.index_select(0, torch.from_numpy(idx).to(dev)).contiguous()
+        p = C.default_params(n_holo=n, m_crop=n // 4, r_vol=r, iterations=iterations, n_med=acq.n_med,
+                             wavelength=acq.wavelength, dx=acq.dx)
+        out = torch.empty((r, r, r), dtype=torch.complex64, device=dev)
+        jobs.append((p, h, bg, acq.ang_x[idx], acq.ang_y[idx], out))
+        meta.append((a, n, r))
+    return jobs, meta
+
+
+def run_batched(args):
+    import torch
+    import ctdm_gb300 as C
+    from ctdm_gb300 import build
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    build.build()
+    cfg = CONFIGS["batched"]
+    jobs, meta = batched_jobs(dev, seed=3000 + rank, count=cfg["tomograms"], iterations=cfg["iterations"])
+    stream = torch.cuda.current_stream(dev)
+    ctx = C.Context(local)
+
+    def one_by_one():
+        for (p, h, bg, ax, ay, out) in jobs:
+            ctx.reconstruct_device(p, h, bg, ax, ay, out, stream=stream)
+
+    batch = C.Batch(lanes=cfg["lanes"], device=local)
+    batch.plan(jobs)
+    for _ in range(args.warmup):
+        batch.run(stream)
+        one_by_one()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+
+    def timed(fn):
+        total = 0.0
+        for _ in range(args.steps):
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            b.synchronize()
+            total += a.elapsed_time(b)
+        return total
+
+    launches0 = C.launch_count()
+    ms_graph = timed(lambda: batch.run(stream))
+    ms_single = timed(one_by_one)
+    launches = C.launch_count() - launches0
+    clocks = sampler.stop()
+    tomos = len(jobs) * args.steps
+    line = {
+        "metric": "tomograms/s (hologram->RI), batched",
+        "value": tomos / (ms_graph / 1e3),
+        "unit": "tomograms/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_graph / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32/c64",
+        "data": "synthetic (two seeded random multi-ellipsoid cells acquired at 181 cone angles, Poisson noise)",
+        "config": {"workload": "batched", "tomograms": len(jobs), "lanes": cfg["lanes"],
+                   "angles": [m[0] for m in meta], "holograms": [m[1] for m in meta],
+                   "volumes": [m[2] for m in meta], "iterations": cfg["iterations"],
+                   "parallelism": f"replicas{world}", "l2": "inputs and volumes far larger than L2"},
+        "one_by_one": {"value": tomos / (ms_single / 1e3), "unit": "tomograms/s",
+                       "ms_per_step": ms_single / args.steps},
+        "speedup_vs_one_by_one": ms_single / ms_graph,
+        "e2e": None,
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+    }
+    print(json.dumps(line))
+    batch.close()
 
 
 # ---------------------------------------------------------------- GPU arm
@@ -309,6 +415,10 @@ def run_reference(args):
     rank, world, local = dist_info()
     if rank != 0:
         return
+    if args.config == "batched":
+        print(json.dumps({"impl": "reference", "unavailable": "the batched workload has no reference counterpart "
+                          "(the reference reconstructs one tomogram per BatchRecon call)"}))
+        return
     cfg = CONFIGS[args.config]
     acq = make_workload(args.config, seed=1000)
     times = []
@@ -352,6 +462,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.config == "batched":
+        run_batched(args)
     else:
         run_ours(args)
 

@@ -196,6 +196,56 @@ def fft(data, dims, batch=1, inverse=False, stream=None):
     check(load().ctdm_fft(_ptr(data), len(dims), d, batch, int(inverse), _stream(stream)), "ctdm_fft")
 
 
+class Batch:
+    """Batched reconstruction (ctdm_batch): jobs = [(params, holo, bg, angx, angy, out), ...]
+    with device tensors; plan() schedules them over `lanes` workspaces, runs them once and
+    captures one CUDA graph; run() is a single graph launch."""
+
+    def __init__(self, lanes=4, device=0):
+        self.lib = load()
+        h = ctypes.c_void_p()
+        check(self.lib.ctdm_batch_create(int(device), int(lanes), ctypes.byref(h)), "ctdm_batch_create")
+        self.handle = h
+        self._keep = []
+
+    def plan(self, jobs):
+        arr = (_lib.Job * len(jobs))()
+        keep = []
+        for i, (params, holo, bg, angx, angy, out) in enumerate(jobs):
+            ax, ay = _f32(angx), _f32(angy)
+            keep += [ax, ay]
+            arr[i].params = params
+            arr[i].n_angles = len(ax)
+            arr[i].d_holo, arr[i].d_bg = _ptr(holo), _ptr(bg)
+            arr[i].h_angx, arr[i].h_angy = ax.ctypes.data, ay.ctypes.data
+            arr[i].d_ri = _ptr(out)
+        check(self.lib.ctdm_batch_plan(self.handle, arr, len(jobs)), "ctdm_batch_plan")
+        self._keep = keep
+        self.n_jobs = len(jobs)
+
+    def run(self, stream=None):
+        check(self.lib.ctdm_batch_run(self.handle, _stream(stream)), "ctdm_batch_run")
+
+    def run_eager(self, stream=None):
+        check(self.lib.ctdm_batch_run_eager(self.handle, _stream(stream)), "ctdm_batch_run_eager")
+
+    def lanes(self):
+        out = (ctypes.c_int * self.n_jobs)()
+        check(self.lib.ctdm_batch_lanes(self.handle, out, self.n_jobs), "ctdm_batch_lanes")
+        return list(out)
+
+    def close(self):
+        if self.handle:
+            self.lib.ctdm_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Tape:
     """Measurement operator A = P F~ of one tomogram (ctdm_tape) with its adjoint,
     shaped like a torch.autograd.Function: forward(V) -> y, backward(dL/dy) -> dL/dV."""

@@ -23,6 +23,14 @@ class Params(ctypes.Structure):
     ]
 
 
+class Job(ctypes.Structure):
+    """ctdm_job (include/ctdm.h)."""
+    _fields_ = [
+        ("params", Params), ("n_angles", c_int), ("d_holo", c_void_p), ("d_bg", c_void_p),
+        ("h_angx", c_void_p), ("h_angy", c_void_p), ("d_ri", c_void_p),
+    ]
+
+
 # name -> (restype, argtypes)
 _SIGS = {
     "ctdm_params_default": (None, [ctypes.POINTER(Params)]),
@@ -68,6 +76,12 @@ _SIGS = {
     "ctdm_reconstruct_gradient": (c_int, [c_void_p, c_int, c_double, c_double, c_double, c_void_p, c_void_p,
                                           c_void_p]),
     "ctdm_contrast_to_ri": (c_int, [c_int, c_void_p, c_double, c_int, c_void_p, c_void_p]),
+    "ctdm_batch_create": (c_int, [c_int, c_int, ctypes.POINTER(c_void_p)]),
+    "ctdm_batch_destroy": (None, [c_void_p]),
+    "ctdm_batch_plan": (c_int, [c_void_p, ctypes.POINTER(Job), c_int]),
+    "ctdm_batch_run": (c_int, [c_void_p, c_void_p]),
+    "ctdm_batch_run_eager": (c_int, [c_void_p, c_void_p]),
+    "ctdm_batch_lanes": (c_int, [c_void_p, P_int, c_int]),
     "ctdm_set_recon_globals": (None, [c_int, c_double, c_double, c_double, c_double, c_int, c_int, ctypes.c_char_p]),
     "DCT_UWLS_Unwrapped": (None, [c_void_p, c_void_p, c_int, c_int]),
     "FastUnwrapping": (None, [c_void_p, c_void_p, c_int, c_int]),

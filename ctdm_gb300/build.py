@@ -18,7 +18,7 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libctdm_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["ctdm_api.cu", "k_recon.cu", "k_qpi.cu", "k_dct.cu", "k_stack.cu", "k_compat.cu", "k_fastuw.cu",
-           "k_gold.cu", "k_noalloc.cu", "k_grad.cu"]
+           "k_gold.cu", "k_noalloc.cu", "k_grad.cu", "batch.cu"]
 
 
 def nvcc():

@@ -76,6 +76,7 @@ void set_error_message(const char *msg) { g_err = msg ? msg : ""; }
 static std::atomic<unsigned long long> g_launches{0};
 namespace ctdm {
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void note_launches(unsigned long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 }  // namespace ctdm
 extern "C" unsigned long long ctdm_launch_count(void) { return g_launches.load(); }
 extern "C" const char *ctdm_version(void) { return "ctdm_gb300 0.1 (sm_103a)"; }
@@ -532,16 +533,13 @@ static ctdm_status validate(const ctdm_params *p, int A, int &M)
 }
 
 // ---------------------------------------------------------------- pipeline
-extern "C" ctdm_status ctdm_reconstruct_device(ctdm_ctx *c, const ctdm_params *p, int A, const float *d_holo,
-                                               const float *d_bg, const float *h_angx, const float *h_angy,
-                                               ctdm_cfloat *d_ri, void *stream)
+// The whole path on stream s with the angle geometry already on the device.  It
+// makes no host-synchronous call once the context's workspace has grown to the
+// call's sizes, so a warmed-up call can be captured into a CUDA graph.
+static ctdm_status pipeline_core(ctdm_ctx *c, const ctdm_params *p, int A, int M, const float *d_holo,
+                                 const float *d_bg, const AngleGeom *d_geom, ctdm_cfloat *d_ri, cudaStream_t s)
 {
-    if (!c || !d_holo || !d_bg || !h_angx || !h_angy || !d_ri) return invalid("ctdm_reconstruct_device: NULL argument");
-    int M;
-    ctdm_status st = validate(p, A, M);
-    if (st != CTDM_OK) return st;
-    CK(cudaSetDevice(c->device), "cudaSetDevice");
-    cudaStream_t s = (cudaStream_t)stream;
+    ctdm_status st;
     const int N = p->n_holo, R = p->r_vol;
     const long mm = (long)M * M, rr = (long)R * R, r3 = rr * R;
     CK(ensure(c, B_PHASE, sizeof(float) * A * mm), "alloc phase");
@@ -617,11 +615,9 @@ extern "C" ctdm_status ctdm_reconstruct_device(ctdm_ctx *c, const ctdm_params *p
     const double fm0 = p->n_med / p->wavelength;
     const double df = 1.0 / (R * p->dx);
     const double k = 2.0 * CTDM_PI_D * p->n_med / p->wavelength;
-    st = upload_geometry(c, h_angx, h_angy, A, fm0, df, s);
-    if (st != CTDM_OK) return st;
     EwaldArgs ea;
     ea.U = B<float2>(c, B_U);
-    ea.geom = B<AngleGeom>(c, B_GEOM);
+    ea.geom = d_geom;
     ea.A = A;
     ea.R = R;
     ea.fm0 = fm0;
@@ -640,10 +636,49 @@ extern "C" ctdm_status ctdm_reconstruct_device(ctdm_ctx *c, const ctdm_params *p
                        reinterpret_cast<float2 *>(d_ri), s);
     if (st != CTDM_OK) return st;
     if (gold_side) CK(cudaStreamWaitEvent(s, c->join, 0), "join wait");
+    return CTDM_OK;
+}
+
+extern "C" ctdm_status ctdm_reconstruct_device(ctdm_ctx *c, const ctdm_params *p, int A, const float *d_holo,
+                                               const float *d_bg, const float *h_angx, const float *h_angy,
+                                               ctdm_cfloat *d_ri, void *stream)
+{
+    if (!c || !d_holo || !d_bg || !h_angx || !h_angy || !d_ri) return invalid("ctdm_reconstruct_device: NULL argument");
+    int M;
+    ctdm_status st = validate(p, A, M);
+    if (st != CTDM_OK) return st;
+    CK(cudaSetDevice(c->device), "cudaSetDevice");
+    cudaStream_t s = (cudaStream_t)stream;
+    st = upload_geometry(c, h_angx, h_angy, A, p->n_med / p->wavelength, 1.0 / (p->r_vol * p->dx), s);
+    if (st != CTDM_OK) return st;
+    st = pipeline_core(c, p, A, M, d_holo, d_bg, B<AngleGeom>(c, B_GEOM), d_ri, s);
+    if (st != CTDM_OK) return st;
     CK(cudaMemcpyAsync(c->carrier, c->buf[B_CARRIER], sizeof(int) * 3, cudaMemcpyDeviceToHost, s), "carrier readback");
     g_err.clear();
     return CTDM_OK;
 }
+
+// ---------------------------------------------------------------- internal interface (batch scheduler)
+namespace ctdm {
+ctdm_status validate_params(const ctdm_params *p, int A, int &M) { return validate(p, A, M); }
+ctdm_status run_pipeline(ctdm_ctx *c, const ctdm_params *p, int A, const float *d_holo, const float *d_bg,
+                         const AngleGeom *d_geom, ctdm_cfloat *d_ri, cudaStream_t s)
+{
+    int M;
+    ctdm_status st = validate(p, A, M);
+    if (st != CTDM_OK) return st;
+    CK(cudaSetDevice(c->device), "cudaSetDevice");
+    return pipeline_core(c, p, A, M, d_holo, d_bg, d_geom, d_ri, s);
+}
+void make_geometry(const float *angx, const float *angy, int A, double fm0, double df, std::vector<AngleGeom> &g)
+{
+    angle_geometry(angx, angy, A, fm0, df, g);
+}
+ctdm_status fail_invalid(const char *msg) { return invalid("%s", msg); }
+ctdm_status fail_cuda(cudaError_t e, const char *what) { return cuda_fail(e, what); }
+void clear_error() { g_err.clear(); }
+int max_angles() { return kMaxAngles; }
+}  // namespace ctdm
 
 extern "C" ctdm_status ctdm_reconstruct(ctdm_ctx *c, const ctdm_params *p, int A, const float *h_holo,
                                         const float *h_bg, const float *h_angx, const float *h_angy,

@@ -107,7 +107,8 @@ CTDM_API ctdm_status ctdm_ctx_stage_times(ctdm_ctx *ctx, double *ms, int *counts
  * first wait that ran out since the last read (1: a TMA tile of the positivity
  * loop's z pass did not arrive).  Synchronises the device; reading clears it. */
 CTDM_API ctdm_status ctdm_ctx_device_status(ctdm_ctx *ctx, int *status);
-/* Number of kernels this library has launched in the process so far. */
+/* Number of kernels this library has launched in the process so far (a batch graph
+ * launch counts the kernels captured in it). */
 CTDM_API unsigned long long ctdm_launch_count(void);
 
 /* --- whole path (replaces HilbertTransform's per-frame loop + BatchRecon) --- */
@@ -120,6 +121,35 @@ CTDM_API ctdm_status ctdm_reconstruct_device(ctdm_ctx *ctx, const ctdm_params *p
 /* Same with host buffers: copies in, reconstructs, copies the volume out, syncs. */
 CTDM_API ctdm_status ctdm_reconstruct(ctdm_ctx *ctx, const ctdm_params *p, int n_angles, const float *h_holo,
                              const float *h_bg, const float *h_angx, const float *h_angy, ctdm_cfloat *h_ri);
+
+/* --- batched reconstruction (no reference counterpart) ----------------------------
+ * Many independent tomograms, each with its own sizes and angle count, scheduled over
+ * `lanes` concurrent workspaces and captured into one CUDA graph: ctdm_batch_run is a
+ * single graph launch for the whole batch.  ctdm_batch_plan validates every job, runs
+ * the batch once eagerly (allocating each lane's workspace for its largest job; the
+ * outputs of that run are valid results), then captures the same launches.  The plan
+ * keeps the job pointers: to reconstruct new data, overwrite the same input buffers
+ * and run again.  Angles are copied at plan time.  The reference's one-tomogram path
+ * is BatchRecon (cTDM/HilbertTransform.cu:1825-2047). */
+typedef struct {
+    ctdm_params params;
+    int n_angles;
+    const float *d_holo;   /* A*N*N f32, device */
+    const float *d_bg;     /* N*N (or A*N*N with bg_per_angle) f32, device */
+    const float *h_angx;   /* A f32 radians, host */
+    const float *h_angy;
+    ctdm_cfloat *d_ri;     /* R^3 complex out, device, octant-shifted */
+} ctdm_job;
+typedef struct ctdm_batch ctdm_batch;
+CTDM_API ctdm_status ctdm_batch_create(int device, int lanes, ctdm_batch **out);
+CTDM_API void ctdm_batch_destroy(ctdm_batch *batch);
+CTDM_API ctdm_status ctdm_batch_plan(ctdm_batch *batch, const ctdm_job *jobs, int n_jobs);
+/* One graph launch on `stream` (cudaStream_t, NULL = legacy default). */
+CTDM_API ctdm_status ctdm_batch_run(ctdm_batch *batch, void *stream);
+/* The planned schedule launched kernel by kernel (no graph), for comparison. */
+CTDM_API ctdm_status ctdm_batch_run_eager(ctdm_batch *batch, void *stream);
+/* Lane each job was assigned to (longest job first onto the least-loaded lane). */
+CTDM_API ctdm_status ctdm_batch_lanes(const ctdm_batch *batch, int *lane_of_job, int n_jobs);
 
 /* --- stages (device pointers) --- */
 /* QPI Algorithm A.  carrier3: in {row, col, radius} (any < 0: detect from the first
