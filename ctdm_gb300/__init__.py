@@ -196,6 +196,33 @@ def fft(data, dims, batch=1, inverse=False, stream=None):
     check(load().ctdm_fft(_ptr(data), len(dims), d, batch, int(inverse), _stream(stream)), "ctdm_fft")
 
 
+def plan_count(r):
+    """FFT plan variants of the loop passes for volume side r."""
+    return int(load().ctdm_plan_count(int(r)))
+
+
+def autotune(r, check_mode=CTDM_CHECK_REF, device=0):
+    """Tune the loop passes for side r now: (variants (x, y, z), {(pass, variant): ms})."""
+    v = (ctypes.c_int * 3)()
+    ms = (ctypes.c_double * 9)(*([float("nan")] * 9))
+    check(load().ctdm_autotune(int(device), int(r), int(check_mode), v, ms, 9), "ctdm_autotune")
+    n = plan_count(r)
+    return tuple(v), {(p, k): ms[3 * p + k] for p in range(3) for k in range(n)}
+
+
+def plans(r, device=0):
+    """(variants (x, y, z), tuned) currently used for side r."""
+    v = (ctypes.c_int * 3)()
+    t = ctypes.c_int()
+    check(load().ctdm_plans(int(device), int(r), v, ctypes.byref(t)), "ctdm_plans")
+    return tuple(v), bool(t.value)
+
+
+def set_plans(r, variants, device=0):
+    v = (ctypes.c_int * 3)(*variants)
+    check(load().ctdm_set_plans(int(device), int(r), v), "ctdm_set_plans")
+
+
 class Batch:
     """Batched reconstruction (ctdm_batch): jobs = [(params, holo, bg, angx, angy, out), ...]
     with device tensors; plan() schedules them over `lanes` workspaces, runs them once and

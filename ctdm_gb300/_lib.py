@@ -82,6 +82,10 @@ _SIGS = {
     "ctdm_batch_run": (c_int, [c_void_p, c_void_p]),
     "ctdm_batch_run_eager": (c_int, [c_void_p, c_void_p]),
     "ctdm_batch_lanes": (c_int, [c_void_p, P_int, c_int]),
+    "ctdm_plan_count": (c_int, [c_int]),
+    "ctdm_autotune": (c_int, [c_int, c_int, c_int, P_int, ctypes.POINTER(c_double), c_int]),
+    "ctdm_plans": (c_int, [c_int, c_int, P_int, P_int]),
+    "ctdm_set_plans": (c_int, [c_int, c_int, P_int]),
     "ctdm_set_recon_globals": (None, [c_int, c_double, c_double, c_double, c_double, c_int, c_int, ctypes.c_char_p]),
     "DCT_UWLS_Unwrapped": (None, [c_void_p, c_void_p, c_int, c_int]),
     "FastUnwrapping": (None, [c_void_p, c_void_p, c_int, c_int]),

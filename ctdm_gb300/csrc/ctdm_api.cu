@@ -499,6 +499,7 @@ static ctdm_status do_positivity(ctdm_ctx *c, int R, int iters, int check_mode, 
     la.s1 = (float)(-1.0 / ((double)R * R * R * k2));
     la.s2 = (float)(-k2 / (n_med * n_med));
     la.err = c->d_err;
+    CK(ensure_tuned(R, check_mode, s), "autotune loop passes");
     StageTimer &tm = c->timer;
     CK(launch_ypass(la, true, s), "y inverse pass");
     tm.mark(S_YINV, s);

@@ -200,51 +200,63 @@ __device__ __forceinline__ void stages(float2 *buf, float2 *v, const float2 *__r
 }
 
 // ---------------------------------------------------------------- plans
-// Per length: lines per CTA (B), threads per line (T), radix sequence.  run()
-// uses the sequence as listed, runr() the reversed one.
-template <int L> struct Plan;
-#define FFTL_PLAN(LL, BB, TT, FWD, REV)                                                             \
-    template <> struct Plan<LL> {                                                                   \
-        static constexpr int B = BB, T = TT;                                                        \
-        static constexpr int PAD = (BB >= 16) ? 1 : (16 / BB);                                      \
-        static constexpr int LP = LL + PAD;                                                         \
-        static constexpr int THREADS = BB * TT;                                                     \
-        static constexpr int E = LL / TT;                                                           \
-        /* first / last radix of the listed order (the reversed order swaps them) */                \
-        template <bool INV, bool GATHER0, bool SCATTER_LAST>                                        \
-        __device__ static __forceinline__ void seq(float2 *buf, float2 *v, const float2 *tw)        \
-        {                                                                                           \
-            stages<LL, TT, LP, INV, GATHER0, SCATTER_LAST, false, 1, FWD>(buf, v, tw,               \
-                                                                   threadIdx.x % BB,                \
-                                                                   threadIdx.x / BB);               \
-        }                                                                                           \
-        template <bool INV, bool GATHER0, bool SCATTER_LAST>                                        \
-        __device__ static __forceinline__ void seqr(float2 *buf, float2 *v, const float2 *tw)       \
-        {                                                                                           \
-            stages<LL, TT, LP, INV, GATHER0, SCATTER_LAST, false, 1, REV>(buf, v, tw,               \
-                                                                   threadIdx.x % BB,                \
-                                                                   threadIdx.x / BB);               \
-        }                                                                                           \
-        /* the same under the row mapping (t = tid % T, b = tid / T) */                             \
-        template <bool INV>                                                                         \
-        __device__ static __forceinline__ void seq_row(float2 *buf, float2 *v, const float2 *tw)    \
-        {                                                                                           \
-            stages<LL, TT, LP, INV, false, false, true, 1, FWD>(buf, v, tw, threadIdx.x / TT,       \
-                                                                threadIdx.x % TT);                  \
-        }                                                                                           \
-        template <bool INV>                                                                         \
-        __device__ static __forceinline__ void seqr_row(float2 *buf, float2 *v, const float2 *tw)   \
-        {                                                                                           \
-            stages<LL, TT, LP, INV, false, false, true, 1, REV>(buf, v, tw, threadIdx.x / TT,       \
-                                                                 threadIdx.x % TT);                 \
-        }                                                                                           \
-        template <bool INV>                                                                         \
-        __device__ static __forceinline__ void run(float2 *buf, const float2 *tw)                   \
-        {                                                                                           \
-            float2 v[E];                                                                            \
-            seq<INV, true, true>(buf, v, tw);                                                       \
-        }                                                                                           \
-    };
+// A plan: line length L, B lines per CTA, T threads per line and the radix
+// sequence.  seq() runs the sequence as listed, seqr() reversed; *_row() are the
+// same under the row mapping.  F0 / RV0: first radix of the listed / reversed order
+// (the radices at the register-resident ends).
+template <int... Rs>
+struct Radices {};
+template <int A, int... Rest>
+struct FirstOf {
+    static constexpr int v = A;
+};
+
+template <int L_, int B_, int T_, class FWD, class REV>
+struct PlanT;
+template <int L_, int B_, int T_, int... FW, int... RV>
+struct PlanT<L_, B_, T_, Radices<FW...>, Radices<RV...>> {
+    static constexpr int L = L_, B = B_, T = T_;
+    static constexpr int PAD = (B >= 16) ? 1 : (16 / B);
+    static constexpr int LP = L + PAD;
+    static constexpr int THREADS = B * T;
+    static constexpr int E = L / T;
+    static constexpr int F0 = FirstOf<FW...>::v, RV0 = FirstOf<RV...>::v;
+    static_assert(E * T == L, "threads per line must divide the length");
+    template <bool INV, bool GATHER0, bool SCATTER_LAST>
+    __device__ static __forceinline__ void seq(float2 *buf, float2 *v, const float2 *tw)
+    {
+        stages<L, T, LP, INV, GATHER0, SCATTER_LAST, false, 1, FW...>(buf, v, tw, threadIdx.x % B, threadIdx.x / B);
+    }
+    template <bool INV, bool GATHER0, bool SCATTER_LAST>
+    __device__ static __forceinline__ void seqr(float2 *buf, float2 *v, const float2 *tw)
+    {
+        stages<L, T, LP, INV, GATHER0, SCATTER_LAST, false, 1, RV...>(buf, v, tw, threadIdx.x % B, threadIdx.x / B);
+    }
+    template <bool INV>
+    __device__ static __forceinline__ void seq_row(float2 *buf, float2 *v, const float2 *tw)
+    {
+        stages<L, T, LP, INV, false, false, true, 1, FW...>(buf, v, tw, threadIdx.x / T, threadIdx.x % T);
+    }
+    template <bool INV>
+    __device__ static __forceinline__ void seqr_row(float2 *buf, float2 *v, const float2 *tw)
+    {
+        stages<L, T, LP, INV, false, false, true, 1, RV...>(buf, v, tw, threadIdx.x / T, threadIdx.x % T);
+    }
+    template <bool INV>
+    __device__ static __forceinline__ void run(float2 *buf, const float2 *tw)
+    {
+        float2 v[E];
+        seq<INV, true, true>(buf, v, tw);
+    }
+};
+
+// Default plan per length (2-D transforms, QPI, DCT, Ewald mapping, and variant 0
+// of the volume passes).
+template <int L>
+struct Plan;
+#define FFTL_PLAN(LL, BB, TT, FWD, REV) \
+    template <>                         \
+    struct Plan<LL> : PlanT<LL, BB, TT, Radices<FWD>, Radices<REV>> {};
 #define FFTL_LIST(...) __VA_ARGS__
 FFTL_PLAN(16, 64, 4, FFTL_LIST(4, 4), FFTL_LIST(4, 4))
 FFTL_PLAN(32, 64, 4, FFTL_LIST(8, 4), FFTL_LIST(4, 8))
@@ -258,20 +270,28 @@ FFTL_PLAN(1024, 8, 32, FFTL_LIST(16, 16, 4), FFTL_LIST(4, 16, 16))
 FFTL_PLAN(1536, 8, 32, FFTL_LIST(16, 16, 3, 2), FFTL_LIST(2, 3, 16, 16))
 FFTL_PLAN(2048, 4, 64, FFTL_LIST(16, 16, 8), FFTL_LIST(8, 16, 16))
 #undef FFTL_PLAN
+#undef FFTL_LIST
 
 // First radix of the listed (forward) sequence and of the reversed one.
-template <int L> struct Ends;
-template <> struct Ends<16> { static constexpr int F = 4, Rv = 4; };
-template <> struct Ends<32> { static constexpr int F = 8, Rv = 4; };
-template <> struct Ends<64> { static constexpr int F = 8, Rv = 8; };
-template <> struct Ends<128> { static constexpr int F = 16, Rv = 8; };
-template <> struct Ends<256> { static constexpr int F = 16, Rv = 16; };
-template <> struct Ends<384> { static constexpr int F = 16, Rv = 3; };
-template <> struct Ends<512> { static constexpr int F = 8, Rv = 8; };
-template <> struct Ends<768> { static constexpr int F = 16, Rv = 3; };
-template <> struct Ends<1024> { static constexpr int F = 16, Rv = 4; };
-template <> struct Ends<1536> { static constexpr int F = 16, Rv = 2; };
-template <> struct Ends<2048> { static constexpr int F = 16, Rv = 8; };
+template <int L>
+struct Ends {
+    static constexpr int F = Plan<L>::F0, Rv = Plan<L>::RV0;
+};
+
+// Plan variants of the volume passes, chosen per pass by the autotuner.  Every
+// stage's butterfly count L / R must be a multiple of T.
+template <int L, int V>
+struct PV;
+template <int L>
+struct PV<L, 0> : Plan<L> {};
+template <> struct PV<256, 1> : PlanT<256, 8, 16, Radices<16, 16>, Radices<16, 16>> {};
+template <> struct PV<256, 2> : PlanT<256, 16, 32, Radices<8, 4, 8>, Radices<8, 4, 8>> {};
+template <> struct PV<384, 1> : PlanT<384, 16, 16, Radices<4, 4, 8, 3>, Radices<3, 8, 4, 4>> {};
+template <> struct PV<384, 2> : PlanT<384, 8, 16, Radices<4, 4, 8, 3>, Radices<3, 8, 4, 4>> {};
+template <> struct PV<512, 1> : PlanT<512, 16, 32, Radices<8, 8, 8>, Radices<8, 8, 8>> {};
+template <> struct PV<512, 2> : PlanT<512, 8, 32, Radices<8, 8, 8>, Radices<8, 8, 8>> {};
+template <> struct PV<768, 1> : PlanT<768, 8, 32, Radices<8, 8, 4, 3>, Radices<3, 4, 8, 8>> {};
+template <> struct PV<768, 2> : PlanT<768, 16, 32, Radices<8, 8, 4, 3>, Radices<3, 4, 8, 8>> {};
 
 // Point index of register slot i (butterfly q = i / R, point r = i % R) at the
 // register-resident end of a sequence whose end radix is R: j + r * (L / R).
@@ -285,6 +305,26 @@ template <int L>
 __host__ __device__ constexpr size_t smem_bytes()
 {
     return sizeof(float2) * Plan<L>::B * Plan<L>::LP;
+}
+template <class P>
+__host__ __device__ constexpr size_t plan_smem()
+{
+    return sizeof(float2) * P::B * P::LP;
+}
+template <class P>
+__host__ __device__ constexpr size_t plan_smem_row()
+{
+    return sizeof(float2) * P::B * (P::L + P::L / 16);
+}
+// Resident CTAs per SM to ask of the register allocator for a plan: `want` for
+// register tiles of up to 16 points, fewer for longer tiles.
+template <class P>
+__host__ __device__ constexpr int plan_min_ctas(int want)
+{
+    // two-stage tiles of up to 16 points: `want` x 256 resident threads per SM;
+    // longer tiles or three-stage lengths (more twiddles live): 512
+    return (P::E <= 16 && P::L <= 256) ? (want * 256 / P::THREADS > 0 ? want * 256 / P::THREADS : 1)
+                                       : (P::E <= 32 ? (512 / P::THREADS > 0 ? 512 / P::THREADS : 1) : 1);
 }
 
 // Resident CTAs per SM to ask of the register allocator: `want` for register

@@ -58,6 +58,21 @@ cudaError_t launch_xpass(const LoopArgs &a, bool final_pass, cudaStream_t s);
 cudaError_t launch_ypass(const LoopArgs &a, bool inverse, cudaStream_t s);
 cudaError_t launch_zpass(const LoopArgs &a, int check_mode, cudaStream_t s);
 
+// Positivity-loop passes by plan variant (one translation unit per volume side).
+enum LoopKind { LOOP_X = 0, LOOP_X_FINAL = 1, LOOP_Y_FWD = 2, LOOP_Y_INV = 3, LOOP_Z = 4 };
+cudaError_t loop_pass_32(int kind, int variant, const LoopArgs &a, int flag, cudaStream_t s);
+cudaError_t loop_pass_64(int kind, int variant, const LoopArgs &a, int flag, cudaStream_t s);
+cudaError_t loop_pass_128(int kind, int variant, const LoopArgs &a, int flag, cudaStream_t s);
+cudaError_t loop_pass_256(int kind, int variant, const LoopArgs &a, int flag, cudaStream_t s);
+cudaError_t loop_pass_384(int kind, int variant, const LoopArgs &a, int flag, cudaStream_t s);
+cudaError_t loop_pass_512(int kind, int variant, const LoopArgs &a, int flag, cudaStream_t s);
+cudaError_t loop_pass_768(int kind, int variant, const LoopArgs &a, int flag, cudaStream_t s);
+// Number of plan variants of the loop passes for volume side R (0: unsupported).
+int loop_plan_count(int R);
+cudaError_t loop_pass_variant(int kind, int variant, const LoopArgs &a, int flag, cudaStream_t s);
+// Autotuner (tune.cu): tunes volume side R on this device on first use.
+cudaError_t ensure_tuned(int R, int check_mode, cudaStream_t s);
+
 // Generic batched transforms.  rows: nlines contiguous lines of length L.
 // cols: lines of length L with element p at (l % nx) + (l / nx) * plane + p * ld.
 cudaError_t fft_rows(float2 *data, int L, long nlines, bool inverse, cudaStream_t s);

@@ -1,0 +1,257 @@
+// Autotuner of the positivity-loop passes: per device and volume side it times
+// every FFT plan variant (lines per CTA, threads per line, radix sequence; see
+// fft_line.cuh PV<R, v>) of the x, y and z passes on scratch volumes and keeps the
+// fastest per pass.  The first reconstruction of a new volume side tunes it
+// (unless CTDM_AUTOTUNE=0 in the environment, or the stream is being captured);
+// ctdm_autotune runs it explicitly and ctdm_set_plans pins a choice.
+//
+// No reference counterpart: the reference calls cuFFT with a fixed plan per call
+// (cTDM/FFT.cu:807-838).
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <set>
+#include <utility>
+#include <vector>
+
+#include "api_internal.h"
+
+namespace ctdm {
+
+struct PlanChoice {
+    int v[3] = {0, 0, 0};   // x, y, z pass
+    bool tuned = false;
+};
+static std::mutex g_tune_mu;
+static std::map<std::pair<int, int>, PlanChoice> g_choice;   // (device, R)
+
+static std::mutex g_cfg_mu;
+static std::set<std::pair<const void *, int>> g_configured;   // (kernel, device) with attributes set
+bool kernel_configured(const void *fn, int dev)
+{
+    std::lock_guard<std::mutex> lk(g_cfg_mu);
+    return g_configured.count({fn, dev}) != 0;
+}
+void mark_kernel_configured(const void *fn, int dev)
+{
+    std::lock_guard<std::mutex> lk(g_cfg_mu);
+    g_configured.insert({fn, dev});
+}
+
+int loop_plan_count(int R)
+{
+    switch (R) {
+    case 32: case 64: case 128: return 1;
+    case 256: case 384: case 512: case 768: return 3;
+    default: return 0;
+    }
+}
+
+cudaError_t loop_pass_variant(int kind, int variant, const LoopArgs &a, int flag, cudaStream_t s)
+{
+    switch (a.R) {
+    case 32: return loop_pass_32(kind, variant, a, flag, s);
+    case 64: return loop_pass_64(kind, variant, a, flag, s);
+    case 128: return loop_pass_128(kind, variant, a, flag, s);
+    case 256: return loop_pass_256(kind, variant, a, flag, s);
+    case 384: return loop_pass_384(kind, variant, a, flag, s);
+    case 512: return loop_pass_512(kind, variant, a, flag, s);
+    case 768: return loop_pass_768(kind, variant, a, flag, s);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+static PlanChoice choice_of(int R)
+{
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_choice.find({dev, R});
+    return it == g_choice.end() ? PlanChoice() : it->second;
+}
+
+cudaError_t launch_xpass(const LoopArgs &a, bool final_pass, cudaStream_t s)
+{
+    return loop_pass_variant(final_pass ? LOOP_X_FINAL : LOOP_X, choice_of(a.R).v[0], a, 0, s);
+}
+cudaError_t launch_ypass(const LoopArgs &a, bool inverse, cudaStream_t s)
+{
+    return loop_pass_variant(inverse ? LOOP_Y_INV : LOOP_Y_FWD, choice_of(a.R).v[1], a, 0, s);
+}
+cudaError_t launch_zpass(const LoopArgs &a, int check_mode, cudaStream_t s)
+{
+    return loop_pass_variant(LOOP_Z, choice_of(a.R).v[2], a, check_mode, s);
+}
+
+// Median time (ms) of `reps` launches of one pass variant on stream s.
+static cudaError_t time_variant(int kind, int v, const LoopArgs &a, int flag, cudaStream_t s, int reps, double &ms)
+{
+    cudaEvent_t e0, e1;
+    cudaError_t e = cudaEventCreate(&e0);
+    if (e != cudaSuccess) return e;
+    e = cudaEventCreate(&e1);
+    if (e != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return e;
+    }
+    std::vector<double> t;
+    e = loop_pass_variant(kind, v, a, flag, s);   // warm-up (module load, attributes)
+    for (int r = 0; r < reps && e == cudaSuccess; r++) {
+        cudaEventRecord(e0, s);
+        e = loop_pass_variant(kind, v, a, flag, s);
+        cudaEventRecord(e1, s);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        float dt = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&dt, e0, e1);
+        t.push_back(dt);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess) return e;
+    std::sort(t.begin(), t.end());
+    ms = t[t.size() / 2];
+    return cudaSuccess;
+}
+
+// Times every variant of every pass at volume side R on zero-filled scratch volumes
+// (the passes are data-independent in cost) and records the fastest.
+cudaError_t autotune_loop(int R, int check_mode, int *chosen, double *ms_out, int n_ms)
+{
+    const int nv = loop_plan_count(R);
+    if (nv == 0) return cudaErrorInvalidValue;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const size_t r3 = (size_t)R * R * R;
+    float2 *G = nullptr, *F2 = nullptr;
+    uint8_t *mask = nullptr;
+    int *err = nullptr;
+    cudaStream_t s = nullptr;
+    e = cudaMalloc(&G, sizeof(float2) * r3);
+    if (e == cudaSuccess) e = cudaMalloc(&F2, sizeof(float2) * r3);
+    if (e == cudaSuccess && check_mode) e = cudaMalloc(&mask, r3);
+    if (e == cudaSuccess) e = cudaMalloc(&err, sizeof(int));
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMemsetAsync(G, 0, sizeof(float2) * r3, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(F2, 0, sizeof(float2) * r3, s);
+    if (e == cudaSuccess && mask) e = cudaMemsetAsync(mask, 0, r3, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(err, 0, sizeof(int), s);
+    PlanChoice pc;
+    if (e == cudaSuccess) {
+        LoopArgs a = {};
+        a.G = G;
+        a.F2 = F2;
+        a.mask = mask;
+        a.out = F2;   // the final x pass is not timed
+        a.R = R;
+        const double k2 = 1.0e14, nm = 1.337;
+        a.inv_n3 = (float)(1.0 / (double)r3);
+        a.k2 = (float)k2;
+        a.n_med = (float)nm;
+        a.n_med2 = (float)(nm * nm);
+        a.s1 = (float)(-1.0 / ((double)r3 * k2));
+        a.s2 = (float)(-k2 / (nm * nm));
+        a.err = err;
+        const int kinds[3] = {LOOP_X, LOOP_Y_FWD, LOOP_Z};
+        for (int p = 0; p < 3 && e == cudaSuccess; p++) {
+            double best = 1e30;
+            for (int v = 0; v < nv && e == cudaSuccess; v++) {
+                double ms = 0;
+                e = time_variant(kinds[p], v, a, check_mode, s, 5, ms);
+                if (ms_out && p * 3 + v < n_ms) ms_out[p * 3 + v] = ms;
+                if (e == cudaSuccess && ms < best) {
+                    best = ms;
+                    pc.v[p] = v;
+                }
+            }
+        }
+        pc.tuned = e == cudaSuccess;
+    }
+    if (s) {
+        cudaStreamSynchronize(s);
+        cudaStreamDestroy(s);
+    }
+    cudaFree(G);
+    cudaFree(F2);
+    cudaFree(mask);
+    cudaFree(err);
+    if (e != cudaSuccess) return e;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_choice[{dev, R}] = pc;
+    }
+    if (chosen)
+        for (int p = 0; p < 3; p++) chosen[p] = pc.v[p];
+    return cudaSuccess;
+}
+
+// Tunes R on first use on this device (see the file comment).
+cudaError_t ensure_tuned(int R, int check_mode, cudaStream_t s)
+{
+    const char *env = std::getenv("CTDM_AUTOTUNE");
+    if (env && std::strcmp(env, "0") == 0) return cudaSuccess;
+    if (loop_plan_count(R) <= 1) return cudaSuccess;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_choice.find({dev, R});
+        if (it != g_choice.end()) return cudaSuccess;   // tuned or pinned
+    }
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    e = cudaStreamIsCapturing(s, &cs);
+    if (e != cudaSuccess || cs != cudaStreamCaptureStatusNone) return cudaSuccess;
+    return autotune_loop(R, check_mode, nullptr, nullptr, 0);
+}
+
+}  // namespace ctdm
+
+using namespace ctdm;
+
+extern "C" int ctdm_plan_count(int R) { return loop_plan_count(R); }
+
+extern "C" ctdm_status ctdm_autotune(int device, int R, int check_mode, int *variants3, double *ms, int n_ms)
+{
+    if (loop_plan_count(R) == 0) return fail_invalid("ctdm_autotune: unsupported volume side");
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return fail_cuda(e, "cudaSetDevice");
+    e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = autotune_loop(R, check_mode != 0, variants3, ms, n_ms);
+    if (e != cudaSuccess) return fail_cuda(e, "autotune");
+    clear_error();
+    return CTDM_OK;
+}
+
+extern "C" ctdm_status ctdm_plans(int device, int R, int *variants3, int *tuned)
+{
+    if (!variants3 || loop_plan_count(R) == 0) return fail_invalid("ctdm_plans: bad argument");
+    PlanChoice pc;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_choice.find({device, R});
+        if (it != g_choice.end()) pc = it->second;
+    }
+    for (int p = 0; p < 3; p++) variants3[p] = pc.v[p];
+    if (tuned) *tuned = pc.tuned ? 1 : 0;
+    clear_error();
+    return CTDM_OK;
+}
+
+extern "C" ctdm_status ctdm_set_plans(int device, int R, const int *variants3)
+{
+    const int nv = loop_plan_count(R);
+    if (!variants3 || nv == 0) return fail_invalid("ctdm_set_plans: bad argument");
+    for (int p = 0; p < 3; p++)
+        if (variants3[p] < 0 || variants3[p] >= nv) return fail_invalid("ctdm_set_plans: variant out of range");
+    PlanChoice pc;
+    for (int p = 0; p < 3; p++) pc.v[p] = variants3[p];
+    pc.tuned = false;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_choice[{device, R}] = pc;
+    clear_error();
+    return CTDM_OK;
+}

@@ -151,6 +151,21 @@ CTDM_API ctdm_status ctdm_batch_run_eager(ctdm_batch *batch, void *stream);
 /* Lane each job was assigned to (longest job first onto the least-loaded lane). */
 CTDM_API ctdm_status ctdm_batch_lanes(const ctdm_batch *batch, int *lane_of_job, int n_jobs);
 
+/* --- autotuner of the positivity-loop passes (no reference counterpart) -------------
+ * Each volume side has ctdm_plan_count(R) FFT plan variants (lines per CTA, threads per
+ * line, radix sequence) for each of the x, y and z passes.  The first reconstruction
+ * of a side on a device times them all on scratch volumes and keeps the fastest per
+ * pass (the call synchronises the device once; set CTDM_AUTOTUNE=0 to keep variant 0).
+ * Variants differ in rounding at the float32 ulp level only. */
+CTDM_API int ctdm_plan_count(int R);
+/* Tune now: variants3 (may be NULL) receives the x, y, z choice; ms (may be NULL)
+ * receives the median time of pass p, variant v at ms[3 * p + v] (n_ms entries). */
+CTDM_API ctdm_status ctdm_autotune(int device, int R, int check_mode, int *variants3, double *ms, int n_ms);
+/* Current choice for (device, R); tuned = 1 when it came from the autotuner. */
+CTDM_API ctdm_status ctdm_plans(int device, int R, int *variants3, int *tuned);
+/* Pin a choice (also disables tuning of that side on that device). */
+CTDM_API ctdm_status ctdm_set_plans(int device, int R, const int *variants3);
+
 /* --- stages (device pointers) --- */
 /* QPI Algorithm A.  carrier3: in {row, col, radius} (any < 0: detect from the first
  * background), out: the carrier used. */

@@ -60,3 +60,15 @@ def test_version_and_error_without_gpu(lib):
     p.n_holo = 100
     rc = L.ctdm_reconstruct_device(ctypes.c_void_p(1), ctypes.byref(p), 4, 1, 1, 1, 1, 1, None)
     assert rc == 1 and b"unsupported" in L.ctdm_last_error()
+
+
+def test_plan_table_without_gpu(lib):
+    """Plan counts and the pinning checks need no GPU."""
+    from ctdm_gb300 import _lib
+    import ctdm_gb300 as C
+    _lib.load()
+    assert C.plan_count(256) == 3 and C.plan_count(64) == 1 and C.plan_count(100) == 0
+    C.set_plans(512, (1, 2, 0), device=3)
+    assert C.plans(512, device=3) == ((1, 2, 0), False)
+    with pytest.raises(C.CtdmError):
+        C.set_plans(512, (0, 3, 0), device=3)
