@@ -86,6 +86,8 @@ _SIGS = {
     "ctdm_autotune": (c_int, [c_int, c_int, c_int, P_int, ctypes.POINTER(c_double), c_int]),
     "ctdm_plans": (c_int, [c_int, c_int, P_int, P_int]),
     "ctdm_set_plans": (c_int, [c_int, c_int, P_int]),
+    "ctdm_loop_scheme": (c_int, [c_int, c_int, P_int]),
+    "ctdm_set_loop_scheme": (c_int, [c_int, c_int, c_int]),
     "ctdm_set_recon_globals": (None, [c_int, c_double, c_double, c_double, c_double, c_int, c_int, ctypes.c_char_p]),
     "DCT_UWLS_Unwrapped": (None, [c_void_p, c_void_p, c_int, c_int]),
     "FastUnwrapping": (None, [c_void_p, c_void_p, c_int, c_int]),

@@ -501,6 +501,18 @@ static ctdm_status do_positivity(ctdm_ctx *c, int R, int iters, int check_mode, 
     la.err = c->d_err;
     CK(ensure_tuned(R, check_mode, s), "autotune loop passes");
     StageTimer &tm = c->timer;
+    if (loop_scheme(R) == 1) {
+        // plane + z passes (the plane pass records under the x-pass stage)
+        for (int it = 0; it < iters; it++) {
+            CK(launch_plane(la, false, s), "plane pass");
+            tm.mark(S_XPASS, s);
+            CK(launch_zpass(la, check_mode, s), "z pass");
+            tm.mark(S_ZPASS, s);
+        }
+        CK(launch_plane(la, true, s), "final plane pass");
+        tm.mark(S_XFINAL, s);
+        return CTDM_OK;
+    }
     CK(launch_ypass(la, true, s), "y inverse pass");
     tm.mark(S_YINV, s);
     for (int it = 0; it < iters; it++) {

@@ -72,6 +72,17 @@ int loop_plan_count(int R);
 cudaError_t loop_pass_variant(int kind, int variant, const LoopArgs &a, int flag, cudaStream_t s);
 // Autotuner (tune.cu): tunes volume side R on this device on first use.
 cudaError_t ensure_tuned(int R, int check_mode, cudaStream_t s);
+// (kernel, device) pairs whose launch attributes have been set.
+bool kernel_configured(const void *fn, int dev);
+void mark_kernel_configured(const void *fn, int dev);
+
+// Plane pass (plane_pass.cuh): x and y transforms of whole planes in thread-block
+// clusters; sides without one return cudaErrorNotSupported / 0 clusters.
+cudaError_t plane_pass_256(const LoopArgs &a, bool final_pass, cudaStream_t s);
+int plane_clusters_256();
+// Loop scheme of side R on this device: 0 = x / y / z / y passes, 1 = plane + z passes.
+int loop_scheme(int R);
+cudaError_t launch_plane(const LoopArgs &a, bool final_pass, cudaStream_t s);
 
 // Generic batched transforms.  rows: nlines contiguous lines of length L.
 // cols: lines of length L with element p at (l % nx) + (l / nx) * plane + p * ld.

@@ -20,9 +20,7 @@
 namespace ctdm {
 
 // Large dynamic shared memory opt-in and the largest carveout, once per kernel and
-// device (the set of configured (kernel, device) pairs is shared by all sizes).
-bool kernel_configured(const void *fn, int dev);
-void mark_kernel_configured(const void *fn, int dev);
+// device (kernel_configured / mark_kernel_configured keep the set of configured pairs).
 
 template <class K>
 static cudaError_t prep_plan_kernel(K kernel, int L, size_t smem)

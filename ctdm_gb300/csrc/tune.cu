@@ -23,6 +23,7 @@ namespace ctdm {
 
 struct PlanChoice {
     int v[3] = {0, 0, 0};   // x, y, z pass
+    int scheme = -1;        // -1 default, 0 x / y / z / y passes, 1 plane + z passes
     bool tuned = false;
 };
 static std::mutex g_tune_mu;
@@ -71,6 +72,37 @@ static PlanChoice choice_of(int R)
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_choice.find({dev, R});
     return it == g_choice.end() ? PlanChoice() : it->second;
+}
+
+static std::map<std::pair<int, int>, int> g_plane_ok;   // (device, R) -> clusters resident
+
+static bool plane_available(int R)
+{
+    if (R != 256) return false;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_plane_ok.find({dev, R});
+        if (it != g_plane_ok.end()) return it->second > 0;
+    }
+    const int n = plane_clusters_256();
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_plane_ok[{dev, R}] = n;
+    return n > 0;
+}
+
+int loop_scheme(int R)
+{
+    const PlanChoice pc = choice_of(R);
+    if (pc.scheme >= 0) return pc.scheme == 1 && plane_available(R) ? 1 : 0;
+    return plane_available(R) ? 1 : 0;
+}
+
+cudaError_t launch_plane(const LoopArgs &a, bool final_pass, cudaStream_t s)
+{
+    if (a.R == 256) return plane_pass_256(a, final_pass, s);
+    return cudaErrorNotSupported;
 }
 
 cudaError_t launch_xpass(const LoopArgs &a, bool final_pass, cudaStream_t s)
@@ -168,6 +200,37 @@ cudaError_t autotune_loop(int R, int check_mode, int *chosen, double *ms_out, in
                 }
             }
         }
+        // loop scheme: one iteration of x / y / z / y against plane + z
+        if (e == cudaSuccess && plane_available(R)) {
+            cudaEvent_t e0, e1;
+            e = cudaEventCreate(&e0);
+            if (e == cudaSuccess) e = cudaEventCreate(&e1);
+            double t4 = 1e30, t2 = 1e30;
+            for (int rep = 0; rep < 4 && e == cudaSuccess; rep++) {
+                float d = 0.f;
+                cudaEventRecord(e0, s);
+                e = loop_pass_variant(LOOP_X, pc.v[0], a, 0, s);
+                if (e == cudaSuccess) e = loop_pass_variant(LOOP_Y_FWD, pc.v[1], a, 0, s);
+                if (e == cudaSuccess) e = loop_pass_variant(LOOP_Z, pc.v[2], a, check_mode, s);
+                if (e == cudaSuccess) e = loop_pass_variant(LOOP_Y_INV, pc.v[1], a, 0, s);
+                cudaEventRecord(e1, s);
+                if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+                if (e == cudaSuccess) e = cudaEventElapsedTime(&d, e0, e1);
+                if (rep > 0) t4 = std::min(t4, (double)d);
+                cudaEventRecord(e0, s);
+                if (e == cudaSuccess) e = launch_plane(a, false, s);
+                if (e == cudaSuccess) e = loop_pass_variant(LOOP_Z, pc.v[2], a, check_mode, s);
+                cudaEventRecord(e1, s);
+                if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+                if (e == cudaSuccess) e = cudaEventElapsedTime(&d, e0, e1);
+                if (rep > 0) t2 = std::min(t2, (double)d);
+            }
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            pc.scheme = t2 < t4 ? 1 : 0;
+            if (ms_out && 9 < n_ms) ms_out[9] = t4;
+            if (ms_out && 10 < n_ms) ms_out[10] = t2;
+        }
         pc.tuned = e == cudaSuccess;
     }
     if (s) {
@@ -247,11 +310,29 @@ extern "C" ctdm_status ctdm_set_plans(int device, int R, const int *variants3)
     if (!variants3 || nv == 0) return fail_invalid("ctdm_set_plans: bad argument");
     for (int p = 0; p < 3; p++)
         if (variants3[p] < 0 || variants3[p] >= nv) return fail_invalid("ctdm_set_plans: variant out of range");
-    PlanChoice pc;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    PlanChoice &pc = g_choice[{device, R}];
     for (int p = 0; p < 3; p++) pc.v[p] = variants3[p];
     pc.tuned = false;
+    clear_error();
+    return CTDM_OK;
+}
+
+extern "C" ctdm_status ctdm_loop_scheme(int device, int R, int *scheme)
+{
+    if (!scheme || loop_plan_count(R) == 0) return fail_invalid("ctdm_loop_scheme: bad argument");
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return fail_cuda(e, "cudaSetDevice");
+    *scheme = loop_scheme(R);
+    clear_error();
+    return CTDM_OK;
+}
+
+extern "C" ctdm_status ctdm_set_loop_scheme(int device, int R, int scheme)
+{
+    if (loop_plan_count(R) == 0 || scheme < 0 || scheme > 1) return fail_invalid("ctdm_set_loop_scheme: bad argument");
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    g_choice[{device, R}] = pc;
+    g_choice[{device, R}].scheme = scheme;
     clear_error();
     return CTDM_OK;
 }

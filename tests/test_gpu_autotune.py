@@ -55,3 +55,50 @@ def test_autotune_reports_all_variants(ctx):
         assert ms[(p, chosen[p])] == min(times)
     got, tuned = C.plans(r)
     assert got == chosen and tuned
+
+
+def test_loop_schemes_agree_at_256(ctx, dev, oracle):
+    """The plane + z scheme (cluster plane pass) and the x / y / z / y scheme give the
+    oracle's volume at 256^3, with and without the hit-mask predicate."""
+    import ctdm_gb300 as C
+    import torch
+    r, iters = 256, 3
+    f2 = synthetic_f2(r, seed=7)
+    counts = ((f2.real != 0) & (f2.imag != 0)).astype(np.uint32)
+    d_f2 = torch.from_numpy(f2).to(dev)
+    d_counts = torch.from_numpy(counts.view(np.int32)).to(dev)
+    out = torch.empty_like(d_f2)
+    saved = C.loop_scheme(r)
+    try:
+        for mode in (0, 1):
+            ref = oracle.positivity(f2, counts, iters, K2, N_MED, mode)
+            for scheme in (0, 1):
+                C.set_loop_scheme(r, scheme)
+                ctx.positivity(d_f2, r, iters, K2, N_MED, out, check_mode=mode, counts=d_counts)
+                torch.cuda.synchronize()
+                g = out.cpu().numpy().astype(np.complex128)
+                err = float(np.sqrt(np.mean(np.abs(g - ref) ** 2)))
+                assert err < RI_TOL, (mode, scheme, err)
+                assert ctx.device_status() == 0
+    finally:
+        C.set_loop_scheme(r, saved)
+
+
+def test_pipeline_full_size_plain(ctx, dev, oracle):
+    """The plain-method workload at its full size (49 x 256^2 holograms -> 256^3,
+    10 iterations) against the FP64 oracle."""
+    import ctdm_gb300 as C
+    import torch
+    from ctdm_gb300 import phantom
+    acq = phantom.config_plain_small(seed=1000)
+    iters = 10
+    p = C.params_for(acq, iters)
+    out = torch.empty((acq.r_vol,) * 3, dtype=torch.complex64, device=dev)
+    ctx.reconstruct_device(p, torch.from_numpy(acq.holograms).to(dev), torch.from_numpy(acq.background).to(dev),
+                           acq.ang_x, acq.ang_y, out)
+    torch.cuda.synchronize()
+    par = oracle.make_params(acq.n_holo, acq.m_crop, acq.r_vol, iters, acq.fm0, acq.df, acq.dx, acq.k2, acq.n_med)
+    ref, car = oracle.pipeline(par, acq.holograms, acq.background, acq.ang_x, acq.ang_y)
+    assert ctx.carrier() == car
+    err = float(np.sqrt(np.mean(np.abs(out.cpu().numpy().astype(np.complex128) - ref) ** 2)))
+    assert err < RI_TOL, err
