@@ -203,20 +203,21 @@ def plan_count(r):
 
 def autotune(r, check_mode=CTDM_CHECK_REF, device=0):
     """Tune the loop passes for side r now: (variants (x, y, z), {(pass, variant): ms}).
-    Where a plane pass exists, the dict also holds ("scheme", 0) and ("scheme", 1): one
+    Where a plane pass exists, the dict also holds ("scheme", s) for s = 0, 1, 2: one
     iteration of each loop scheme."""
     v = (ctypes.c_int * 3)()
-    ms = (ctypes.c_double * 11)(*([float("nan")] * 11))
-    check(load().ctdm_autotune(int(device), int(r), int(check_mode), v, ms, 11), "ctdm_autotune")
+    ms = (ctypes.c_double * 12)(*([float("nan")] * 12))
+    check(load().ctdm_autotune(int(device), int(r), int(check_mode), v, ms, 12), "ctdm_autotune")
     n = plan_count(r)
     out = {(p, k): ms[3 * p + k] for p in range(3) for k in range(n)}
-    if ms[9] == ms[9]:
-        out[("scheme", 0)], out[("scheme", 1)] = ms[9], ms[10]
+    for sc in range(3):
+        if ms[9 + sc] == ms[9 + sc]:
+            out[("scheme", sc)] = ms[9 + sc]
     return tuple(v), out
 
 
 def loop_scheme(r, device=0):
-    """0: x / y / z / y line passes; 1: plane + z passes."""
+    """0: x / y / z / y line passes; 1, 2: plane + z passes (two plane-pass variants)."""
     s = ctypes.c_int()
     check(load().ctdm_loop_scheme(int(device), int(r), ctypes.byref(s)), "ctdm_loop_scheme")
     return s.value

@@ -6,9 +6,9 @@
 CTDM_LOOP_SIZE_3(256)
 
 namespace ctdm {
-cudaError_t plane_pass_256(const LoopArgs &a, bool final_pass, cudaStream_t s)
+cudaError_t plane_pass_256(const LoopArgs &a, bool final_pass, int variant, cudaStream_t s)
 {
-    return run_plane_pass<256, 8>(a, final_pass, s);
+    return variant == 2 ? run_plane_pass<256, 8, 4>(a, final_pass, s) : run_plane_pass<256, 8, 3>(a, final_pass, s);
 }
-int plane_clusters_256() { return plane_pass_clusters<256, 8>(); }
+int plane_clusters_256() { return plane_pass_clusters<256, 8, 3>(); }
 }  // namespace ctdm

@@ -240,7 +240,8 @@ __global__ void __launch_bounds__(Plan<L>::THREADS) ewald_kernel(EwaldArgs a, co
     extern __shared__ float4 smem4[];
     float2 *buf = reinterpret_cast<float2 *>(smem4);
     uint32_t *cnt = reinterpret_cast<uint32_t *>(buf + P::B * P::LP);
-    AngleGeom *geo = reinterpret_cast<AngleGeom *>(cnt + P::B * L);
+    float2 *stage = reinterpret_cast<float2 *>(cnt + P::B * L);              // 32 values per warp
+    AngleGeom *geo = reinterpret_cast<AngleGeom *>(stage + P::THREADS);
     const long line0 = (long)blockIdx.x * P::B;   // line = x + R*y, B consecutive x
     for (int e = threadIdx.x; e < P::B * P::LP; e += P::THREADS) buf[e] = make_float2(0.f, 0.f);
     for (int e = threadIdx.x; e < P::B * L; e += P::THREADS) cnt[e] = 0u;
@@ -270,18 +271,23 @@ __global__ void __launch_bounds__(Plan<L>::THREADS) ewald_kernel(EwaldArgs a, co
                     val = make_float2(-fz * four_pi * u.y, fz * four_pi * u.x);
                 }
             }
-            // angle order per voxel: lanes are applied one after another
-            unsigned pending = __ballot_sync(0xffffffffu, nz >= 0);
-            while (pending) {
-                const int q = __ffs(pending) - 1;
-                if (lane == q) {
-                    float2 c = col[nz];
-                    col[nz] = make_float2(c.x + val.x, c.y + val.y);
-                    ccol[nz] += 1u;
+            // angle order per voxel: lanes hitting the same voxel form a group whose
+            // lowest lane adds the members' values in lane (= angle) order, the same
+            // sequence of float additions as applying the lanes one after another
+            if (__ballot_sync(0xffffffffu, nz >= 0) == 0u) continue;
+            const unsigned grp = __match_any_sync(0xffffffffu, nz);
+            stage[warp * 32 + lane] = val;
+            __syncwarp();
+            if (nz >= 0 && (__ffs(grp) - 1) == lane) {
+                float2 c = col[nz];
+                for (unsigned m = grp; m; m &= m - 1) {
+                    const float2 w = stage[warp * 32 + __ffs(m) - 1];
+                    c = make_float2(c.x + w.x, c.y + w.y);
                 }
-                __syncwarp();
-                pending &= pending - 1;
+                col[nz] = c;
+                ccol[nz] += (uint32_t)__popc(grp);
             }
+            __syncwarp();
         }
     }
     __syncthreads();
@@ -317,7 +323,8 @@ template <int L>
 static cudaError_t ewald_launch(const EwaldArgs &a, cudaStream_t s)
 {
     using P = Plan<L>;
-    const size_t smem = fftl::smem_bytes<L>() + sizeof(uint32_t) * P::B * L + sizeof(AngleGeom) * a.A;
+    const size_t smem = fftl::smem_bytes<L>() + sizeof(uint32_t) * P::B * L + sizeof(float2) * P::THREADS +
+                        sizeof(AngleGeom) * a.A;
     auto k = ewald_kernel<L>;
     cudaError_t e = prep_launch<L>(k, smem);
     if (e != cudaSuccess) return e;

@@ -78,9 +78,10 @@ void mark_kernel_configured(const void *fn, int dev);
 
 // Plane pass (plane_pass.cuh): x and y transforms of whole planes in thread-block
 // clusters; sides without one return cudaErrorNotSupported / 0 clusters.
-cudaError_t plane_pass_256(const LoopArgs &a, bool final_pass, cudaStream_t s);
+cudaError_t plane_pass_256(const LoopArgs &a, bool final_pass, int variant, cudaStream_t s);
 int plane_clusters_256();
-// Loop scheme of side R on this device: 0 = x / y / z / y passes, 1 = plane + z passes.
+// Loop scheme of side R on this device: 0 = x / y / z / y passes, 1 and 2 = plane + z
+// passes (plane pass register targets of 3 and 4 CTAs per SM).
 int loop_scheme(int R);
 cudaError_t launch_plane(const LoopArgs &a, bool final_pass, cudaStream_t s);
 

@@ -34,8 +34,10 @@ struct PlaneCfg {
     static_assert(RL % P::B == 0, "rows per CTA must be a multiple of the plan's lines per CTA");
 };
 
-template <int L, int C, bool FINAL>
-__global__ void __launch_bounds__(fftl::Plan<L>::THREADS, 3) plane_kernel(LoopArgs a, const float2 *__restrict__ tw)
+// MINB: resident CTAs per SM the register allocation aims for (3: no spills at
+// R = 256; 4: more latency hiding for some spill traffic; the autotuner picks).
+template <int L, int C, int MINB, bool FINAL>
+__global__ void __launch_bounds__(fftl::Plan<L>::THREADS, MINB) plane_kernel(LoopArgs a, const float2 *__restrict__ tw)
 {
     namespace cg = cooperative_groups;
     using Cfg = PlaneCfg<L, C>;
@@ -113,11 +115,11 @@ __global__ void __launch_bounds__(fftl::Plan<L>::THREADS, 3) plane_kernel(LoopAr
 }
 
 // Launches the plane pass of side L with C-CTA clusters over all L planes.
-template <int L, int C>
+template <int L, int C, int MINB>
 static cudaError_t run_plane_pass(const LoopArgs &a, bool final_pass, cudaStream_t s)
 {
     using Cfg = PlaneCfg<L, C>;
-    auto k = final_pass ? plane_kernel<L, C, true> : plane_kernel<L, C, false>;
+    auto k = final_pass ? plane_kernel<L, C, MINB, true> : plane_kernel<L, C, MINB, false>;
     if (!twiddles(L)) return cudaErrorInitializationError;
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -148,11 +150,11 @@ static cudaError_t run_plane_pass(const LoopArgs &a, bool final_pass, cudaStream
 }
 
 // Number of clusters of the plane pass that fit on the device at once (0: none).
-template <int L, int C>
+template <int L, int C, int MINB>
 static int plane_pass_clusters()
 {
     using Cfg = PlaneCfg<L, C>;
-    auto k = plane_kernel<L, C, false>;
+    auto k = plane_kernel<L, C, MINB, false>;
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM) != cudaSuccess) return 0;
     if (C > 8 && cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) return 0;
     cudaLaunchConfig_t cfg = {};

@@ -23,7 +23,7 @@ namespace ctdm {
 
 struct PlanChoice {
     int v[3] = {0, 0, 0};   // x, y, z pass
-    int scheme = -1;        // -1 default, 0 x / y / z / y passes, 1 plane + z passes
+    int scheme = -1;        // -1 default, 0 x / y / z / y passes, 1 / 2 plane + z passes
     bool tuned = false;
 };
 static std::mutex g_tune_mu;
@@ -95,14 +95,19 @@ static bool plane_available(int R)
 int loop_scheme(int R)
 {
     const PlanChoice pc = choice_of(R);
-    if (pc.scheme >= 0) return pc.scheme == 1 && plane_available(R) ? 1 : 0;
+    if (pc.scheme >= 0) return pc.scheme >= 1 && plane_available(R) ? pc.scheme : 0;
     return plane_available(R) ? 1 : 0;
+}
+
+static cudaError_t plane_variant(const LoopArgs &a, bool final_pass, int scheme, cudaStream_t s)
+{
+    if (a.R == 256) return plane_pass_256(a, final_pass, scheme, s);
+    return cudaErrorNotSupported;
 }
 
 cudaError_t launch_plane(const LoopArgs &a, bool final_pass, cudaStream_t s)
 {
-    if (a.R == 256) return plane_pass_256(a, final_pass, s);
-    return cudaErrorNotSupported;
+    return plane_variant(a, final_pass, loop_scheme(a.R), s);
 }
 
 cudaError_t launch_xpass(const LoopArgs &a, bool final_pass, cudaStream_t s)
@@ -200,36 +205,36 @@ cudaError_t autotune_loop(int R, int check_mode, int *chosen, double *ms_out, in
                 }
             }
         }
-        // loop scheme: one iteration of x / y / z / y against plane + z
+        // loop scheme: one iteration of x / y / z / y against plane + z (both plane variants)
         if (e == cudaSuccess && plane_available(R)) {
             cudaEvent_t e0, e1;
             e = cudaEventCreate(&e0);
             if (e == cudaSuccess) e = cudaEventCreate(&e1);
-            double t4 = 1e30, t2 = 1e30;
+            double best[3] = {1e30, 1e30, 1e30};
             for (int rep = 0; rep < 4 && e == cudaSuccess; rep++) {
-                float d = 0.f;
-                cudaEventRecord(e0, s);
-                e = loop_pass_variant(LOOP_X, pc.v[0], a, 0, s);
-                if (e == cudaSuccess) e = loop_pass_variant(LOOP_Y_FWD, pc.v[1], a, 0, s);
-                if (e == cudaSuccess) e = loop_pass_variant(LOOP_Z, pc.v[2], a, check_mode, s);
-                if (e == cudaSuccess) e = loop_pass_variant(LOOP_Y_INV, pc.v[1], a, 0, s);
-                cudaEventRecord(e1, s);
-                if (e == cudaSuccess) e = cudaEventSynchronize(e1);
-                if (e == cudaSuccess) e = cudaEventElapsedTime(&d, e0, e1);
-                if (rep > 0) t4 = std::min(t4, (double)d);
-                cudaEventRecord(e0, s);
-                if (e == cudaSuccess) e = launch_plane(a, false, s);
-                if (e == cudaSuccess) e = loop_pass_variant(LOOP_Z, pc.v[2], a, check_mode, s);
-                cudaEventRecord(e1, s);
-                if (e == cudaSuccess) e = cudaEventSynchronize(e1);
-                if (e == cudaSuccess) e = cudaEventElapsedTime(&d, e0, e1);
-                if (rep > 0) t2 = std::min(t2, (double)d);
+                for (int sc = 0; sc < 3 && e == cudaSuccess; sc++) {
+                    float d = 0.f;
+                    cudaEventRecord(e0, s);
+                    if (sc == 0) {
+                        e = loop_pass_variant(LOOP_X, pc.v[0], a, 0, s);
+                        if (e == cudaSuccess) e = loop_pass_variant(LOOP_Y_FWD, pc.v[1], a, 0, s);
+                        if (e == cudaSuccess) e = loop_pass_variant(LOOP_Z, pc.v[2], a, check_mode, s);
+                        if (e == cudaSuccess) e = loop_pass_variant(LOOP_Y_INV, pc.v[1], a, 0, s);
+                    } else {
+                        e = plane_variant(a, false, sc, s);
+                        if (e == cudaSuccess) e = loop_pass_variant(LOOP_Z, pc.v[2], a, check_mode, s);
+                    }
+                    cudaEventRecord(e1, s);
+                    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+                    if (e == cudaSuccess) e = cudaEventElapsedTime(&d, e0, e1);
+                    if (rep > 0) best[sc] = std::min(best[sc], (double)d);
+                }
             }
             cudaEventDestroy(e0);
             cudaEventDestroy(e1);
-            pc.scheme = t2 < t4 ? 1 : 0;
-            if (ms_out && 9 < n_ms) ms_out[9] = t4;
-            if (ms_out && 10 < n_ms) ms_out[10] = t2;
+            pc.scheme = (int)(std::min_element(best, best + 3) - best);
+            for (int sc = 0; sc < 3; sc++)
+                if (ms_out && 9 + sc < n_ms) ms_out[9 + sc] = best[sc];
         }
         pc.tuned = e == cudaSuccess;
     }
@@ -330,7 +335,7 @@ extern "C" ctdm_status ctdm_loop_scheme(int device, int R, int *scheme)
 
 extern "C" ctdm_status ctdm_set_loop_scheme(int device, int R, int scheme)
 {
-    if (loop_plan_count(R) == 0 || scheme < 0 || scheme > 1) return fail_invalid("ctdm_set_loop_scheme: bad argument");
+    if (loop_plan_count(R) == 0 || scheme < 0 || scheme > 2) return fail_invalid("ctdm_set_loop_scheme: bad argument");
     std::lock_guard<std::mutex> lk(g_tune_mu);
     g_choice[{device, R}].scheme = scheme;
     clear_error();

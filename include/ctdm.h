@@ -165,12 +165,13 @@ CTDM_API ctdm_status ctdm_autotune(int device, int R, int check_mode, int *varia
 CTDM_API ctdm_status ctdm_plans(int device, int R, int *variants3, int *tuned);
 /* Pin a choice (also disables tuning of that side on that device). */
 CTDM_API ctdm_status ctdm_set_plans(int device, int R, const int *variants3);
-/* Loop scheme of side R: 0 = x / y / z / y line passes (72 R^3 bytes per iteration),
- * 1 = plane pass (x and y transforms of whole planes by 8-CTA thread-block clusters,
- * each plane kept in L2 between its row and column phases) + z pass (40 R^3 bytes).  Scheme 1 exists for
- * R = 256 and is the default where the device can co-schedule its clusters; the
- * autotuner keeps the faster.  ctdm_autotune's ms[9], ms[10] (when n_ms > 10) receive
- * one iteration of scheme 0 and of scheme 1. */
+/* Loop scheme of side R: 0 = x / y / z / y line passes (72 R^3 bytes per iteration);
+ * 1, 2 = plane pass (x and y transforms of whole planes by 8-CTA thread-block clusters,
+ * each plane kept in L2 between its row and column phases; register targets of 3 and
+ * 4 CTAs per SM) + z pass (40 R^3 bytes).  The plane schemes exist for R = 256; scheme 1
+ * is the default where the device can co-schedule the clusters, and the autotuner
+ * keeps the fastest.  ctdm_autotune's ms[9..11] (when n_ms > 11) receive one
+ * iteration of schemes 0, 1 and 2. */
 CTDM_API ctdm_status ctdm_loop_scheme(int device, int R, int *scheme);
 CTDM_API ctdm_status ctdm_set_loop_scheme(int device, int R, int scheme);
 

@@ -72,7 +72,7 @@ def test_loop_schemes_agree_at_256(ctx, dev, oracle):
     try:
         for mode in (0, 1):
             ref = oracle.positivity(f2, counts, iters, K2, N_MED, mode)
-            for scheme in (0, 1):
+            for scheme in (0, 1, 2):
                 C.set_loop_scheme(r, scheme)
                 ctx.positivity(d_f2, r, iters, K2, N_MED, out, check_mode=mode, counts=d_counts)
                 torch.cuda.synchronize()
