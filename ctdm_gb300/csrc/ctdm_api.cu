@@ -288,7 +288,12 @@ extern "C" ctdm_status ctdm_ctx_create(int device, ctdm_ctx **out)
     CK(ensure_tables(), "building twiddle tables");
     ctdm_ctx *c = new ctdm_ctx();
     c->device = device;
-    cudaError_t e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
+    // the side stream carries work the reconstruction does not wait for (Goldstein
+    // beside the DCT path): lowest priority, so the block scheduler serves the
+    // call's stream first
+    int prio_lo = 0, prio_hi = 0;
+    cudaError_t e = cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, prio_lo);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_err, sizeof(int));

@@ -209,7 +209,7 @@ cudaError_t goldstein_cuts(const int8_t *charges, int A, int W, int H, uint8_t *
 enum : unsigned {
     F_CUT = 1u, F_UB = 2u, F_PREV = 4u, F_LIST = 8u, F_NEW = 16u, F_CAND = 32u, F_READY = 64u, F_MARK = 128u
 };
-constexpr int FF_THREADS = 512;
+constexpr int FF_THREADS = 256;
 
 __device__ __forceinline__ unsigned byte_or(uint8_t *p, unsigned bits)
 {

@@ -88,33 +88,48 @@ cudaError_t qpi_find_carrier(const float *bg, int N, float2 *scratch, unsigned l
 // holo: A holograms N x N (float, [a][y][x]); T1: A x N x M complex ([a][y][m]).
 // Column m of the window is spectrum column k = (c - N/2 + m - M/2) mod N of the
 // unshifted transform (the quadrant swap folded into the index).
+//
+// Row mapping (threads along the row pair, 16-point register tiles): every thread
+// loads its first-stage points of the two packed rows straight from HBM (unit
+// stride across the warp), the transform ends in registers, and the spectrum is
+// parked in shared memory only for the symmetric window extraction.
 template <int N>
-__global__ void __launch_bounds__(Plan<N>::THREADS) qpi_rows_kernel(const float *__restrict__ holo, float2 *T1,
-                                                                   const int *__restrict__ carrier, long npairs,
-                                                                   int M, const float2 *__restrict__ tw)
+struct QRows : fftl::Plan<N> {};
+template <> struct QRows<512> : fftl::PlanT<512, 8, 32, fftl::Radices<8, 8, 8>, fftl::Radices<8, 8, 8>> {};
+template <> struct QRows<1024> : fftl::PlanT<1024, 4, 64, fftl::Radices<16, 16, 4>, fftl::Radices<4, 16, 16>> {};
+template <> struct QRows<2048> : fftl::PlanT<2048, 2, 128, fftl::Radices<16, 16, 8>, fftl::Radices<8, 16, 16>> {};
+
+template <int N>
+__global__ void __launch_bounds__(QRows<N>::THREADS) qpi_rows_kernel(const float *__restrict__ holo, float2 *T1,
+                                                                    const int *__restrict__ carrier, long npairs,
+                                                                    int M, const float2 *__restrict__ tw)
 {
-    using P = Plan<N>;
+    using P = QRows<N>;
+    using Y = fftl::Lay<N, P::LP, true>;
     extern __shared__ float4 smem4[];
     float2 *buf = reinterpret_cast<float2 *>(smem4);
-    const long pair0 = (long)blockIdx.x * P::B;   // pair q covers rows 2q, 2q+1 of the stack
-    for (int e = threadIdx.x; e < P::B * N; e += P::THREADS) {
-        const int b = e / N, p = e - b * N;
-        const long q = pair0 + b;
-        float2 v = make_float2(0.f, 0.f);
-        if (q < npairs) v = make_float2(__ldcs(&holo[(2 * q) * N + p]), __ldcs(&holo[(2 * q + 1) * N + p]));
-        buf[b * P::LP + p] = v;
+    const int t = threadIdx.x % P::T, b = threadIdx.x / P::T;
+    const long q = (long)blockIdx.x * P::B + b;   // pair q covers rows 2q, 2q+1 of the stack
+    const bool ok = q < npairs;
+    const float *r0 = holo + (ok ? 2 * q : 0) * N;
+    float2 v[P::E];
+#pragma unroll
+    for (int i = 0; i < P::E; i++) {
+        const int p = fftl::slot_pos<N, P::T, P::F0>(i, t);
+        v[i] = ok ? make_float2(__ldcs(&r0[p]), __ldcs(&r0[N + p])) : make_float2(0.f, 0.f);
     }
+    P::template seq_row<false>(buf, v, tw);
+    float2 *line = buf + b * Y::LINE;
+#pragma unroll
+    for (int i = 0; i < P::E; i++) line[Y::at(fftl::slot_pos<N, P::T, P::RV0>(i, t))] = v[i];
     __syncthreads();
-    P::template run<false>(buf, tw);
+    if (!ok) return;
     const int c = carrier[1];
-    for (int e = threadIdx.x; e < P::B * M; e += P::THREADS) {
-        const int b = e / M, m = e - b * M;
-        const long q = pair0 + b;
-        if (q >= npairs) continue;
+    for (int m = t; m < M; m += P::T) {
         int k = (c - N / 2 + m - M / 2) % N;
         if (k < 0) k += N;
-        const float2 z1 = buf[b * P::LP + k];
-        const float2 z2 = buf[b * P::LP + ((N - k) % N)];
+        const float2 z1 = line[Y::at(k)];
+        const float2 z2 = line[Y::at((N - k) % N)];
         // two real rows from one complex transform: Xa = (Z_k + conj Z_{N-k})/2,
         // Xb = (Z_k - conj Z_{N-k})/(2i)
         const float2 xa = make_float2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
@@ -127,13 +142,20 @@ __global__ void __launch_bounds__(Plan<N>::THREADS) qpi_rows_kernel(const float 
 // ------------------------------------------------------------ forward column pass
 // Lines l = m + M*a, element y at T1[a*N*M + y*M + m].  Keeps window rows
 // ky = (r - N/2 + j - M/2) mod N, masks to |offsets| <= radius and stores at the
-// ifftshifted position of S (A x M x M).
+// ifftshifted position of S (A x M x M).  T1 is L2-resident (one chunk of
+// holograms), the first stage loads straight into registers and the spectrum is
+// parked in shared memory only for the window extraction.
 template <int N>
-__global__ void __launch_bounds__(Plan<N>::THREADS) qpi_cols_kernel(const float2 *__restrict__ T1, float2 *S,
-                                                                   const int *__restrict__ carrier, long nlines,
-                                                                   int M, const float2 *__restrict__ tw)
+struct QCols : fftl::Plan<N> {};
+template <> struct QCols<1024> : fftl::PlanT<1024, 4, 64, fftl::Radices<16, 16, 4>, fftl::Radices<4, 16, 16>> {};
+template <> struct QCols<2048> : fftl::PlanT<2048, 2, 128, fftl::Radices<16, 16, 8>, fftl::Radices<8, 16, 16>> {};
+
+template <int N>
+__global__ void __launch_bounds__(QCols<N>::THREADS) qpi_cols_kernel(const float2 *__restrict__ T1, float2 *S,
+                                                                    const int *__restrict__ carrier, long nlines,
+                                                                    int M, const float2 *__restrict__ tw)
 {
-    using P = Plan<N>;
+    using P = QCols<N>;
     extern __shared__ float4 smem4[];
     float2 *buf = reinterpret_cast<float2 *>(smem4);
     const long line0 = (long)blockIdx.x * P::B;
@@ -143,9 +165,15 @@ __global__ void __launch_bounds__(Plan<N>::THREADS) qpi_cols_kernel(const float2
     const int m = ok ? (int)(l % M) : 0;
     const long a = ok ? l / M : 0;
     const float2 *src = T1 + a * (long)N * M + m;
-    for (int p = t; p < N; p += P::T) buf[b * P::LP + p] = ok ? __ldcs(&src[(long)p * M]) : make_float2(0.f, 0.f);
+    float2 v[P::E];
+#pragma unroll
+    for (int i = 0; i < P::E; i++)
+        v[i] = ok ? __ldcs(&src[(long)fftl::slot_pos<N, P::T, P::F0>(i, t) * M]) : make_float2(0.f, 0.f);
+    P::template seq<false, false, false>(buf, v, tw);
+    float2 *line = buf + b * P::LP;
+#pragma unroll
+    for (int i = 0; i < P::E; i++) line[fftl::slot_pos<N, P::T, P::RV0>(i, t)] = v[i];
     __syncthreads();
-    P::template run<false>(buf, tw);
     if (!ok) return;
     const int r = carrier[0], rad = carrier[2];
     const int ox = m - M / 2;
@@ -155,9 +183,9 @@ __global__ void __launch_bounds__(Plan<N>::THREADS) qpi_cols_kernel(const float2
         const int oy = j - M / 2;
         int ky = (r - N / 2 + oy) % N;
         if (ky < 0) ky += N;
-        float2 v = buf[b * P::LP + ky];
-        if (abs(ox) > rad || abs(oy) > rad) v = make_float2(0.f, 0.f);
-        dst[(long)((j + M / 2) % M) * M + io] = v;
+        float2 vv = line[ky];
+        if (abs(ox) > rad || abs(oy) > rad) vv = make_float2(0.f, 0.f);
+        dst[(long)((j + M / 2) % M) * M + io] = vv;
     }
 }
 
@@ -210,20 +238,23 @@ template <int N>
 static cudaError_t qpi_fwd_launch(const float *holo, int A, int M, const int *carrier, float2 *T1, float2 *S,
                                   cudaStream_t s)
 {
-    using P = Plan<N>;
-    const size_t smem = fftl::smem_bytes<N>();
+    using PR = QRows<N>;
+    const size_t smem_r = fftl::plan_smem_row<PR>();
     const long npairs = (long)A * N / 2;
-    cudaError_t e = set_smem<N>(qpi_rows_kernel<N>, smem);
+    cudaError_t e = set_smem<N>(qpi_rows_kernel<N>, smem_r);
     if (e != cudaSuccess) return e;
-    qpi_rows_kernel<N><<<(unsigned)((npairs + P::B - 1) / P::B), P::THREADS, smem, s>>>(holo, T1, carrier, npairs, M,
-                                                                                        twiddles(N)); note_launch();
+    qpi_rows_kernel<N><<<(unsigned)((npairs + PR::B - 1) / PR::B), PR::THREADS, smem_r, s>>>(holo, T1, carrier, npairs,
+                                                                                           M, twiddles(N));
+    note_launch();
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
+    using PC = QCols<N>;
     const long nl = (long)A * M;
+    const size_t smem = fftl::plan_smem<PC>();
     e = set_smem<N>(qpi_cols_kernel<N>, smem);
     if (e != cudaSuccess) return e;
-    qpi_cols_kernel<N><<<(unsigned)((nl + P::B - 1) / P::B), P::THREADS, smem, s>>>(T1, S, carrier, nl, M,
-                                                                                   twiddles(N)); note_launch();
+    qpi_cols_kernel<N><<<(unsigned)((nl + PC::B - 1) / PC::B), PC::THREADS, smem, s>>>(T1, S, carrier, nl, M,
+                                                                                      twiddles(N)); note_launch();
     return cudaGetLastError();
 }
 

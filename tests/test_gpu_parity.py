@@ -72,7 +72,7 @@ def test_fft_multidim(ctx, dev, dims):
 
 
 # ---------------------------------------------------------------- QPI
-@pytest.mark.parametrize("n,angles", [(64, 4), (256, 3)])
+@pytest.mark.parametrize("n,angles", [(64, 4), (256, 3), (512, 3), (1024, 2), (2048, 1)])
 def test_qpi_matches_oracle(ctx, dev, oracle, n, angles):
     from ctdm_gb300 import phantom
     acq = phantom.acquisition(n, n, angles, seed=n, pixel=0.1e-6 * 256 / n)
