@@ -194,7 +194,8 @@ const float *dct_eigen(int M)
 // ---------------------------------------------------------------- context
 enum BufId {
     B_PHASE, B_AMP, B_PHU, B_CHG, B_CUT, B_GOLD, B_U, B_F2, B_COUNTS, B_G, B_T1, B_S, B_BGF, B_DCT, B_MASK, B_GEOM,
-    B_CARRIER, B_KEY, B_SCRATCH, B_HOLO, B_BG, B_RI, B_GSTATE, B_GLIST, B_GSTATUS, B_FASTW, B_FASTIN, B_TMP, B_GWORK, NBUF
+    B_CARRIER, B_KEY, B_SCRATCH, B_HOLO, B_BG, B_RI, B_GSTATE, B_GLIST, B_GSTATUS, B_FASTW, B_FASTIN, B_TMP, B_GWORK,
+    B_TMASK, B_TCOUNT, B_TVALS, NBUF
 };
 
 // Stage boundaries recorded with CUDA events when timing is enabled.
@@ -491,7 +492,7 @@ static ctdm_status do_qpi(ctdm_ctx *c, int N, int M, int A, const float *holo, c
 static ctdm_status do_positivity(ctdm_ctx *c, int R, int iters, int check_mode, double k2, double n_med,
                                  const float2 *F2, const uint8_t *mask, float2 *G, float2 *ri, cudaStream_t s)
 {
-    LoopArgs la;
+    LoopArgs la = {};
     la.G = G;
     la.F2 = F2;
     la.mask = mask;
@@ -505,6 +506,22 @@ static ctdm_status do_positivity(ctdm_ctx *c, int R, int iters, int check_mode, 
     la.s2 = (float)(-k2 / (n_med * n_med));
     la.err = c->d_err;
     CK(ensure_tuned(R, check_mode, s), "autotune loop passes");
+    // the z pass reads the measured samples packed per tile when its plan allows
+    const int TB = loop_ztile(R);
+    la.packed = 0;
+    if (TB > 0) {
+        const long r3 = (long)R * R * R, tiles = (long)R * R / TB;
+        CK(ensure(c, B_TMASK, sizeof(uint32_t) * tiles * R), "alloc packed masks");
+        CK(ensure(c, B_TCOUNT, sizeof(int) * tiles), "alloc packed counts");
+        CK(ensure(c, B_TVALS, sizeof(float2) * r3), "alloc packed values");
+        CK(pack_measured(F2, check_mode == CTDM_CHECK_MASK ? mask : nullptr, R, TB, B<uint32_t>(c, B_TMASK),
+                         B<int>(c, B_TCOUNT), B<float2>(c, B_TVALS), s),
+           "pack measured samples");
+        la.tmask = B<uint32_t>(c, B_TMASK);
+        la.tcount = B<int>(c, B_TCOUNT);
+        la.tvals = B<float2>(c, B_TVALS);
+        la.packed = 1;
+    }
     StageTimer &tm = c->timer;
     if (loop_scheme(R) == 1) {
         // plane + z passes (the plane pass records under the x-pass stage)

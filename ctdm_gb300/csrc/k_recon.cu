@@ -332,6 +332,101 @@ static cudaError_t ewald_launch(const EwaldArgs &a, cudaStream_t s)
     return cudaGetLastError();
 }
 
+// ------------------------------------------------------------ packed measured samples
+// One CTA per z-pass tile (TB consecutive x of one y, all z): the keep bits of each
+// z row by a warp ballot, an exclusive prefix of the per-row counts, then the kept
+// values in (z, b) order at the tile's fixed offset.
+template <int TB>
+__global__ void __launch_bounds__(256) pack_measured_kernel(const float2 *__restrict__ F2,
+                                                           const uint8_t *__restrict__ mask, int R, uint32_t *tmask,
+                                                           int *tcount, float2 *tvals)
+{
+    extern __shared__ int spre[];   // R prefixes, then 8 warp totals
+    int *swarp = spre + R;
+    constexpr int ZR = 256 / TB;    // z rows per step
+    const long tile = blockIdx.x;
+    const long line0 = tile * TB;
+    const long rr = (long)R * R;
+    const int b = threadIdx.x % TB, zr = threadIdx.x / TB;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int sub = lane / TB;
+    uint32_t *tm = tmask + tile * R;
+    for (int z0 = 0; z0 < R; z0 += ZR) {
+        const int z = z0 + zr;
+        bool keep = false;
+        if (z < R) {
+            const long idx = line0 + b + (long)z * rr;
+            if (mask) {
+                keep = mask[idx] != 0;
+            } else {
+                const float2 f = F2[idx];
+                keep = f.x != 0.0f && f.y != 0.0f;
+            }
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, keep);
+        const uint32_t m = TB == 32 ? bal : (bal >> (sub * TB)) & ((1u << TB) - 1u);
+        if (b == 0 && z < R) {
+            tm[z] = m;
+            spre[z] = __popc(m);
+        }
+    }
+    __syncthreads();
+    // exclusive prefix of the row counts: up to 3 consecutive rows per thread
+    constexpr int IT = 3;
+    int own[IT], sum = 0;
+#pragma unroll
+    for (int k = 0; k < IT; k++) {
+        const int z = threadIdx.x * IT + k;
+        own[k] = z < R ? spre[z] : 0;
+        sum += own[k];
+    }
+    int incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int n = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += n;
+    }
+    if (lane == 31) swarp[warp] = incl;
+    __syncthreads();
+    int before = 0;
+    for (int w = 0; w < warp; w++) before += swarp[w];
+    int run = before + incl - sum;
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < IT; k++) {
+        const int z = threadIdx.x * IT + k;
+        if (z < R) spre[z] = run;
+        run += own[k];
+    }
+    if (threadIdx.x == 255) tcount[tile] = run;
+    __syncthreads();
+    float2 *tv = tvals + tile * (long)TB * R;
+    const uint32_t below = (1u << b) - 1u;
+    for (int z0 = 0; z0 < R; z0 += ZR) {
+        const int z = z0 + zr;
+        if (z >= R) continue;
+        const uint32_t m = tm[z];
+        if (!((m >> b) & 1u)) continue;
+        tv[spre[z] + __popc(m & below)] = F2[line0 + b + (long)z * rr];
+    }
+}
+
+cudaError_t pack_measured(const float2 *F2, const uint8_t *mask, int R, int TB, uint32_t *tmask, int *tcount,
+                          float2 *tvals, cudaStream_t s)
+{
+    if (R > 768) return cudaErrorInvalidValue;
+    const unsigned tiles = (unsigned)((long)R * R / TB);
+    const size_t smem = sizeof(int) * (R + 8);
+    switch (TB) {
+    case 8: pack_measured_kernel<8><<<tiles, 256, smem, s>>>(F2, mask, R, tmask, tcount, tvals); break;
+    case 16: pack_measured_kernel<16><<<tiles, 256, smem, s>>>(F2, mask, R, tmask, tcount, tvals); break;
+    case 32: pack_measured_kernel<32><<<tiles, 256, smem, s>>>(F2, mask, R, tmask, tcount, tvals); break;
+    default: return cudaErrorInvalidValue;
+    }
+    note_launch();
+    return cudaGetLastError();
+}
+
 // Volume sides supported by the reconstruction passes.
 #define CTDM_DISPATCH_R(Rrt, FN, ...)                  \
     switch (Rrt) {                                     \

@@ -51,7 +51,20 @@ struct LoopArgs {
     float s2;   // -k^2 / n_med^2
     int *err;   // device status word: a bounded wait that ran out records a nonzero code
     int staged; // z pass: F2 / mask tiles staged by TMA (set by the launcher)
+    // measured samples packed per z-pass tile (TB = the z plan's lines per CTA):
+    // tmask[tile * R + z] bit b = voxel (x0 + b, y, z) keeps its measured value,
+    // tcount[tile] = kept samples, tvals + tile * TB * R = the kept values in (z, b)
+    // order.  packed = 0: the z pass reads F2 / mask instead.
+    const uint32_t *tmask;
+    const int *tcount;
+    const float2 *tvals;
+    int packed;
 };
+
+// Packs F2 (mode 0: re != 0 && im != 0; mode 1: mask != 0) into per-tile masks,
+// counts and values for the z pass (TB lines per tile, 8, 16 or 32).
+cudaError_t pack_measured(const float2 *F2, const uint8_t *mask, int R, int TB, uint32_t *tmask, int *tcount,
+                          float2 *tvals, cudaStream_t s);
 
 cudaError_t launch_ewald(const EwaldArgs &a, cudaStream_t s);
 cudaError_t launch_xpass(const LoopArgs &a, bool final_pass, cudaStream_t s);
@@ -67,6 +80,16 @@ cudaError_t loop_pass_256(int kind, int variant, const LoopArgs &a, int flag, cu
 cudaError_t loop_pass_384(int kind, int variant, const LoopArgs &a, int flag, cudaStream_t s);
 cudaError_t loop_pass_512(int kind, int variant, const LoopArgs &a, int flag, cudaStream_t s);
 cudaError_t loop_pass_768(int kind, int variant, const LoopArgs &a, int flag, cudaStream_t s);
+int loop_ztile_32(int variant);
+int loop_ztile_64(int variant);
+int loop_ztile_128(int variant);
+int loop_ztile_256(int variant);
+int loop_ztile_384(int variant);
+int loop_ztile_512(int variant);
+int loop_ztile_768(int variant);
+// Tile width (lines per CTA) of the z pass in use for side R when it reads packed
+// measured samples, else 0.
+int loop_ztile(int R);
 // Number of plan variants of the loop passes for volume side R (0: unsupported).
 int loop_plan_count(int R);
 cudaError_t loop_pass_variant(int kind, int variant, const LoopArgs &a, int flag, cudaStream_t s);

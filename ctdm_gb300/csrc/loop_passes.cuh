@@ -186,6 +186,101 @@ __global__ void __launch_bounds__(P::THREADS, fftl::plan_min_ctas<P>(3))
     for (int i = 0; i < P::E; i++) __stcs(&a.G[base + (long)fftl::slot_pos<L, P::T, P::F0>(i, t) * nl], v[i]);
 }
 
+// ------------------------------------------------------------ z pass on packed measured samples
+// The same pass reading only the measured samples: the tile's keep masks (one word
+// per z) and its packed values arrive by bulk copies issued before the forward
+// transform; the replacement indexes the packed values by a prefix count over z.
+template <class P>
+constexpr bool zpass_packable()
+{
+    return (P::B == 8 || P::B == 16 || P::B == 32) && P::B <= P::L &&
+           sizeof(float2) * P::B * P::L <= 64 * 1024 && P::THREADS >= P::L / 2 && (P::L * 4) % 16 == 0;
+}
+
+template <class P>
+constexpr size_t zpass_packed_smem()
+{
+    return 128 + sizeof(float2) * P::B * P::L + sizeof(uint32_t) * P::L + sizeof(int) * P::L + 64 +
+           fftl::plan_smem<P>() + 16;
+}
+
+template <class P>
+__global__ void __launch_bounds__(P::THREADS, fftl::plan_min_ctas<P>(3))
+    zpass_packed_kernel(LoopArgs a, const float2 *__restrict__ tw)
+{
+    constexpr int L = P::L;
+    extern __shared__ float4 smem4[];
+    char *base0 = reinterpret_cast<char *>(smem4);
+    char *al = base0 + ((128 - (tma::smem_addr(base0) & 127)) & 127);
+    float2 *svals = reinterpret_cast<float2 *>(al);                          // P::B * L
+    uint32_t *smask = reinterpret_cast<uint32_t *>(svals + P::B * L);        // L
+    int *spre = reinterpret_cast<int *>(smask + L);                          // L
+    int *swarp = spre + L;                                                   // 16
+    float2 *buf = reinterpret_cast<float2 *>(swarp + 16);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(buf + P::B * P::LP);
+    const long nl = (long)L * L;
+    const long line0 = (long)blockIdx.x * P::B;   // line = x + L y; tile = line0 / B
+    const long tile = line0 / P::B;
+    if (threadIdx.x == 0) {
+        tma::mbar_init(bar, 1);
+        tma::fence_barrier_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int cnt = a.tcount[tile];
+        const uint32_t vbytes = (uint32_t)(((cnt + 1) & ~1) * sizeof(float2));
+        tma::mbar_expect_tx(bar, (uint32_t)(L * sizeof(uint32_t)) + vbytes);
+        tma::bulk_load(smask, a.tmask + tile * L, (uint32_t)(L * sizeof(uint32_t)), bar);
+        if (vbytes) tma::bulk_load(svals, a.tvals + tile * (long)P::B * L, vbytes, bar);
+    }
+    const int b = threadIdx.x % P::B, t = threadIdx.x / P::B;
+    const long base = line0 + b;
+    float2 v[P::E];
+#pragma unroll
+    for (int i = 0; i < P::E; i++) v[i] = __ldcs(&a.G[base + (long)fftl::slot_pos<L, P::T, P::F0>(i, t) * nl]);
+    P::template seq<false, false, false>(buf, v, tw);
+    tma::mbar_wait(bar, 0, a.err, 3);
+    // exclusive prefix over z of the kept counts (two z per thread at most)
+    {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        const int z0 = 2 * threadIdx.x;
+        const int c0 = z0 < L ? __popc(smask[z0]) : 0, c1 = z0 + 1 < L ? __popc(smask[z0 + 1]) : 0;
+        int incl = c0 + c1;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int n = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += n;
+        }
+        if (lane == 31) swarp[warp] = incl;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            const int nw = P::THREADS / 32;
+            int w = threadIdx.x < nw ? swarp[threadIdx.x] : 0;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int n = __shfl_up_sync(0xffffffffu, w, o);
+                if (threadIdx.x >= o) w += n;
+            }
+            if (threadIdx.x < nw) swarp[threadIdx.x] = w;   // inclusive warp totals
+        }
+        __syncthreads();
+        const int excl = incl - (c0 + c1) + (warp > 0 ? swarp[warp - 1] : 0);
+        if (z0 < L) spre[z0] = excl;
+        if (z0 + 1 < L) spre[z0 + 1] = excl + c0;
+        __syncthreads();
+    }
+    const uint32_t below = (1u << b) - 1u;
+#pragma unroll
+    for (int i = 0; i < P::E; i++) {
+        const int z = fftl::slot_pos<L, P::T, P::RV0>(i, t);
+        const uint32_t m = smask[z];
+        if ((m >> b) & 1u) v[i] = svals[spre[z] + __popc(m & below)];
+    }
+    P::template seqr<true, false, false>(buf, v, tw);
+#pragma unroll
+    for (int i = 0; i < P::E; i++) __stcs(&a.G[base + (long)fftl::slot_pos<L, P::T, P::F0>(i, t) * nl], v[i]);
+}
+
 // ------------------------------------------------------------ launchers
 // kind: LOOP_X, LOOP_X_FINAL, LOOP_Y_FWD, LOOP_Y_INV, LOOP_Z (flag = check mode)
 template <class P>
@@ -203,6 +298,12 @@ static cudaError_t run_loop_pass(int kind, const LoopArgs &a, int flag, cudaStre
     } else if (kind == LOOP_Y_FWD || kind == LOOP_Y_INV) {
         const size_t smem = fftl::plan_smem<P>();
         auto k = kind == LOOP_Y_INV ? ypass_kernel<P, true> : ypass_kernel<P, false>;
+        e = prep_plan_kernel(k, L, smem);
+        if (e != cudaSuccess) return e;
+        k<<<grid, P::THREADS, smem, s>>>(a, twiddles(L));
+    } else if (a.packed && zpass_packable<P>()) {
+        const size_t smem = zpass_packed_smem<P>();
+        auto k = zpass_packed_kernel<P>;
         e = prep_plan_kernel(k, L, smem);
         if (e != cudaSuccess) return e;
         k<<<grid, P::THREADS, smem, s>>>(a, twiddles(L));
@@ -230,6 +331,13 @@ static cudaError_t run_loop_pass(int kind, const LoopArgs &a, int flag, cudaStre
     return cudaGetLastError();
 }
 
+// Lines per z-pass CTA when that plan reads packed measured samples, else 0.
+template <class P>
+constexpr int zpass_tile()
+{
+    return zpass_packable<P>() ? P::B : 0;
+}
+
 }  // namespace ctdm
 
 // One translation unit per volume side: loop_pass_<R>(kind, variant, args, flag, stream).
@@ -239,6 +347,11 @@ static cudaError_t run_loop_pass(int kind, const LoopArgs &a, int flag, cudaStre
     {                                                                                                     \
         (void)variant;                                                                                    \
         return run_loop_pass<fftl::PV<LL, 0>>(kind, a, flag, s);                                         \
+    }                                                                                                     \
+    int loop_ztile_##LL(int variant)                                                                      \
+    {                                                                                                     \
+        (void)variant;                                                                                    \
+        return zpass_tile<fftl::PV<LL, 0>>();                                                             \
     }                                                                                                     \
     }
 #define CTDM_LOOP_SIZE_3(LL)                                                                              \
@@ -250,5 +363,10 @@ static cudaError_t run_loop_pass(int kind, const LoopArgs &a, int flag, cudaStre
         case 2: return run_loop_pass<fftl::PV<LL, 2>>(kind, a, flag, s);                                  \
         default: return run_loop_pass<fftl::PV<LL, 0>>(kind, a, flag, s);                                 \
         }                                                                                                 \
+    }                                                                                                     \
+    int loop_ztile_##LL(int variant)                                                                      \
+    {                                                                                                     \
+        return variant == 1 ? zpass_tile<fftl::PV<LL, 1>>()                                               \
+                            : (variant == 2 ? zpass_tile<fftl::PV<LL, 2>>() : zpass_tile<fftl::PV<LL, 0>>()); \
     }                                                                                                     \
     }

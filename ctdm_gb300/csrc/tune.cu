@@ -65,6 +65,32 @@ cudaError_t loop_pass_variant(int kind, int variant, const LoopArgs &a, int flag
     }
 }
 
+static PlanChoice choice_of(int R);
+
+int loop_ztile(int R)
+{
+    const char *env = std::getenv("CTDM_PACKED_Z");
+    if (env && std::strcmp(env, "0") == 0) return 0;
+    int v = 0;
+    {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_choice.find({dev, R});
+        if (it != g_choice.end()) v = it->second.v[2];
+    }
+    switch (R) {
+    case 32: return loop_ztile_32(v);
+    case 64: return loop_ztile_64(v);
+    case 128: return loop_ztile_128(v);
+    case 256: return loop_ztile_256(v);
+    case 384: return loop_ztile_384(v);
+    case 512: return loop_ztile_512(v);
+    case 768: return loop_ztile_768(v);
+    default: return 0;
+    }
+}
+
 static PlanChoice choice_of(int R)
 {
     int dev = 0;

@@ -102,3 +102,30 @@ def test_pipeline_full_size_plain(ctx, dev, oracle):
     assert ctx.carrier() == car
     err = float(np.sqrt(np.mean(np.abs(out.cpu().numpy().astype(np.complex128) - ref) ** 2)))
     assert err < RI_TOL, err
+
+
+@pytest.mark.parametrize("r", [64, 256])
+def test_packed_measured_samples_bit_identical(ctx, dev, r):
+    """The z pass on packed measured samples replaces exactly the voxels the dense
+    pass replaces, with the same values: volumes are bit-identical (both predicates)."""
+    import os
+    import torch
+    f2 = synthetic_f2(r, seed=11 + r)
+    counts = ((f2.real != 0) & (f2.imag != 0)).astype(np.uint32)
+    counts[: r // 2] = 0                        # hit mask differs from the value predicate
+    d_f2 = torch.from_numpy(f2).to(dev)
+    d_counts = torch.from_numpy(counts.view(np.int32)).to(dev)
+    outs = {}
+    for packed in ("1", "0"):
+        os.environ["CTDM_PACKED_Z"] = packed
+        try:
+            for mode in (0, 1):
+                out = torch.empty_like(d_f2)
+                ctx.positivity(d_f2, r, 3, K2, N_MED, out, check_mode=mode, counts=d_counts)
+                torch.cuda.synchronize()
+                outs[(packed, mode)] = out.cpu().numpy()
+        finally:
+            os.environ.pop("CTDM_PACKED_Z", None)
+    for mode in (0, 1):
+        assert np.array_equal(outs[("1", mode)], outs[("0", mode)]), mode
+    assert not np.array_equal(outs[("1", 0)], outs[("1", 1)])
