@@ -32,6 +32,8 @@ CONFIGS = {
     "plain_small": dict(iterations=10, goldstein=False),
     "wrap_heavy": dict(iterations=20, goldstein=True),
     "batched": dict(iterations=10, goldstein=False, tomograms=64, lanes=4),
+    "gradient": dict(iterations=10, goldstein=False),
+    "gradient_small": dict(iterations=10, goldstein=False),
 }
 
 
@@ -275,6 +277,115 @@ def run_batched(args):
     batch.close()
 
 
+# ---------------------------------------------------------------- gradient form vs positivity loop
+def run_gradient(args):
+    """The differentiable form (FISTA on 1/2 ||P F V - y||^2 + lambda TV(V) with the
+    hand-written adjoint, optionally with the positivity constraint as a proximal
+    step) against the positivity loop on the same measured data:
+    RI RMSE against the phantom's band-limited RI volume and device time, for a
+    schedule of gradient iteration counts.  `value` is tomograms/s of the gradient
+    form at the first iteration count whose RMSE is at most the loop's (front end
+    included); null when none reaches it."""
+    import torch
+    import ctdm_gb300 as C
+    from ctdm_gb300 import build, phantom
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    build.build()
+    cfg = CONFIGS[args.config]
+    if args.config == "gradient":
+        # 1024^2 holograms, 181 angles on a cone at NA 1.2, 512^3 volume
+        acq = phantom.acquisition(1024, 512, 181, na=1.2, seed=4000 + rank)
+    else:
+        acq = phantom.config_plain_small(seed=1000 + rank)
+    r = acq.r_vol
+    iters = cfg["iterations"]
+    ctx = C.Context(local)
+    stream = torch.cuda.current_stream(dev)
+    holo = torch.from_numpy(acq.holograms).to(dev)
+    bg = torch.from_numpy(acq.background).to(dev)
+    out = torch.empty((r, r, r), dtype=torch.complex64, device=dev)
+
+    def ev():
+        return torch.cuda.Event(enable_timing=True)
+
+    p = C.params_for(acq, iters)
+    p0 = C.params_for(acq, 0)
+    for _ in range(args.warmup):
+        ctx.reconstruct_device(p, holo, bg, acq.ang_x, acq.ang_y, out, stream=stream)
+    torch.cuda.synchronize()
+    # plain method, whole path; and the path without loop bodies (front end + final pass)
+    a, b = ev(), ev()
+    a.record(stream)
+    ctx.reconstruct_device(p, holo, bg, acq.ang_x, acq.ang_y, out, stream=stream)
+    b.record(stream)
+    b.synchronize()
+    t_plain = a.elapsed_time(b)
+    n_plain = out.clone()
+    a, b = ev(), ev()
+    a.record(stream)
+    ctx.reconstruct_device(p0, holo, bg, acq.ang_x, acq.ang_y, out, stream=stream)
+    b.record(stream)
+    b.synchronize()
+    t_front = a.elapsed_time(b)
+    ptr, nbytes = ctx.buffer(7)          # measured data F2 of that call
+    truth_f2 = torch.from_numpy(phantom.f2_truth(acq)).to(dev)
+    n_true = torch.empty_like(out)
+    ctx.positivity(truth_f2, r, 0, acq.k2, acq.n_med, n_true)
+    del truth_f2
+    torch.cuda.synchronize()
+
+    def rmse(x):
+        return float(torch.sqrt(torch.mean(torch.abs(x - n_true) ** 2)))
+
+    rmse_plain = rmse(n_plain)
+    tape = C.Tape(ptr, r, acq.k2, device=local)
+    V = torch.zeros((r, r, r), dtype=torch.complex64, device=dev)
+    n_g = torch.empty_like(out)
+    runs = []
+    best = None
+    for pos, lam in ((True, 0.0), (True, 1e-4), (False, 0.0), (False, 1e-3)):
+        for j in (2, 3, 4, 5, 6, 8, 10, 20, 40):
+            V.zero_()
+            torch.cuda.synchronize()
+            a, b = ev(), ev()
+            a.record(stream)
+            tape.reconstruct(V, j, lam=lam, eps=1e-3, step=1.0 if lam == 0.0 else 0.0, stream=stream,
+                             positivity=pos)
+            C.contrast_to_ri(V, r, acq.n_med, n_g, clamp=True, stream=stream)
+            b.record(stream)
+            b.synchronize()
+            t = a.elapsed_time(b)
+            e = rmse(n_g)
+            runs.append({"positivity": pos, "lambda": lam, "iterations": j, "ms": round(t, 3), "ri_rmse": e})
+            if e <= rmse_plain and (best is None or t < best["ms"]):
+                best = {"positivity": pos, "lambda": lam, "iterations": j, "ms": t, "ri_rmse": e}
+    tape.close()
+    t_grad = None if best is None else t_front + best["ms"]
+    line = {
+        "metric": "tomograms/s (hologram->RI), gradient form at the positivity loop's RI RMSE",
+        "value": None if t_grad is None else 1e3 / t_grad,
+        "unit": "tomograms/s",
+        "n_gpus": 1,
+        "steps": 1,
+        "warmup": args.warmup,
+        "ms_per_step": t_grad,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32/c64",
+        "data": "synthetic (seeded Rytov phantom, Poisson noise); RMSE against the phantom's band-limited RI",
+        "config": {"workload": args.config, "holograms": f"{len(acq.ang_x)}x{acq.n_holo}^2", "volume": f"{r}^3",
+                   "positivity_iterations": iters},
+        "plain": {"ms": t_plain, "ri_rmse": rmse_plain, "tomograms_per_s": 1e3 / t_plain},
+        "front_end_ms": t_front,
+        "gradient_best": best,
+        "gradient_runs": runs,
+    }
+    print(json.dumps(line))
+
+
 # ---------------------------------------------------------------- GPU arm
 def run_ours(args):
     import torch
@@ -415,9 +526,9 @@ def run_reference(args):
     rank, world, local = dist_info()
     if rank != 0:
         return
-    if args.config == "batched":
-        print(json.dumps({"impl": "reference", "unavailable": "the batched workload has no reference counterpart "
-                          "(the reference reconstructs one tomogram per BatchRecon call)"}))
+    if args.config == "batched" or args.config.startswith("gradient"):
+        print(json.dumps({"impl": "reference", "unavailable": f"the {args.config} workload has no reference "
+                          "counterpart (the reference has one positivity-loop reconstruction per BatchRecon call)"}))
         return
     cfg = CONFIGS[args.config]
     acq = make_workload(args.config, seed=1000)
@@ -464,6 +575,8 @@ def main():
         run_reference(args)
     elif args.config == "batched":
         run_batched(args)
+    elif args.config.startswith("gradient"):
+        run_gradient(args)
     else:
         run_ours(args)
 

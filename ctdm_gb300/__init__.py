@@ -325,10 +325,14 @@ class Tape:
               "ctdm_loss_grad")
         return loss.value
 
-    def reconstruct(self, V, iterations, lam=1e-3, eps=1e-4, step=0.0, record_loss=False, stream=None):
+    def reconstruct(self, V, iterations, lam=1e-3, eps=1e-4, step=0.0, record_loss=False, stream=None,
+                    positivity=False):
+        """FISTA on 1/2 ||A V - y||^2 + lam TV_eps(V) from V (in place); positivity=True
+        projects every update onto the reference's positivity set."""
         hist = np.zeros(max(iterations, 1), np.float64) if record_loss else None
-        check(self.lib.ctdm_reconstruct_gradient(self.handle, int(iterations), float(lam), float(eps), float(step),
-                                                 _ptr(V), _ptr(hist), _stream(stream)), "ctdm_reconstruct_gradient")
+        check(self.lib.ctdm_reconstruct_gradient_ex(self.handle, int(iterations), float(lam), float(eps), float(step),
+                                                    int(positivity), _ptr(V), _ptr(hist), _stream(stream)),
+              "ctdm_reconstruct_gradient_ex")
         return hist
 
     def close(self):

@@ -75,6 +75,8 @@ _SIGS = {
     "ctdm_loss_grad": (c_int, [c_void_p, c_void_p, c_double, c_double, c_void_p, ctypes.POINTER(c_double)]),
     "ctdm_reconstruct_gradient": (c_int, [c_void_p, c_int, c_double, c_double, c_double, c_void_p, c_void_p,
                                           c_void_p]),
+    "ctdm_reconstruct_gradient_ex": (c_int, [c_void_p, c_int, c_double, c_double, c_double, c_int, c_void_p,
+                                             c_void_p, c_void_p]),
     "ctdm_contrast_to_ri": (c_int, [c_int, c_void_p, c_double, c_int, c_void_p, c_void_p]),
     "ctdm_batch_create": (c_int, [c_int, c_int, ctypes.POINTER(c_void_p)]),
     "ctdm_batch_destroy": (None, [c_void_p]),

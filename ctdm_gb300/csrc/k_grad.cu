@@ -227,11 +227,37 @@ __global__ void tv_grad_kernel(const float2 *__restrict__ V, int R, float lambda
 }
 
 // FISTA: V+ = W - tau g;  W = V+ + beta (V+ - V)
+// Projection of a contrast V onto the positivity set of the reference's est_n clamp
+// (cTDM/Recon_kernel.cu:305-342: Re n >= n_med, Im n >= 0 for n = n_med sqrt(1 + V)):
+// s = sqrt(1 + V) (principal root), s' = (max(Re s, 1), max(Im s, 0)), V' = s'^2 - 1.
+__device__ __forceinline__ float2 project_contrast(float2 v)
+{
+    const float c = 1.0f + v.x, d = v.y;
+    const float mod = hypotf(c, d);
+    float a, b;
+    if (d == 0.0f) {
+        a = sqrtf(fmaxf(c, 0.0f));
+        b = 0.0f;
+    } else if (c >= 0.0f) {
+        a = sqrtf((mod + c) * 0.5f);
+        b = d / (2.0f * a);
+    } else {
+        b = sqrtf((mod - c) * 0.5f);
+        a = fabsf(d) / (2.0f * b);
+        if (d < 0.0f) b = -b;
+    }
+    a = fmaxf(a, 1.0f);
+    b = fmaxf(b, 0.0f);
+    return make_float2(a * a - b * b - 1.0f, 2.0f * a * b);
+}
+
+template <bool PROJECT>
 __global__ void fista_kernel(float2 *V, float2 *W, const float2 *__restrict__ g, long n, float tau, float beta)
 {
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
         const float2 w = W[i], gg = g[i], v = V[i];
-        const float2 vn = make_float2(w.x - tau * gg.x, w.y - tau * gg.y);
+        float2 vn = make_float2(w.x - tau * gg.x, w.y - tau * gg.y);
+        if (PROJECT) vn = project_contrast(vn);
         V[i] = vn;
         W[i] = make_float2(vn.x + beta * (vn.x - v.x), vn.y + beta * (vn.y - v.y));
     }
@@ -428,8 +454,9 @@ extern "C" ctdm_status ctdm_loss_grad(ctdm_tape *t, const ctdm_cfloat *d_V, doub
     return CTDM_OK;
 }
 
-extern "C" ctdm_status ctdm_reconstruct_gradient(ctdm_tape *t, int iterations, double lambda, double eps,
-                                                 double step, ctdm_cfloat *d_V, double *h_loss, void *stream)
+extern "C" ctdm_status ctdm_reconstruct_gradient_ex(ctdm_tape *t, int iterations, double lambda, double eps,
+                                                    double step, int positivity, ctdm_cfloat *d_V, double *h_loss,
+                                                    void *stream)
 {
     if (!t || !d_V || iterations < 0) return fail(CTDM_ERR_INVALID, "ctdm_reconstruct_gradient: bad argument%s");
     GCK(cudaSetDevice(t->device), "cudaSetDevice");
@@ -464,11 +491,22 @@ extern "C" ctdm_status ctdm_reconstruct_gradient(ctdm_tape *t, int iterations, d
         }
         if (h_loss) h_loss[it] = loss;   // objective at the extrapolated point
         const double tn = 0.5 * (1.0 + std::sqrt(1.0 + 4.0 * tk * tk));
-        fista_kernel<<<grid_for(n), 256, 0, s>>>(V, t->wmom, t->grad, n, (float)tau, (float)((tk - 1.0) / tn)); note_launch();
+        const float beta = (float)((tk - 1.0) / tn);
+        if (positivity)
+            fista_kernel<true><<<grid_for(n), 256, 0, s>>>(V, t->wmom, t->grad, n, (float)tau, beta);
+        else
+            fista_kernel<false><<<grid_for(n), 256, 0, s>>>(V, t->wmom, t->grad, n, (float)tau, beta);
+        note_launch();
         GCK(cudaGetLastError(), "update");
         tk = tn;
     }
     return CTDM_OK;
+}
+
+extern "C" ctdm_status ctdm_reconstruct_gradient(ctdm_tape *t, int iterations, double lambda, double eps,
+                                                 double step, ctdm_cfloat *d_V, double *h_loss, void *stream)
+{
+    return ctdm_reconstruct_gradient_ex(t, iterations, lambda, eps, step, 0, d_V, h_loss, stream);
 }
 
 extern "C" ctdm_status ctdm_contrast_to_ri(int R, const ctdm_cfloat *d_V, double n_med, int clamp, ctdm_cfloat *d_ri,

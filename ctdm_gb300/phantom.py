@@ -184,3 +184,23 @@ def config_wrap_heavy(seed=2000, angles=121):
 def small_case(seed=7, n=64, r=64, angles=6, na=0.9, pixel=0.4e-6, photons=1000.0):
     """Tiny acquisition for parity tests: FOV 25.6 um at 0.4 um pixels."""
     return acquisition(n, r, angles, na=na, seed=seed, pixel=pixel, photons=photons)
+
+
+def f2_truth(acq, r=None, chunk=16):
+    """The phantom's scattering potential on the reconstruction's k-space grid, in
+    the layout and scale of the measured data F2 (x fastest; signed frequency index
+    ii at x = ii mod R; F2 = f_hat / dx^3, the scale the Ewald mapping gives the
+    measured samples).  Every voxel is filled, so the positivity path with zero loop
+    bodies turns it into the phantom's band-limited RI volume (the ground truth for
+    error against the phantom).  complex64 (R, R, R) as [z][y][x]."""
+    r = r or acq.r_vol
+    df = 1.0 / (r * acq.dx)
+    sgn = np.fft.fftfreq(r, 1.0 / r) * df
+    ky, kx = np.meshgrid(sgn, sgn, indexing="ij")     # [y][x]
+    out = np.empty((r, r, r), np.complex64)
+    scale = 1.0 / acq.dx ** 3
+    for z0 in range(0, r, chunk):
+        kz = sgn[z0:z0 + chunk][:, None, None]
+        out[z0:z0 + chunk] = (potential_hat(acq.ellipsoids, acq.n_med, acq.wavelength, kx[None], ky[None], kz)
+                              * scale).astype(np.complex64)
+    return out

@@ -234,6 +234,13 @@ CTDM_API ctdm_status ctdm_loss_grad(ctdm_tape *tape, const ctdm_cfloat *d_V, dou
  * the objective per iteration (synchronises each iteration when given). */
 CTDM_API ctdm_status ctdm_reconstruct_gradient(ctdm_tape *tape, int iterations, double lambda, double eps, double step,
                                                ctdm_cfloat *d_V, double *h_loss, void *stream);
+/* The same with the positivity constraint of the reference's loop as a proximal step
+ * (positivity = 1): each update is projected onto Re n >= n_med, Im n >= 0 for
+ * n = n_med sqrt(1 + V).  With lambda = 0 and step 1 the iteration is the reference's
+ * data-replacement / positivity loop with Nesterov momentum. */
+CTDM_API ctdm_status ctdm_reconstruct_gradient_ex(ctdm_tape *tape, int iterations, double lambda, double eps,
+                                                  double step, int positivity, ctdm_cfloat *d_V, double *h_loss,
+                                                  void *stream);
 /* n = n_med sqrt(1 + V), optional positivity clamp, octant-shifted like the reference output. */
 CTDM_API ctdm_status ctdm_contrast_to_ri(int R, const ctdm_cfloat *d_V, double n_med, int clamp, ctdm_cfloat *d_ri,
                                          void *stream);

@@ -92,9 +92,18 @@ def loss_grad(V, idx, y, lam=0.0, eps=1e-4):
     return L, g
 
 
-def fista(V0, idx, y, iterations, lam=0.0, eps=1e-4, step=None):
+def project_positivity(V):
+    """Contrast V projected onto the positivity set of the est_n clamp: s = sqrt(1 + V)
+    (principal root), s' = (max(Re s, 1), max(Im s, 0)), V' = s'^2 - 1."""
+    s = np.sqrt(1.0 + np.asarray(V, np.complex128))
+    s = np.maximum(s.real, 1.0) + 1j * np.maximum(s.imag, 0.0)
+    return s * s - 1.0
+
+
+def fista(V0, idx, y, iterations, lam=0.0, eps=1e-4, step=None, positivity=False):
     """Accelerated gradient descent in the form the library runs:
-    V+ = W - tau grad L(W); W = V+ + (t_k - 1)/t_{k+1} (V+ - V).  Returns (V, losses at W)."""
+    V+ = W - tau grad L(W) (projected onto the positivity set when asked);
+    W = V+ + (t_k - 1)/t_{k+1} (V+ - V).  Returns (V, losses at W)."""
     tau = step if step else 1.0 / (1.0 + 12.0 * lam / eps)
     V = np.asarray(V0, np.complex128).copy()
     W = V.copy()
@@ -105,6 +114,8 @@ def fista(V0, idx, y, iterations, lam=0.0, eps=1e-4, step=None):
         hist.append(L)
         tn = 0.5 * (1.0 + np.sqrt(1.0 + 4.0 * t * t))
         Vn = W - tau * g
+        if positivity:
+            Vn = project_positivity(Vn)
         W = Vn + ((t - 1.0) / tn) * (Vn - V)
         V = Vn
         t = tn

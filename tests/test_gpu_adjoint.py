@@ -166,6 +166,23 @@ def test_fista_matches_fp64(ctx, dev):
     tape.close()
 
 
+def test_projected_fista_matches_fp64(ctx, dev):
+    """FISTA with the positivity constraint as a proximal step, against FP64."""
+    import torch
+    r, iters = 32, 8
+    tape, _, _, rng = _random_tape(ctx, dev, r, seed=9)
+    y, idx = tape.data()
+    V0 = np.zeros((r, r, r), np.complex64)
+    V = T(V0, dev)
+    tape.reconstruct(V, iters, 0.0, 1e-2, step=1.0, positivity=True)
+    torch.cuda.synchronize()
+    Vr, _ = AD.fista(V0, idx, y.astype(np.complex128), iters, 0.0, 1e-2, step=1.0, positivity=True)
+    assert rel(V.cpu().numpy(), Vr) < 1e-4
+    s = np.sqrt(1.0 + V.cpu().numpy().astype(np.complex128))
+    assert s.real.min() >= 1.0 - 1e-5 and s.imag.min() >= -1e-5    # every iterate is feasible
+    tape.close()
+
+
 def test_contrast_to_ri(ctx, dev):
     import torch
     import ctdm_gb300 as C
