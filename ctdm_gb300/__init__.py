@@ -16,6 +16,7 @@ from ._lib import CtdmError, Params, check, load  # noqa: F401
 CTDM_UNWRAP_REF, CTDM_UNWRAP_EXACT = 0, 1
 CTDM_CHECK_REF, CTDM_CHECK_MASK = 0, 1
 CTDM_METHOD_DCT, CTDM_METHOD_FAST, CTDM_METHOD_GOLDSTEIN = 0, 1, 2
+CTDM_QPI_B, CTDM_QPI_A = 0, 1
 
 
 def _ptr(x):
@@ -138,6 +139,13 @@ class Context:
         c = (ctypes.c_int * 3)(*carrier)
         check(self.lib.ctdm_qpi(self.handle, n, m, n_angles, _ptr(holo), _ptr(bg), int(bg_per_angle), c, _ptr(phase),
                                 _ptr(amp), _stream(stream)), "ctdm_qpi")
+        return tuple(c)
+
+    def qpi_b(self, n, holo, bg, phase, amp, n_angles, bg_per_angle=False, center=(-1, -1), stream=None):
+        """QPI Algorithm B; returns (background carrier column, frame-1 carrier column)."""
+        c = (ctypes.c_int * 2)(*center)
+        check(self.lib.ctdm_qpi_b(self.handle, n, n_angles, _ptr(holo), _ptr(bg), int(bg_per_angle), c, _ptr(phase),
+                                  _ptr(amp), _stream(stream)), "ctdm_qpi_b")
         return tuple(c)
 
     def unwrap_dct(self, phi, out, n_maps, m, mode=CTDM_UNWRAP_REF, stream=None):

@@ -19,7 +19,7 @@ class Params(ctypes.Structure):
         ("n_holo", c_int), ("m_crop", c_int), ("r_vol", c_int), ("iterations", c_int),
         ("unwrap_mode", c_int), ("check_mode", c_int), ("unwrap_method", c_int), ("run_goldstein", c_int),
         ("bg_per_angle", c_int), ("carrier_r", c_int), ("carrier_c", c_int), ("carrier_radius", c_int),
-        ("n_med", c_double), ("wavelength", c_double), ("dx", c_double),
+        ("n_med", c_double), ("wavelength", c_double), ("dx", c_double), ("qpi_method", c_int),
     ]
 
 
@@ -52,6 +52,8 @@ _SIGS = {
                                  c_void_p]),
     "ctdm_qpi": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_int, P_int, c_void_p, c_void_p,
                          c_void_p]),
+    "ctdm_qpi_b": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_int, P_int, c_void_p, c_void_p, c_void_p]),
+    "extractQPI_AlgorithmB": (None, [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_int]),
     "ctdm_unwrap_dct": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p]),
     "ctdm_unwrap_fast": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p]),
     "ctdm_goldstein": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, P_int,

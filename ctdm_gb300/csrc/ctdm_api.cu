@@ -195,7 +195,7 @@ const float *dct_eigen(int M)
 enum BufId {
     B_PHASE, B_AMP, B_PHU, B_CHG, B_CUT, B_GOLD, B_U, B_F2, B_COUNTS, B_G, B_T1, B_S, B_BGF, B_DCT, B_MASK, B_GEOM,
     B_CARRIER, B_KEY, B_SCRATCH, B_HOLO, B_BG, B_RI, B_GSTATE, B_GLIST, B_GSTATUS, B_FASTW, B_FASTIN, B_TMP, B_GWORK,
-    B_TMASK, B_TCOUNT, B_TVALS, NBUF
+    B_TMASK, B_TCOUNT, B_TVALS, B_QMAG, NBUF
 };
 
 // Stage boundaries recorded with CUDA events when timing is enabled.
@@ -280,6 +280,7 @@ extern "C" void ctdm_params_default(ctdm_params *p)
     p->n_med = 1.333;      // cTDM/HilbertTransform.cu:18
     p->wavelength = 532e-9;
     p->dx = 5.5e-6 / 85.0 * 1024.0 / 256.0;   // CameraPixelSize/Mag*1024/R (:1854) at the defaults
+    p->qpi_method = CTDM_QPI_A;
 }
 
 extern "C" ctdm_status ctdm_ctx_create(int device, ctdm_ctx **out)
@@ -552,11 +553,66 @@ static ctdm_status do_positivity(ctdm_ctx *c, int R, int iters, int check_mode, 
     return CTDM_OK;
 }
 
+// QPI Algorithm B for A holograms: carrier columns (frame 1 and background, or given),
+// background field(s), window rows, inverse transforms with the phase/amp epilogue.
+// car: {background column, frame-1 column, -1} on the device.
+static ctdm_status do_qpi_b(ctdm_ctx *c, int N, int A, const float *holo, const float *bg, int bg_per_angle,
+                            const int *center_in, float *phase, float *amp, cudaStream_t s)
+{
+    if (N < 64 || N > 2048 || (N & (N - 1))) return invalid("hologram side %d unsupported", N);
+    if (A < 1) return invalid("no angles");
+    const int M = N / 4;
+    const long mm = (long)M * M, nn = (long)N * N;
+    CK(ensure(c, B_CARRIER, sizeof(int) * 3), "alloc carrier");
+    int *car = B<int>(c, B_CARRIER);
+    if (center_in && center_in[0] >= 0 && center_in[1] >= 0) {
+        if (center_in[0] >= N || center_in[1] >= N) return invalid("carrier column outside the spectrum");
+        CK(set_carrier(car, center_in[0], center_in[1], -1, s), "set carrier");
+    } else {
+        CK(ensure(c, B_QMAG, sizeof(float) * (N / 4) * N), "alloc histogram scratch");
+        CK(set_carrier(car, 0, 0, -1, s), "reset carrier");
+        // frame 1 of sequence1DFFT: the SP frame's own column first, then the background's
+        CK(qpib_spectrum_center(holo, N, B<float>(c, B_QMAG), car + 1, s), "carrier column (frame 1)");
+        CK(qpib_spectrum_center(bg, N, B<float>(c, B_QMAG), car, s), "carrier column (background)");
+    }
+    const int nbg = bg_per_angle ? A : 1;
+    const int rows = A > nbg ? A : nbg;
+    CK(ensure(c, B_T1, sizeof(float2) * rows * mm), "alloc window rows");
+    CK(ensure(c, B_BGF, sizeof(float2) * nbg * mm), "alloc BG field");
+    float2 *T = B<float2>(c, B_T1), *bgf = B<float2>(c, B_BGF);
+    CK(qpib_window(bg, nbg, N, car, T, s), "qpi B background window");
+    CK(qpib_inverse(T, nbg, M, bgf, nullptr, 0, nullptr, nullptr, s), "qpi B background field");
+    CK(qpib_window(holo, 1, N, car + 1, T, s), "qpi B window (frame 1)");
+    if (A > 1) CK(qpib_window(holo + nn, A - 1, N, car, T + mm, s), "qpi B window");
+    CK(qpib_inverse(T, A, M, nullptr, bgf, bg_per_angle ? mm : 0, phase, amp, s), "qpi B fields");
+    return CTDM_OK;
+}
+
+extern "C" ctdm_status ctdm_qpi_b(ctdm_ctx *c, int N, int A, const float *d_holo, const float *d_bg, int bg_per_angle,
+                                  int *center2, float *d_phase, float *d_amp, void *stream)
+{
+    if (!c || !d_holo || !d_bg || !d_phase || !d_amp) return invalid("ctdm_qpi_b: NULL argument");
+    CK(cudaSetDevice(c->device), "cudaSetDevice");
+    cudaStream_t s = (cudaStream_t)stream;
+    ctdm_status st = do_qpi_b(c, N, A, d_holo, d_bg, bg_per_angle, center2, d_phase, d_amp, s);
+    if (st != CTDM_OK) return st;
+    CK(cudaMemcpyAsync(c->carrier, c->buf[B_CARRIER], sizeof(int) * 3, cudaMemcpyDeviceToHost, s), "carrier");
+    CK(cudaStreamSynchronize(s), "carrier");
+    if (center2) {
+        center2[0] = c->carrier[0];
+        center2[1] = c->carrier[1];
+    }
+    g_err.clear();
+    return CTDM_OK;
+}
+
 static ctdm_status validate(const ctdm_params *p, int A, int &M)
 {
     if (!p) return invalid("params is NULL");
     const int N = p->n_holo;
     M = p->m_crop ? p->m_crop : N / 4;
+    if (p->qpi_method != CTDM_QPI_A && p->qpi_method != CTDM_QPI_B) return invalid("unknown QPI method %d", p->qpi_method);
+    if (p->qpi_method == CTDM_QPI_B && M != N / 4) return invalid("QPI Algorithm B fixes the window side to N/4");
     if (N < 64 || N > 2048 || (N & (N - 1))) return invalid("hologram side %d unsupported", N);
     if (!ok_crop(M) || M > N) return invalid("window side %d unsupported", M);
     if (!ok_volume(p->r_vol) || p->r_vol > N) return invalid("volume side %d unsupported", p->r_vol);
@@ -591,7 +647,12 @@ static ctdm_status pipeline_core(ctdm_ctx *c, const ctdm_params *p, int A, int M
     StageTimer &tm = c->timer;
     tm.start(s);
     const int car_in[3] = {p->carrier_r, p->carrier_c, p->carrier_radius};
-    st = do_qpi(c, N, M, A, d_holo, d_bg, p->bg_per_angle, car_in, B<float>(c, B_PHASE), B<float>(c, B_AMP), s);
+    if (p->qpi_method == CTDM_QPI_B) {
+        const int cen_in[2] = {p->carrier_c, p->carrier_c};
+        st = do_qpi_b(c, N, A, d_holo, d_bg, p->bg_per_angle, cen_in, B<float>(c, B_PHASE), B<float>(c, B_AMP), s);
+    } else {
+        st = do_qpi(c, N, M, A, d_holo, d_bg, p->bg_per_angle, car_in, B<float>(c, B_PHASE), B<float>(c, B_AMP), s);
+    }
     if (st != CTDM_OK) return st;
     tm.mark(S_QPI, s);
 
@@ -989,6 +1050,56 @@ extern "C" void ctdm_set_recon_globals(int recon_size, double n_med, double wave
     g_iter_time = iter_time;
     g_recon_save = recon_save;
     g_save_dir = save_dir ? save_dir : ".";
+}
+
+// Carrier column of Algorithm B per device, set by frame 1 (the reference keeps it in
+// the global max_idx_seq1D, cTDM/HilbertTransform.cu:1636-1640).
+static std::map<int, int> g_qpib_column;
+
+extern "C" void extractQPI_AlgorithmB(float *SP, float *BG, ctdm_cfloat *cuSP_FFT, ctdm_cfloat *cuBG_FFT, int Nx, int Ny,
+                                      int frame)
+{
+    ctdm_ctx *c = default_ctx();
+    if (!c) return;
+    if (!SP || !BG || !cuSP_FFT || !cuBG_FFT) { invalid("extractQPI_AlgorithmB: NULL argument"); return; }
+    if (Nx != Ny || Nx < 64 || Nx > 2048 || (Nx & (Nx - 1))) {
+        invalid("extractQPI_AlgorithmB: square power-of-two holograms of 64..2048 only");
+        return;
+    }
+    const int N = Nx, M = N / 4;
+    const long nn = (long)N * N;
+    if (ensure(c, B_HOLO, sizeof(float) * nn) != cudaSuccess || ensure(c, B_BG, sizeof(float) * nn) != cudaSuccess ||
+        ensure(c, B_T1, sizeof(float2) * M * M) != cudaSuccess || ensure(c, B_QMAG, sizeof(float) * M * N) != cudaSuccess ||
+        ensure(c, B_CARRIER, sizeof(int) * 3) != cudaSuccess) {
+        cuda_fail(cudaErrorMemoryAllocation, "extractQPI_AlgorithmB");
+        return;
+    }
+    if (cudaMemcpy(c->buf[B_HOLO], SP, sizeof(float) * nn, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(c->buf[B_BG], BG, sizeof(float) * nn, cudaMemcpyHostToDevice) != cudaSuccess) {
+        cuda_fail(cudaGetLastError(), "extractQPI_AlgorithmB upload");
+        return;
+    }
+    int *car = B<int>(c, B_CARRIER);
+    cudaError_t e = cudaSuccess;
+    if (frame == 1) {
+        // the SP frame's own column, then the background's, which later frames keep
+        e = qpib_spectrum_center(B<float>(c, B_HOLO), N, B<float>(c, B_QMAG), car + 1, 0);
+        if (e == cudaSuccess) e = qpib_spectrum_center(B<float>(c, B_BG), N, B<float>(c, B_QMAG), car, 0);
+        int host[2] = {0, 0};
+        if (e == cudaSuccess) e = cudaMemcpy(host, car, sizeof(int) * 2, cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) g_qpib_column[c->device] = host[0];
+    } else {
+        auto it = g_qpib_column.find(c->device);
+        if (it == g_qpib_column.end()) { invalid("extractQPI_AlgorithmB: frame 1 has not run on this device"); return; }
+        e = set_carrier(car, it->second, it->second, -1, 0);
+    }
+    float2 *T = B<float2>(c, B_T1);
+    if (e == cudaSuccess) e = qpib_window(B<float>(c, B_HOLO), 1, N, car + 1, T, 0);
+    if (e == cudaSuccess) e = qpib_inverse(T, 1, M, reinterpret_cast<float2 *>(cuSP_FFT), nullptr, 0, nullptr, nullptr, 0);
+    if (e == cudaSuccess) e = qpib_window(B<float>(c, B_BG), 1, N, car, T, 0);
+    if (e == cudaSuccess) e = qpib_inverse(T, 1, M, reinterpret_cast<float2 *>(cuBG_FFT), nullptr, 0, nullptr, nullptr, 0);
+    if (e != cudaSuccess) { cuda_fail(e, "extractQPI_AlgorithmB"); return; }
+    finish("extractQPI_AlgorithmB");
 }
 
 extern "C" void DCT_UWLS_Unwrapped(float *ImgDst, float *ImgSrc, int sizeX, int sizeY)

@@ -286,6 +286,235 @@ cudaError_t qpi_inverse_window(float2 *S, int A, int M, float2 *field_out, const
     CTDM_DISPATCH_L(M, qpi_inv_launch, S, A, field_out, bgf, bg_stride, phase, amp, s)
 }
 
+// ------------------------------------------------------------ QPI Algorithm B
+// extractQPI_AlgorithmB / sequence1DFFT (cTDM/HilbertTransform.cu:1587-1660): rows
+// resampled N -> N/4 by the bilinear tap rule (:3658-3723; x ratio (N-1)/N, y ratio
+// (N-1)/(N/4), taps past the edge read 0), an N-point transform along x per row, the
+// swap of the x halves (shiftArray :1745-1758).  Frame 1 takes the carrier column
+// from the column sums of |X| (HistogramFT :1727-1743, thrust::max_element over
+// [int(0.6 N), N), mirrored when within N/8 of the edge); every frame keeps N/4
+// columns from c - N/8 (CropFTdomain :1800-1812), swaps their halves, inverse
+// transforms them (N/4 points) and stores them scaled by 1/(N/4), conjugated and
+// transposed (copySharedMem :1704-1724).
+//
+// Row pass: two output rows packed in one complex transform (row mapping, first
+// stage straight from the bilinear taps), the spectrum parked in shared memory for
+// the unpacking; it either records |X| of both rows (histogram frames) or writes the
+// cropped, half-swapped window rows.
+
+__device__ __forceinline__ float qpib_tap(const float *__restrict__ h, int N, float xr, float yr, int i, int j)
+{
+    const int ix = (int)(xr * (float)i), iy = (int)(yr * (float)j);
+    const float a = xr * (float)i - (float)ix, b = yr * (float)j - (float)iy;
+    const float d00 = (ix < N && iy < N) ? __ldg(&h[(long)iy * N + ix]) : 0.f;
+    const float d10 = (ix + 1 < N && iy < N) ? __ldg(&h[(long)iy * N + ix + 1]) : 0.f;
+    const float d01 = (ix < N && iy + 1 < N) ? __ldg(&h[(long)(iy + 1) * N + ix]) : 0.f;
+    const float d11 = (ix + 1 < N && iy + 1 < N) ? __ldg(&h[(long)(iy + 1) * N + ix + 1]) : 0.f;
+    const float t1 = a * d10 + (-d00 * a + d00);
+    const float t2 = a * d11 + (-d01 * a + d01);
+    return b * t2 + (-t1 * b + t1);
+}
+
+// holo: A holograms N x N; pairs q cover output rows (2q, 2q+1) of the A * N/4 rows.
+// mag != NULL: |X| of the shifted spectrum rows (N floats per row).  Else T gets
+// the M = N/4 window columns per row, half-swapped.  center: device int.
+template <int N>
+__global__ void __launch_bounds__(QRows<N>::THREADS) qpib_rows_kernel(const float *__restrict__ holo, long npairs,
+                                                                     float *mag, float2 *T,
+                                                                     const int *__restrict__ center,
+                                                                     const float2 *__restrict__ tw)
+{
+    using P = QRows<N>;
+    using Y = fftl::Lay<N, P::LP, true>;
+    constexpr int H = N / 4, M = N / 4;
+    extern __shared__ float4 smem4[];
+    float2 *buf = reinterpret_cast<float2 *>(smem4);
+    const int t = threadIdx.x % P::T, b = threadIdx.x / P::T;
+    const long q = (long)blockIdx.x * P::B + b;
+    const bool ok = q < npairs;
+    const long r0 = ok ? 2 * q : 0;                 // global output row (a * H + j)
+    const float *h0 = holo + (r0 / H) * (long)N * N, *h1 = holo + ((r0 + 1) / H) * (long)N * N;
+    const int j0 = (int)(r0 % H), j1 = (int)((r0 + 1) % H);
+    const float xr = (float)(N - 1) / (float)N, yr = (float)(N - 1) / (float)H;
+    float2 v[P::E];
+#pragma unroll
+    for (int i = 0; i < P::E; i++) {
+        const int p = fftl::slot_pos<N, P::T, P::F0>(i, t);
+        v[i] = ok ? make_float2(qpib_tap(h0, N, xr, yr, p, j0), qpib_tap(h1, N, xr, yr, p, j1))
+                  : make_float2(0.f, 0.f);
+    }
+    P::template seq_row<false>(buf, v, tw);
+    float2 *line = buf + b * Y::LINE;
+#pragma unroll
+    for (int i = 0; i < P::E; i++) line[Y::at(fftl::slot_pos<N, P::T, P::RV0>(i, t))] = v[i];
+    __syncthreads();
+    if (!ok) return;
+    if (mag) {
+        for (int x = t; x < N; x += P::T) {
+            const int k = (x + N / 2) % N;          // shifted position x holds bin k
+            const float2 z1 = line[Y::at(k)], z2 = line[Y::at((N - k) % N)];
+            const float2 xa = make_float2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
+            const float2 xb = make_float2(0.5f * (z1.y + z2.y), -0.5f * (z1.x - z2.x));
+            mag[r0 * N + x] = sqrtf(xa.x * xa.x + xa.y * xa.y);
+            mag[(r0 + 1) * N + x] = sqrtf(xb.x * xb.x + xb.y * xb.y);
+        }
+        return;
+    }
+    const int c = *center;
+    for (int x2 = t; x2 < M; x2 += P::T) {
+        const int x = (x2 + M / 2) % M;             // half swap of the window
+        const int ks = x - N / 8 + c;               // column of the shifted spectrum
+        float2 xa = make_float2(0.f, 0.f), xb = make_float2(0.f, 0.f);
+        if (ks >= 0 && ks < N) {
+            const int k = (ks + N / 2) % N;
+            const float2 z1 = line[Y::at(k)], z2 = line[Y::at((N - k) % N)];
+            xa = make_float2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
+            xb = make_float2(0.5f * (z1.y + z2.y), -0.5f * (z1.x - z2.x));
+        }
+        T[r0 * M + x2] = xa;
+        T[(r0 + 1) * M + x2] = xb;
+    }
+}
+
+// Column sums of |X| over the H rows of one hologram's spectrum, in row order, and
+// the first maximum over [int(0.6 N), N), mirrored to N - c when N - c < N/8.
+__global__ void qpib_center_kernel(const float *__restrict__ mag, int N, int H, int *center)
+{
+    __shared__ unsigned long long best[32];
+    unsigned long long key = 0ull;
+    const int lo = (int)(N * 0.6);
+    for (int i = lo + threadIdx.x; i < N; i += blockDim.x) {
+        float s = 0.f;
+        for (int j = 0; j < H; j++) s += mag[(long)j * N + i];
+        const unsigned long long k2 = ((unsigned long long)__float_as_uint(s) << 32) | (unsigned long long)(~(unsigned)i);
+        if (k2 > key) key = k2;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long other = __shfl_xor_sync(0xffffffffu, key, o);
+        if (other > key) key = other;
+    }
+    if ((threadIdx.x & 31) == 0) best[threadIdx.x >> 5] = key;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long k = best[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++)
+            if (best[w] > k) k = best[w];
+        int c = (int)(~(unsigned)(k & 0xffffffffull));
+        if (N - c < (N / 4) / 2) c = N - c;
+        *center = c;
+    }
+}
+
+// Inverse M-point transforms of the window rows, 1/M, conjugate, transposed store:
+// field[a][X * M + Y] from row Y, column X; with bgf the phase / amplitude epilogue
+// of calcWrapPhase instead (cTDM/HilbertTransform.cu:3618-3639).
+template <int M>
+__global__ void __launch_bounds__(Plan<M>::THREADS) qpib_inv_kernel(const float2 *__restrict__ T, long nrows,
+                                                                   float2 *field_out, const float2 *__restrict__ bgf,
+                                                                   long bg_stride, float *phase, float *amp,
+                                                                   const float2 *__restrict__ tw)
+{
+    using P = Plan<M>;
+    extern __shared__ float4 smem4[];
+    float2 *buf = reinterpret_cast<float2 *>(smem4);
+    const long row0 = (long)blockIdx.x * P::B;
+    for (int e = threadIdx.x; e < P::B * M; e += P::THREADS) {
+        const int bb = e / M, x = e - bb * M;
+        const long r = row0 + bb;
+        buf[bb * P::LP + x] = r < nrows ? T[r * M + x] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    float2 v[P::E];
+    P::template seq<true, true, false>(buf, v, tw);
+    const int b = threadIdx.x % P::B, t = threadIdx.x / P::B;
+    const long r = row0 + b;
+    if (r >= nrows) return;
+    const long a = r / M;
+    const int yy = (int)(r % M);
+    const long mm = (long)M * M;
+    const float sc = 1.0f / (float)M;
+#pragma unroll
+    for (int i = 0; i < P::E; i++) {
+        const int X = fftl::slot_pos<M, P::T, P::RV0>(i, t);
+        const float2 f = make_float2(v[i].x * sc, -v[i].y * sc);
+        const long o = a * mm + (long)X * M + yy;
+        if (field_out) {
+            field_out[o] = f;
+        } else {
+            const float2 g = bgf[a * bg_stride + (long)X * M + yy];
+            float ph = atan2f(g.y, g.x) - atan2f(f.y, f.x);
+            if (isnan(ph) || isinf(ph)) ph = 0.f;
+            float am = sqrtf(f.x * f.x + f.y * f.y) / sqrtf(g.x * g.x + g.y * g.y);
+            if (isnan(am) || isinf(am)) am = 0.f;
+            phase[o] = ph;
+            amp[o] = am;
+        }
+    }
+}
+
+template <int N>
+static cudaError_t qpib_rows_launch(const float *holo, int A, float *mag, float2 *T, const int *center, cudaStream_t s)
+{
+    using PR = QRows<N>;
+    if constexpr (N < 64) {
+        return cudaErrorInvalidValue;
+    } else {
+        const size_t smem = fftl::plan_smem_row<PR>();
+        const long npairs = (long)A * (N / 4) / 2;
+        cudaError_t e = set_smem<N>(qpib_rows_kernel<N>, smem);
+        if (e != cudaSuccess) return e;
+        qpib_rows_kernel<N><<<(unsigned)((npairs + PR::B - 1) / PR::B), PR::THREADS, smem, s>>>(holo, npairs, mag, T,
+                                                                                              center, twiddles(N));
+        note_launch();
+        return cudaGetLastError();
+    }
+}
+
+template <int M>
+static cudaError_t qpib_inv_launch(const float2 *T, int A, float2 *field_out, const float2 *bgf, long bg_stride,
+                                   float *phase, float *amp, cudaStream_t s)
+{
+    using P = Plan<M>;
+    const size_t smem = fftl::smem_bytes<M>();
+    cudaError_t e = set_smem<M>(qpib_inv_kernel<M>, smem);
+    if (e != cudaSuccess) return e;
+    const long nrows = (long)A * M;
+    qpib_inv_kernel<M><<<(unsigned)((nrows + P::B - 1) / P::B), P::THREADS, smem, s>>>(T, nrows, field_out, bgf,
+                                                                                      bg_stride, phase, amp,
+                                                                                      twiddles(M));
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t qpib_spectrum_center(const float *holo, int N, float *mag, int *center, cudaStream_t s)
+{
+    cudaError_t e;
+    switch (N) {
+    case 64: e = qpib_rows_launch<64>(holo, 1, mag, nullptr, nullptr, s); break;
+    case 128: e = qpib_rows_launch<128>(holo, 1, mag, nullptr, nullptr, s); break;
+    case 256: e = qpib_rows_launch<256>(holo, 1, mag, nullptr, nullptr, s); break;
+    case 512: e = qpib_rows_launch<512>(holo, 1, mag, nullptr, nullptr, s); break;
+    case 1024: e = qpib_rows_launch<1024>(holo, 1, mag, nullptr, nullptr, s); break;
+    case 2048: e = qpib_rows_launch<2048>(holo, 1, mag, nullptr, nullptr, s); break;
+    default: return cudaErrorInvalidValue;
+    }
+    if (e != cudaSuccess) return e;
+    qpib_center_kernel<<<1, 1024, 0, s>>>(mag, N, N / 4, center);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t qpib_window(const float *holo, int A, int N, const int *center, float2 *T, cudaStream_t s)
+{
+    CTDM_DISPATCH_L(N, qpib_rows_launch, holo, A, nullptr, T, center, s)
+}
+
+cudaError_t qpib_inverse(const float2 *T, int A, int M, float2 *field_out, const float2 *bgf, long bg_stride,
+                         float *phase, float *amp, cudaStream_t s)
+{
+    CTDM_DISPATCH_L(M, qpib_inv_launch, T, A, field_out, bgf, bg_stride, phase, amp, s)
+}
+
 }  // namespace ctdm
 
 namespace ctdm {

@@ -18,6 +18,16 @@ cudaError_t qpi_forward_window(const float *holo, int A, int N, int M, const int
 cudaError_t qpi_inverse_window(float2 *S, int A, int M, float2 *field_out, const float2 *bgf, long bg_stride,
                                float *phase, float *amp, cudaStream_t s);
 
+// QPI Algorithm B --------------------------------------------------------
+// Carrier column of one hologram from its y-downsampled row spectra (mag: N/4 * N
+// floats of scratch; center: device int).
+cudaError_t qpib_spectrum_center(const float *holo, int N, float *mag, int *center, cudaStream_t s);
+// Window rows of A holograms (T: A * (N/4) rows of N/4 complex) for the carrier column.
+cudaError_t qpib_window(const float *holo, int A, int N, const int *center, float2 *T, cudaStream_t s);
+// Inverse window transforms into transposed fields, or phase/amp against bgf.
+cudaError_t qpib_inverse(const float2 *T, int A, int M, float2 *field_out, const float2 *bgf, long bg_stride,
+                         float *phase, float *amp, cudaStream_t s);
+
 // DCT least-squares unwrap -----------------------------------------------
 // A phase maps M x M (float) -> unwrapped maps.  T: A*M*M float scratch.
 // mode 0 = reference IDCT twiddle, 1 = exact DCT-III.

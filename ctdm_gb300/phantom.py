@@ -121,10 +121,13 @@ def rytov_field(ells, n_med, wavelength, n, pixel, ang_x, ang_y):
     return ut.T                                # CopyDataArray transposes: hologram [y, x]
 
 
-def holograms_from_fields(fields, photons, rng):
+def holograms_from_fields(fields, photons, rng, carrier=(0.125, 0.125)):
+    """Off-axis holograms; carrier (cycles per pixel along x, y), by default a quarter
+    of Nyquist on both axes (the 2-D window of Algorithm A); Algorithm B filters along
+    x only and wants the carrier along x, e.g. (0.25, 0)."""
     n = fields.shape[-1]
     yy, xx = np.mgrid[0:n, 0:n]
-    ref = np.exp(-2j * np.pi * (xx / 8.0 + yy / 8.0))   # carrier at a quarter Nyquist
+    ref = np.exp(-2j * np.pi * (carrier[0] * xx + carrier[1] * yy))
     i0 = photons / 2.0
     out = []
     for u in fields:
@@ -157,15 +160,15 @@ def random_cell(rng, fov):
 
 
 def acquisition(n, r, angles, na=0.9, seed=0, pixel=0.1e-6, wavelength=532e-9, n_med=1.337,
-                photons=1000.0, ells=None, scale=1.0, **cell):
+                photons=1000.0, ells=None, scale=1.0, carrier=(0.125, 0.125), **cell):
     """One tomogram: `angles` SP holograms of N x N plus one background."""
     rng = np.random.default_rng(seed)
     if ells is None:
         ells = cell_phantom(rng, scale=scale, **cell)
     ax, ay = cone_angles(angles, na, n_med)
     fields = np.stack([rytov_field(ells, n_med, wavelength, n, pixel, ax[a], ay[a]) for a in range(angles)])
-    holo = holograms_from_fields(fields, photons, rng)
-    bg = holograms_from_fields(np.zeros((1, n, n), np.complex128), photons, rng)[0]
+    holo = holograms_from_fields(fields, photons, rng, carrier)
+    bg = holograms_from_fields(np.zeros((1, n, n), np.complex128), photons, rng, carrier)[0]
     return Acquisition(holo, bg, ax, ay, n, n // 4, r, pixel, wavelength, n_med, ells)
 
 

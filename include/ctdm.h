@@ -56,6 +56,11 @@ typedef struct ctdm_ctx ctdm_ctx;
  * (F2.re != 0 && F2.im != 0) or the Ewald hit mask. */
 #define CTDM_CHECK_REF 0
 #define CTDM_CHECK_MASK 1
+/* Phase retrieval (the reference's QPI_Method values, cTDM/HilbertTransform.cu:27):
+ * Algorithm B = 1-D filtering of y-downsampled rows (the reference's default), Algorithm A
+ * = 2-D window of the hologram spectrum (the default here). */
+#define CTDM_QPI_B 0
+#define CTDM_QPI_A 1
 /* Which unwrapped phase feeds the reconstruction. */
 #define CTDM_METHOD_DCT 0
 #define CTDM_METHOD_FAST 1
@@ -75,6 +80,7 @@ typedef struct {
     double n_med;        /* medium refractive index */
     double wavelength;   /* vacuum wavelength (m) */
     double dx;           /* reconstruction voxel (m) */
+    int qpi_method;      /* reference QPI_Method numbering: CTDM_QPI_B (0) or CTDM_QPI_A (1, default) */
 } ctdm_params;
 
 /* Default parameters (reference defaults where they exist). */
@@ -180,6 +186,13 @@ CTDM_API ctdm_status ctdm_set_loop_scheme(int device, int R, int scheme);
  * background), out: the carrier used. */
 CTDM_API ctdm_status ctdm_qpi(ctdm_ctx *ctx, int N, int M, int A, const float *d_holo, const float *d_bg, int bg_per_angle,
                      int *carrier3, float *d_phase, float *d_amp, void *stream);
+/* QPI Algorithm B (extractQPI_AlgorithmB, cTDM/HilbertTransform.cu:1587-1660): phase and
+ * amplitude maps of M = N/4 side, transposed like the reference's copySharedMem.
+ * center2: in {column, column} (any < 0: detect), out {background column, frame-1
+ * column}: the reference takes frame 1's column from frame 1's own spectrum and every
+ * later frame's from the background's.  Synchronises the stream. */
+CTDM_API ctdm_status ctdm_qpi_b(ctdm_ctx *ctx, int N, int A, const float *d_holo, const float *d_bg, int bg_per_angle,
+                                int *center2, float *d_phase, float *d_amp, void *stream);
 CTDM_API ctdm_status ctdm_unwrap_dct(ctdm_ctx *ctx, int A, int M, int mode, const float *d_phi, float *d_out, void *stream);
 /* FastUnwrapping: d_phi is normalised in place like the reference. */
 CTDM_API ctdm_status ctdm_unwrap_fast(ctdm_ctx *ctx, int A, int M, float *d_phi, float *d_out, void *stream);
@@ -270,6 +283,11 @@ CTDM_API ctdm_status ctdm_fft(ctdm_cfloat *d_data, int rank, const int *dims, in
 CTDM_API void ctdm_set_recon_globals(int recon_size, double n_med, double wavelength_nm, double camera_pixel_um, double mag,
                             int iter_time, int recon_save, const char *save_dir);
 
+/* cTDM/HilbertTransform.cu:1587 (declared in HilbertTransform.cuh) -- host SP/BG
+ * holograms (Nx*Ny float, Nx == Ny), device fields out (Nx/4 * Ny/4).  frame == 1
+ * detects the carrier columns (kept per device for the later frames). */
+CTDM_API void extractQPI_AlgorithmB(float *SP, float *BG, ctdm_cfloat *cuSP_FFT, ctdm_cfloat *cuBG_FFT, int Nx, int Ny,
+                                    int frame);
 /* cTDM/DCT_Unwrapping.cuh:106 -- device pointers, sizeX == sizeY. */
 CTDM_API void DCT_UWLS_Unwrapped(float *ImgDst, float *ImgSrc, int sizeX, int sizeY);
 /* cTDM/FastUnwrapping.cuh:12 -- (src, dst) order; src is normalised in place. */

@@ -260,6 +260,90 @@ void or_qpi_field(const float *holo, int n, int m, int r, int c, int radius, cpl
     free(a);
 }
 
+/* ------------------------------------------------------------------------- */
+/* QPI Algorithm B                                                            */
+/* ------------------------------------------------------------------------- */
+
+/* The y-downsampled row spectra of Algorithm B (extractQPI_AlgorithmB and
+ * sequence1DFFT, cTDM/HilbertTransform.cu:1587-1660): bilinear resample of the N x N
+ * hologram to N x N/4 by the tap rule of bilinear_interpolation_kernel (:3658-3723;
+ * x ratio (N-1)/N, y ratio (N-1)/(N/4), taps past the edge read 0), an N-point
+ * forward transform of every row, then the swap of the two x halves (shiftArray
+ * :1745-1758).  spec: N/4 rows of N. */
+static void qpib_spectra(const float *holo, int n, cplx *spec)
+{
+    const int h = n / 4;
+    const float xr = (float)(n - 1) / (float)n, yr = (float)(n - 1) / (float)h;
+    for (int j = 0; j < h; j++) {
+        cplx *row = spec + (long)j * n;
+        for (int i = 0; i < n; i++) {
+            int ix = (int)(xr * (float)i), iy = (int)(yr * (float)j);
+            double a = (double)(xr * (float)i - (float)ix), b = (double)(yr * (float)j - (float)iy);
+            double d00 = (ix < n && iy < n) ? holo[(long)iy * n + ix] : 0;
+            double d10 = (ix + 1 < n && iy < n) ? holo[(long)iy * n + ix + 1] : 0;
+            double d01 = (ix < n && iy + 1 < n) ? holo[(long)(iy + 1) * n + ix] : 0;
+            double d11 = (ix + 1 < n && iy + 1 < n) ? holo[(long)(iy + 1) * n + ix + 1] : 0;
+            double t1 = a * d10 + (-d00 * a + d00);
+            double t2 = a * d11 + (-d01 * a + d01);
+            row[i] = b * t2 + (-t1 * b + t1);
+        }
+        or_fft1d(row, n, -1);
+        for (int i = 0; i < n / 2; i++) {
+            cplx t = row[i];
+            row[i] = row[i + n / 2];
+            row[i + n / 2] = t;
+        }
+    }
+}
+
+/* Carrier column of Algorithm B (frame 1 of sequence1DFFT, :1626-1641): the column
+ * sums of |X| over the N/4 rows (HistogramFT :1727-1743), the first maximum over
+ * columns [int(0.6 N), N) (thrust::max_element), mirrored to N - c when N - c < N/8. */
+int or_qpib_center(const float *holo, int n)
+{
+    const int h = n / 4;
+    cplx *spec = (cplx *)malloc(sizeof(cplx) * (long)n * h);
+    qpib_spectra(holo, n, spec);
+    int best = (int)(n * 0.6);
+    double bv = -1.0;
+    for (int i = (int)(n * 0.6); i < n; i++) {
+        double s = 0;
+        for (int j = 0; j < h; j++) s += cabs(spec[i + (long)j * n]);
+        if (s > bv) { bv = s; best = i; }
+    }
+    free(spec);
+    if (n - best < (n / 4) / 2) best = n - best;
+    return best;
+}
+
+/* Algorithm B field (:1643-1659): N/4 columns of each row spectrum from c - N/8
+ * (CropFTdomain :1800-1812; columns outside the spectrum read 0, where the reference
+ * would read past its array), swap of the halves (N/4), inverse N/4-point transform,
+ * scale 1/(N/4) with conjugation and a transpose (copySharedMem :1704-1724).
+ * field: M x M, M = N/4, field[X * M + Y] from row Y, column X. */
+void or_qpib_field(const float *holo, int n, int center, cplx *field)
+{
+    const int m = n / 4;
+    cplx *spec = (cplx *)malloc(sizeof(cplx) * (long)n * m);
+    cplx *row = (cplx *)malloc(sizeof(cplx) * m);
+    qpib_spectra(holo, n, spec);
+    for (int y = 0; y < m; y++) {
+        for (int x = 0; x < m; x++) {
+            int k = x - n / 8 + center;
+            row[x] = (k >= 0 && k < n) ? spec[k + (long)y * n] : 0;
+        }
+        for (int x = 0; x < m / 2; x++) {
+            cplx t = row[x];
+            row[x] = row[x + m / 2];
+            row[x + m / 2] = t;
+        }
+        or_fft1d(row, m, +1);
+        for (int x = 0; x < m; x++) field[(long)x * m + y] = conj(row[x] / (double)m);
+    }
+    free(row);
+    free(spec);
+}
+
 /* calcWrapPhase (cTDM/HilbertTransform.cu:3618-3639): phase = arg BG - arg SP (not
  * rewrapped), amp = |SP| / |BG|; NaN/inf -> 0 for both. */
 void or_wrap_phase(const cplx *sp, const cplx *bg, int count, double *phase, double *amp)
@@ -940,6 +1024,7 @@ typedef struct {
     int check_mode;   /* 0 ref_compat predicate, 1 hit mask */
     int carrier_r, carrier_c, carrier_radius; /* < 0: detect from the background */
     double fm0, df, dx, k2, n_med;
+    int qpi_method;   /* reference QPI_Method numbering: 0 Algorithm B, 1 Algorithm A */
 } or_params;
 
 /* Phase and amplitude stacks for A angles (R*R each, after resize+crop and
@@ -948,19 +1033,42 @@ void or_front_end(const or_params *p, const float *sp, const float *bg, int na, 
                   double *phase_out, double *amp_out, int *carrier /* r, c, radius */)
 {
     int n = p->n, m = p->m, r = p->r;
+    const int method_b = p->qpi_method == 0;
     int cr = p->carrier_r, cc = p->carrier_c, rad = p->carrier_radius;
-    if (cr < 0 || cc < 0 || rad < 0) or_qpi_carrier(bg, n, &cr, &cc, &rad);
-    if (carrier) { carrier[0] = cr; carrier[1] = cc; carrier[2] = rad; }
+    int cb = -1, cs0 = -1;   /* Algorithm B: carrier columns of the background and of frame 1 */
+    if (method_b) {
+        m = n / 4;
+        if (cc >= 0) {
+            cb = cs0 = cc;
+        } else {
+            /* frame 1 of sequence1DFFT computes the column from its own spectrum, the
+             * SP first and then the BG; later frames keep the BG's */
+            cs0 = or_qpib_center(sp, n);
+            cb = or_qpib_center(bg, n);
+        }
+        if (carrier) { carrier[0] = cb; carrier[1] = cs0; carrier[2] = -1; }
+    } else {
+        if (cr < 0 || cc < 0 || rad < 0) or_qpi_carrier(bg, n, &cr, &cc, &rad);
+        if (carrier) { carrier[0] = cr; carrier[1] = cc; carrier[2] = rad; }
+    }
     long mm = (long)m * m;
     cplx *bgf = (cplx *)malloc(sizeof(cplx) * mm);
-    if (!bg_per_angle) or_qpi_field(bg, n, m, cr, cc, rad, bgf);
+    if (!bg_per_angle) {
+        if (method_b) or_qpib_field(bg, n, cb, bgf);
+        else or_qpi_field(bg, n, m, cr, cc, rad, bgf);
+    }
     for (int a = 0; a < na; a++) {
         cplx *spf = (cplx *)malloc(sizeof(cplx) * mm);
         double *ph = (double *)malloc(sizeof(double) * mm), *am = (double *)malloc(sizeof(double) * mm);
         double *uw = (double *)malloc(sizeof(double) * mm);
         double *pr = (double *)malloc(sizeof(double) * r * r), *ar = (double *)malloc(sizeof(double) * r * r);
-        or_qpi_field(sp + (long)a * n * n, n, m, cr, cc, rad, spf);
-        if (bg_per_angle) or_qpi_field(bg + (long)a * n * n, n, m, cr, cc, rad, bgf);
+        if (method_b) {
+            or_qpib_field(sp + (long)a * n * n, n, a == 0 ? cs0 : cb, spf);
+            if (bg_per_angle) or_qpib_field(bg + (long)a * n * n, n, cb, bgf);
+        } else {
+            or_qpi_field(sp + (long)a * n * n, n, m, cr, cc, rad, spf);
+            if (bg_per_angle) or_qpi_field(bg + (long)a * n * n, n, m, cr, cc, rad, bgf);
+        }
         or_wrap_phase(spf, bgf, (int)mm, ph, am);
         or_dct_unwrap(ph, m, m, p->unwrap_mode, uw);
         or_resize_crop(uw, am, m, m, n, n, r, pr, ar);

@@ -58,7 +58,7 @@ class Params(ctypes.Structure):
         ("unwrap_mode", ctypes.c_int), ("check_mode", ctypes.c_int),
         ("carrier_r", ctypes.c_int), ("carrier_c", ctypes.c_int), ("carrier_radius", ctypes.c_int),
         ("fm0", ctypes.c_double), ("df", ctypes.c_double), ("dx", ctypes.c_double),
-        ("k2", ctypes.c_double), ("n_med", ctypes.c_double),
+        ("k2", ctypes.c_double), ("n_med", ctypes.c_double), ("qpi_method", ctypes.c_int),
     ]
 
 
@@ -101,6 +101,21 @@ def qpi_field(holo, m, r, c, radius):
     holo = _f32(holo)
     out = np.zeros((m, m), np.complex128)
     lib().or_qpi_field(_p(holo), holo.shape[0], int(m), int(r), int(c), int(radius), _p(out))
+    return out
+
+
+def qpib_center(holo):
+    """Algorithm B carrier column from the column histogram of the row spectra."""
+    holo = _f32(holo)
+    return int(lib().or_qpib_center(_p(holo), holo.shape[0]))
+
+
+def qpib_field(holo, center):
+    """Algorithm B field (M x M, M = N/4) for the given carrier column."""
+    holo = _f32(holo)
+    m = holo.shape[0] // 4
+    out = np.zeros((m, m), np.complex128)
+    lib().or_qpib_field(_p(holo), holo.shape[0], int(center), _p(out))
     return out
 
 
@@ -238,8 +253,10 @@ def positivity(F2, counts, iters, k2, n_med, check_mode=0):
     return out
 
 
-def make_params(n, m, r, iters, fm0, df, dx, k2, n_med, unwrap_mode=0, check_mode=0, carrier=None):
+def make_params(n, m, r, iters, fm0, df, dx, k2, n_med, unwrap_mode=0, check_mode=0, carrier=None, qpi_method=1):
+    """qpi_method in the reference's numbering: 0 Algorithm B, 1 Algorithm A."""
     p = Params()
+    p.qpi_method = qpi_method
     p.n, p.m, p.r, p.iters = n, m, r, iters
     p.unwrap_mode, p.check_mode = unwrap_mode, check_mode
     cr, cc, rad = carrier if carrier is not None else (-1, -1, -1)

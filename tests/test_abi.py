@@ -47,7 +47,8 @@ def test_params_struct_layout(lib):
     _lib.load().ctdm_params_default(ctypes.byref(p))
     assert p.n_holo == 1024 and p.r_vol == 256 and p.iterations == 101
     assert p.carrier_r == -1 and abs(p.n_med - 1.333) < 1e-12
-    assert ctypes.sizeof(_lib.Params) == 12 * 4 + 3 * 8
+    assert p.qpi_method == 1   # Algorithm A by default (CTDM_QPI_A)
+    assert ctypes.sizeof(_lib.Params) == 12 * 4 + 3 * 8 + 8   # trailing int padded to 8
 
 
 def test_version_and_error_without_gpu(lib):
