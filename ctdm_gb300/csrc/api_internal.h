@@ -1,6 +1,7 @@
-// Internal interface between the C-ABI runtime (ctdm_api.cu) and the batch
-// scheduler (batch.cu).  Not part of the public header.
+// Internal interface between the C-ABI runtime (ctdm_api.cu), the batch scheduler
+// (batch.cu) and the job driver (driver.cu).  Not part of the public header.
 #pragma once
+#include <string>
 #include <vector>
 
 #include "ctdm.h"
@@ -17,8 +18,13 @@ ctdm_status run_pipeline(ctdm_ctx *c, const ctdm_params *p, int A, const float *
 void make_geometry(const float *angx, const float *angy, int A, double fm0, double df, std::vector<AngleGeom> &g);
 ctdm_status fail_invalid(const char *msg);
 ctdm_status fail_cuda(cudaError_t e, const char *what);
+ctdm_status fail_io(const std::string &msg);
 void clear_error();
 int max_angles();
 // Counts kernels a graph replay launches (the launch counter of ctdm_launch_count).
 void note_launches(unsigned long long n);
+// BatchRecon on host R x R stacks with the globals of ctdm_set_recon_globals; writes
+// the .rimap file (the status-returning form of the reference-named BatchRecon).
+ctdm_status batch_recon(const float *PhaseStack, const float *AmpStack, const float *sampleAngleRadX,
+                        const float *sampleAngleRadY, int ReconFrame);
 }  // namespace ctdm

@@ -772,6 +772,11 @@ void make_geometry(const float *angx, const float *angy, int A, double fm0, doub
 }
 ctdm_status fail_invalid(const char *msg) { return invalid("%s", msg); }
 ctdm_status fail_cuda(cudaError_t e, const char *what) { return cuda_fail(e, what); }
+ctdm_status fail_io(const std::string &msg)
+{
+    g_err = msg;
+    return CTDM_ERR_IO;
+}
 void clear_error() { g_err.clear(); }
 int max_angles() { return kMaxAngles; }
 }  // namespace ctdm
@@ -1233,22 +1238,16 @@ extern "C" void cuFFT2D(ctdm_cfloat *ImgArray, int sizeX, int sizeY, int dir)
     finish("cuFFT2D");
 }
 
-static bool write_file(const std::string &path, const void *data, size_t bytes)
-{
-    FILE *f = fopen(path.c_str(), "wb");
-    if (!f) return false;
-    const bool ok = fwrite(data, 1, bytes, f) == bytes;
-    fclose(f);
-    return ok;
-}
-
-extern "C" void BatchRecon(float *PhaseStack, float *AmpStack, float *sampleAngleRadX, float *sampleAngleRadY,
-                           int ReconFrame)
+namespace ctdm {
+// BatchRecon with the globals above (cTDM/HilbertTransform.cu:1825-2047): host R x R
+// stacks and angles in, 3D-RI-*.rimap written into SaveDir.
+ctdm_status batch_recon(const float *PhaseStack, const float *AmpStack, const float *sampleAngleRadX,
+                        const float *sampleAngleRadY, int ReconFrame)
 {
     ctdm_ctx *c = default_ctx();
-    if (!c) return;
+    if (!c) return invalid("BatchRecon: no CUDA device");
     const int R = g_recon;
-    if (!ok_volume(R) || ReconFrame < 1 || ReconFrame > kMaxAngles) { invalid("BatchRecon: size unsupported"); return; }
+    if (!ok_volume(R) || ReconFrame < 1 || ReconFrame > kMaxAngles) return invalid("BatchRecon: size unsupported");
     const long rr = (long)R * R, r3 = rr * R;
     // constants of BatchRecon (cTDM/HilbertTransform.cu:1839-1862)
     const double lambda = g_wavelength_nm * 1e-9;
@@ -1264,11 +1263,16 @@ extern "C" void BatchRecon(float *PhaseStack, float *AmpStack, float *sampleAngl
         cudaMalloc(&U, sizeof(float2) * ReconFrame * rr) != cudaSuccess ||
         cudaMalloc(&F2, sizeof(float2) * r3) != cudaSuccess || cudaMalloc(&ri, sizeof(float2) * r3) != cudaSuccess) {
         cleanup();
+        cudaGetLastError();
         set_err("BatchRecon: device allocation failed");
-        return;
+        return CTDM_ERR_NOMEM;
     }
-    cudaMemcpy(ph, PhaseStack, sizeof(float) * ReconFrame * rr, cudaMemcpyHostToDevice);
-    cudaMemcpy(am, AmpStack, sizeof(float) * ReconFrame * rr, cudaMemcpyHostToDevice);
+    cudaError_t e = cudaMemcpy(ph, PhaseStack, sizeof(float) * ReconFrame * rr, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(am, AmpStack, sizeof(float) * ReconFrame * rr, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cleanup();
+        return cuda_fail(e, "BatchRecon upload");
+    }
     ctdm_status st = ctdm_stack_spectra(c, ReconFrame, R, ph, am, reinterpret_cast<ctdm_cfloat *>(U), 0);
     if (st == CTDM_OK)
         st = ctdm_map_ewald(c, ReconFrame, R, reinterpret_cast<ctdm_cfloat *>(U), sampleAngleRadX, sampleAngleRadY, fm0,
@@ -1276,27 +1280,20 @@ extern "C" void BatchRecon(float *PhaseStack, float *AmpStack, float *sampleAngl
     if (st == CTDM_OK)
         st = ctdm_positivity(c, R, g_iter_time + 1, CTDM_CHECK_REF, k * k, g_nmed, reinterpret_cast<ctdm_cfloat *>(F2),
                              nullptr, reinterpret_cast<ctdm_cfloat *>(ri), 0);
-    if (st != CTDM_OK) { cleanup(); return; }
-    std::vector<float2> host(r3);
-    if (cudaMemcpy(host.data(), ri, sizeof(float2) * r3, cudaMemcpyDeviceToHost) != cudaSuccess) {
+    if (st != CTDM_OK) {
         cleanup();
-        set_err("BatchRecon: download failed");
-        return;
+        return st;
     }
+    std::vector<ctdm_cfloat> host(r3);
+    e = cudaMemcpy(host.data(), ri, sizeof(float2) * r3, cudaMemcpyDeviceToHost);
     cleanup();
-    // export (cTDM/HilbertTransform.cu:2013-2041): raw complex64, or the real / imaginary part
-    char name[256];
-    bool ok = true;
-    if (g_recon_save == 0) {
-        snprintf(name, sizeof name, "/3D-RI-Complex_%dx%dx%d.rimap", R, R, R);
-        ok = write_file(g_save_dir + name, host.data(), sizeof(float2) * r3);
-    } else {
-        std::vector<float> part(r3);
-        for (long i = 0; i < r3; i++) part[i] = g_recon_save == 1 ? host[i].x : host[i].y;
-        snprintf(name, sizeof name, g_recon_save == 1 ? "/3D-RI-Real_%dx%dx%d.rimap" : "/3D-RI-Imag_%dx%dx%d.rimap", R,
-                 R, R);
-        ok = write_file(g_save_dir + name, part.data(), sizeof(float) * r3);
-    }
-    if (!ok) { set_err("BatchRecon: cannot write %s%s", g_save_dir.c_str(), name); return; }
-    g_err.clear();
+    if (e != cudaSuccess) return cuda_fail(e, "BatchRecon download");
+    return ctdm_write_rimap(g_save_dir.c_str(), R, g_recon_save, host.data());
+}
+}  // namespace ctdm
+
+extern "C" void BatchRecon(float *PhaseStack, float *AmpStack, float *sampleAngleRadX, float *sampleAngleRadY,
+                           int ReconFrame)
+{
+    batch_recon(PhaseStack, AmpStack, sampleAngleRadX, sampleAngleRadY, ReconFrame);
 }

@@ -486,6 +486,48 @@ static cudaError_t qpib_inv_launch(const float2 *T, int A, float2 *field_out, co
     return cudaGetLastError();
 }
 
+// ------------------------------------------------------------ angle camera (AngCal_GPU)
+// AngCal_GPU (cTDM/HilbertTransform.cu:2920-2983): forward 2-D transform of the
+// angle-camera image, quadrant swap, log10 |X| with NaN/inf -> 0 (cufftComplex2Real
+// :2986-2996), first maximum over the flattened range [int(0.53 N^2), int(0.79 N^2)).
+// spec: the transformed image (N x N complex, unshifted).  pos: device int (index).
+__device__ __forceinline__ unsigned order_key(float v)
+{
+    const unsigned u = __float_as_uint(v);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);   // unsigned order = float order
+}
+
+__global__ void angcal_argmax_kernel(const float2 *__restrict__ spec, int N, long lo, long hi, unsigned long long *key)
+{
+    unsigned long long best = 0ull;
+    for (long e = lo + blockIdx.x * (long)blockDim.x + threadIdx.x; e < hi; e += (long)gridDim.x * blockDim.x) {
+        const int xs = (int)(e % N), ys = (int)(e / N);
+        const float2 v = spec[(long)((xs + N / 2) % N) + (long)N * ((ys + N / 2) % N)];
+        float m = log10f(sqrtf(v.x * v.x + v.y * v.y));
+        if (isnan(m) || isinf(m)) m = 0.f;
+        const unsigned long long k = ((unsigned long long)order_key(m) << 32) | (unsigned long long)(~(unsigned)e);
+        if (k > best) best = k;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long other = __shfl_xor_sync(0xffffffffu, best, o);
+        if (other > best) best = other;
+    }
+    if ((threadIdx.x & 31) == 0) atomicMax(key, best);
+}
+
+cudaError_t angcal_peak(const float *img, int N, float2 *scratch, unsigned long long *key, cudaStream_t s)
+{
+    const long n2 = (long)N * N;
+    real_to_complex_kernel<<<1024, 256, 0, s>>>(img, scratch, n2); note_launch();
+    cudaError_t e = fft_rows(scratch, N, N, false, s);
+    if (e == cudaSuccess) e = fft_cols(scratch, N, N, N, 0, N, false, s);
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(key, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return e;
+    angcal_argmax_kernel<<<256, 256, 0, s>>>(scratch, N, (long)(n2 * 0.53), (long)(n2 * 0.79), key); note_launch();
+    return cudaGetLastError();
+}
+
 cudaError_t qpib_spectrum_center(const float *holo, int N, float *mag, int *center, cudaStream_t s)
 {
     cudaError_t e;

@@ -122,6 +122,31 @@ __global__ void __launch_bounds__(256) prep_kernel(const float *__restrict__ pha
     }
 }
 
+// bilinear_interpolation_kernel M -> N over whole maps (the per-frame resize of the
+// job driver, cTDM/HilbertTransform.cu:1044-1047), phase and amplitude.
+__global__ void resize_maps_kernel(const float *__restrict__ ph, const float *__restrict__ am, int A, int M, int N,
+                                   float *ph_out, float *am_out)
+{
+    const long nn = (long)N * N, total = (long)A * nn;
+    const float xr = (float)(M - 1) / (float)N;
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
+        const long a = e / nn;
+        const int p = (int)(e - a * nn), i = p % N, j = p / N;
+        ph_out[e] = resize_at(ph + a * (long)M * M, M, xr, i, j);
+        am_out[e] = resize_at(am + a * (long)M * M, M, xr, i, j);
+    }
+}
+
+cudaError_t resize_maps(const float *ph, const float *am, int A, int M, int N, float *ph_out, float *am_out,
+                        cudaStream_t s)
+{
+    long blocks = ((long)A * N * N + 255) / 256;
+    if (blocks > 8192) blocks = 8192;
+    resize_maps_kernel<<<(unsigned)blocks, 256, 0, s>>>(ph, am, A, M, N, ph_out, am_out);
+    note_launch();
+    return cudaGetLastError();
+}
+
 cudaError_t prep_rytov(const float *phase, const float *amp, int A, int M, int N, int R, float2 *U0, cudaStream_t s)
 {
     dim3 grid((R + 31) / 32, (R + 31) / 32, A), block(32, 8);

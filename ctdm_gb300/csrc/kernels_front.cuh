@@ -28,6 +28,13 @@ cudaError_t qpib_window(const float *holo, int A, int N, const int *center, floa
 cudaError_t qpib_inverse(const float2 *T, int A, int M, float2 *field_out, const float2 *bgf, long bg_stride,
                          float *phase, float *amp, cudaStream_t s);
 
+// Angle camera: index of the spectrum peak of AngCal_GPU in *key's low word
+// (complemented; see angcal_peak).  scratch: N*N complex.
+cudaError_t angcal_peak(const float *img, int N, float2 *scratch, unsigned long long *key, cudaStream_t s);
+// Whole-map bilinear resize M -> N of phase and amplitude stacks.
+cudaError_t resize_maps(const float *ph, const float *am, int A, int M, int N, float *ph_out, float *am_out,
+                        cudaStream_t s);
+
 // DCT least-squares unwrap -----------------------------------------------
 // A phase maps M x M (float) -> unwrapped maps.  T: A*M*M float scratch.
 // mode 0 = reference IDCT twiddle, 1 = exact DCT-III.

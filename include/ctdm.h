@@ -274,6 +274,72 @@ CTDM_API ctdm_status ctdm_unwrap_dct_noalloc(int A, int M, int mode, const float
  * fastest-first; inverse = 1 uses exp(+i), no scaling. */
 CTDM_API ctdm_status ctdm_fft(ctdm_cfloat *d_data, int rank, const int *dims, int batch, int inverse, void *stream);
 
+/* --- on-disk formats and the JobList driver (cTDM/HilbertTransform.cu:70-175,
+ * 327-1230, 1316-1544, 2437-2455, 2680-2731) ------------------------------------- */
+/* 8-bit grey BMP as the reference's read_bmp stores it: header width at byte 18 read as
+ * nr, height at 22 as nc, palette skipped, nr lines of nc bytes (padded to 4), bottom
+ * line first, image[j * nr + i] = byte j of line i counted from the top.  image NULL:
+ * only *width / *height are filled (bmp_header). */
+CTDM_API ctdm_status ctdm_read_bmp(const char *path, int *width, int *height, uint8_t *image);
+/* Per-frame map file (outputImg / openImage): 1-byte status, angle x and y (float64),
+ * size x and y (int32), then size_x * size_y (phase, amp) float32 pairs, no padding. */
+CTDM_API ctdm_status ctdm_write_phimap(const char *path, int status, double angle_x, double angle_y, int size_x,
+                                       int size_y, const float *phase, const float *amp);
+/* phase / amp may be NULL (header only). */
+CTDM_API ctdm_status ctdm_read_phimap(const char *path, int *status, double *angle_x, double *angle_y, int *size_x,
+                                      int *size_y, float *phase, float *amp);
+/* dir/3D-RI-{Complex,Real,Imag}_RxRxR.rimap from a host R^3 volume; save_mode 0 complex64,
+ * 1 real part, 2 imaginary part (float32). */
+CTDM_API ctdm_status ctdm_write_rimap(const char *dir, int R, int save_mode, const ctdm_cfloat *h_ri);
+/* Frame check (checkArray on the centre half of an N x N phase map with limit_std and
+ * limit_range when resize_flag = 1, on the whole map with 0.5 and 5 pi when 0):
+ * 1 when the frame is rejected. */
+CTDM_API int ctdm_check_frame(const float *phase, int N, int resize_flag, double limit_std, double limit_range);
+/* Illumination angle from an N x N angle-camera image (row-major, x fastest): the
+ * first maximum of log10 |FFT2| (quadrant-swapped) over flat indices
+ * [int(0.53 N^2), int(0.79 N^2)), fx = (N/2 - 1 - column) / (N pixel), sin theta =
+ * mag fx n_med^-1 wavelength, angle = -sign(sin theta) |asin| (AngCal_GPU,
+ * cTDM/HilbertTransform.cu:2920-2983, whose 511 and 1024 are N/2 - 1 and N at N = 1024).
+ * peak (may be NULL) receives the flat index of the maximum. */
+CTDM_API ctdm_status ctdm_angle_from_image(const float *h_img, int N, double n_med, double wavelength_nm, double mag,
+                                           double camera_pixel_um, float *angle, long *peak);
+
+/* One job of a JobList: the 20 ordered key=value fields of a parameter file
+ * (cTDM/HilbertTransform.cu:96-120) and two optional trailing keys, QPI_Method and
+ * IterTime, which the reference fixes at compile time (:25, :35). */
+typedef struct {
+    char sp_dir[256], bg_dir[256], ang_dir[256], save_dir[256];
+    int row_pts[2], col_pts[2];
+    int recon_flag;        /* 0 maps only, 1 maps + reconstruction, 2 reconstruction from saved maps */
+    int recon_save;        /* .rimap content: 0 complex, 1 real, 2 imaginary */
+    int size_type;         /* 0: R = 256, 1: R = 512 */
+    int resize_flag;       /* 1: centre R x R window of the map, 0: bilinear resize to R */
+    double n_med, mag, camera_pixel_um, wavelength_nm;
+    int save_phase_stack, save_amp_stack; /* 1: also write Phase%03d_NxN.raw / Amp%03d_NxN.raw */
+    double criteria_range, criteria_std;
+    int qpi_method;        /* reference numbering: 0 Algorithm B (default), 1 Algorithm A */
+    int iter_time;         /* BatchRecon runs iter_time + 1 loop bodies (default 100) */
+} ctdm_job_file;
+
+typedef struct {
+    int frames;            /* frames found (Buffer*.bmp pairs, or saved buffer*.phimap files) */
+    int rejected;          /* frames that failed the check */
+    int recon_frames;      /* frames reconstructed (0: no reconstruction ran) */
+    int n_holo;            /* hologram side */
+    int recon_size;        /* volume side */
+} ctdm_job_result;
+
+/* The reference's defaults (cTDM/HilbertTransform.cu:11-35). */
+CTDM_API void ctdm_job_defaults(ctdm_job_file *job);
+/* Parses one parameter file (fields in the reference's order; spaces after '=' are
+ * allowed; values end at white space). */
+CTDM_API ctdm_status ctdm_parse_job_file(const char *path, ctdm_job_file *job);
+/* Runs one job like HilbertTransform with SpeedTestFlag = 0 (the mode that writes maps
+ * and reconstructs): all frames' QPI, unwrapping and resizing run batched on the GPU;
+ * buffer%03d.phimap per frame; reconstruction of the frames that pass the check.
+ * Folders use '/'.  result may be NULL. */
+CTDM_API ctdm_status ctdm_run_job(const ctdm_job_file *job, ctdm_job_result *result);
+
 /* ------------------------------------------------------------------------- */
 /* Drop-in replacements for the reference entry points (void, default stream) */
 /* ------------------------------------------------------------------------- */
@@ -316,6 +382,21 @@ CTDM_API void check_F_3D(ctdm_cfloat *F, ctdm_cfloat *F2, int Image_Width, int I
 CTDM_API void cuFFT3D(ctdm_cfloat *ImgArray, int sizeX, int sizeY, int sizeZ, int dir);
 /* cTDM/FFT.cuh:25 -- dir -1 forward, +1 inverse scaled by 1/(XY) and conjugated. */
 CTDM_API void cuFFT2D(ctdm_cfloat *ImgArray, int sizeX, int sizeY, int dir);
+/* cTDM/HilbertTransform.cu:70 -- each white-space separated entry of the job list is a
+ * parameter file, parsed and run in turn.  Returns 0 when the list cannot be opened,
+ * else 1; a failed job leaves its message in ctdm_last_error and the next job runs. */
+CTDM_API int scriptFileRead(char *script);
+/* cTDM/HilbertTransform.cuh:127 -- one job with the folders given and every other
+ * field from the parameter file scriptFileRead parsed last (the reference's file-scope
+ * globals), or the defaults.  rowSize, colSize, StartNo, SpaceNo and EndNo are not
+ * used (the reference uses them only on its unreachable half-size branch). */
+CTDM_API void HilbertTransform(char *SPDir, char *BGDir, char *AngDir, char *SaveDir, int rowPts[], int colPts[],
+                               int rowSize, int colSize, int StartNo, int SpaceNo, int EndNo);
+/* cTDM/HilbertTransform.cu:2920 -- host N x N angle image (sizeX == sizeY), optics
+ * from the last parsed parameter file or the defaults. */
+CTDM_API float AngCal_GPU(float *src, int sizeX, int sizeY, int frame, int totalFrame);
+/* cTDM/HilbertTransform.cu:3056 -- nonzero when the std or range exceeds its limit. */
+CTDM_API int checkArray(float *array2D, float limitSTD, float limitRange, int size);
 /* cTDM/HilbertTransform.cuh:132 -- host stacks (R*R*frames) and angles (radians);
  * reconstructs with the globals above and writes 3D-RI-*.rimap into SaveDir. */
 CTDM_API void BatchRecon(float *PhaseStack, float *AmpStack, float *sampleAngleRadX, float *sampleAngleRadY, int ReconFrame);
