@@ -31,6 +31,24 @@ class Job(ctypes.Structure):
     ]
 
 
+class JobFile(ctypes.Structure):
+    """ctdm_job_file (include/ctdm.h): one parameter file of a JobList."""
+    _fields_ = [
+        ("sp_dir", ctypes.c_char * 256), ("bg_dir", ctypes.c_char * 256), ("ang_dir", ctypes.c_char * 256),
+        ("save_dir", ctypes.c_char * 256), ("row_pts", c_int * 2), ("col_pts", c_int * 2),
+        ("recon_flag", c_int), ("recon_save", c_int), ("size_type", c_int), ("resize_flag", c_int),
+        ("n_med", c_double), ("mag", c_double), ("camera_pixel_um", c_double), ("wavelength_nm", c_double),
+        ("save_phase_stack", c_int), ("save_amp_stack", c_int), ("criteria_range", c_double),
+        ("criteria_std", c_double), ("qpi_method", c_int), ("iter_time", c_int),
+    ]
+
+
+class JobResult(ctypes.Structure):
+    """ctdm_job_result (include/ctdm.h)."""
+    _fields_ = [("frames", c_int), ("rejected", c_int), ("recon_frames", c_int), ("n_holo", c_int),
+                ("recon_size", c_int)]
+
+
 # name -> (restype, argtypes)
 _SIGS = {
     "ctdm_params_default": (None, [ctypes.POINTER(Params)]),
@@ -106,6 +124,22 @@ _SIGS = {
     "cuFFT3D": (None, [c_void_p, c_int, c_int, c_int, c_int]),
     "cuFFT2D": (None, [c_void_p, c_int, c_int, c_int]),
     "BatchRecon": (None, [c_void_p, c_void_p, c_void_p, c_void_p, c_int]),
+    "ctdm_read_bmp": (c_int, [ctypes.c_char_p, P_int, P_int, c_void_p]),
+    "ctdm_write_phimap": (c_int, [ctypes.c_char_p, c_int, c_double, c_double, c_int, c_int, c_void_p, c_void_p]),
+    "ctdm_read_phimap": (c_int, [ctypes.c_char_p, P_int, ctypes.POINTER(c_double), ctypes.POINTER(c_double), P_int,
+                                 P_int, c_void_p, c_void_p]),
+    "ctdm_write_rimap": (c_int, [ctypes.c_char_p, c_int, c_int, c_void_p]),
+    "ctdm_check_frame": (c_int, [c_void_p, c_int, c_int, c_double, c_double]),
+    "ctdm_angle_from_image": (c_int, [c_void_p, c_int, c_double, c_double, c_double, c_double,
+                                      ctypes.POINTER(c_float), ctypes.POINTER(ctypes.c_long)]),
+    "ctdm_job_defaults": (None, [ctypes.POINTER(JobFile)]),
+    "ctdm_parse_job_file": (c_int, [ctypes.c_char_p, ctypes.POINTER(JobFile)]),
+    "ctdm_run_job": (c_int, [ctypes.POINTER(JobFile), ctypes.POINTER(JobResult)]),
+    "scriptFileRead": (c_int, [ctypes.c_char_p]),
+    "HilbertTransform": (None, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, P_int, P_int,
+                                c_int, c_int, c_int, c_int, c_int]),
+    "AngCal_GPU": (c_float, [c_void_p, c_int, c_int, c_int, c_int]),
+    "checkArray": (c_int, [c_void_p, c_float, c_float, c_int]),
 }
 
 EXPORTED = tuple(_SIGS)

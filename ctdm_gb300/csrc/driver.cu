@@ -550,8 +550,10 @@ ctdm_status process_frames(const ctdm_job_file &jb, int R, ctdm_job_result &r, S
     const long nn = (long)N * N, mm = (long)M * M, rr = (long)R * R;
     const bool xy = is_dir(join(jb.ang_dir, "X")) && is_dir(join(jb.ang_dir, "Y"));
     const bool alg_b = jb.qpi_method == CTDM_QPI_B;
-    // frames per batch: 256 MiB of sample holograms on the device
-    const int C = std::max(1, std::min({F, (int)((1l << 28) / (4 * nn)), max_angles()}));
+    // frames per batch: 256 MiB of sample holograms on the device, or CTDM_JOB_BATCH_FRAMES
+    int C = std::max(1, std::min({F, (int)((1l << 28) / (4 * nn)), max_angles()}));
+    if (const char *env = getenv("CTDM_JOB_BATCH_FRAMES"))
+        if (atoi(env) > 0) C = std::min(C, atoi(env));
 
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);

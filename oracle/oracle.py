@@ -286,3 +286,49 @@ def pipeline(params, sp, bg, angx, angy, bg_per_angle=False):
     lib().or_pipeline(ctypes.byref(params), _p(sp), _p(bg), na, int(bg_per_angle), _p(angx), _p(angy),
                       _p(out), car)
     return out, tuple(car)
+
+
+# ---- job driver pieces (numpy restatements) ------------------------------------------
+def angcal_peak(img):
+    """AngCal_GPU (cTDM/HilbertTransform.cu:2920-2983): flat index of the first maximum
+    of log10 |FFT2(img)| (quadrant-swapped, NaN/inf -> 0, cufftComplex2Real :2986-2996)
+    over [int(0.53 N^2), int(0.79 N^2)).  img: (N, N) picture, x fastest."""
+    img = np.asarray(img, np.float64)
+    n = img.shape[0]
+    spec = np.fft.fftshift(np.fft.fft2(img))
+    with np.errstate(divide="ignore"):
+        m = np.log10(np.abs(spec)).astype(np.float32)
+    m[~np.isfinite(m)] = 0
+    lo, hi = int(n * n * 0.53), int(n * n * 0.79)
+    return lo + int(np.argmax(m.ravel()[lo:hi]))
+
+
+def angcal_angle(peak, n, n_med, wavelength_nm, mag, camera_pixel_um):
+    """The angle AngCal_GPU derives from the peak column (float32 as written, with its
+    511 and 1024 read as N/2 - 1 and N)."""
+    posx = peak % n
+    fm = np.float32(n_med / (wavelength_nm * 1e-9))
+    fx = np.float32((n // 2 - 1 - posx) * 1 / (n * camera_pixel_um * 1e-6))
+    st = np.float32(np.float32(mag) * fx / fm)
+    a = abs(float(np.arcsin(np.float64(st))))
+    return np.float32(a if st < 0 else -a)
+
+
+def check_array(values, limit_std, limit_range):
+    """checkArray (cTDM/HilbertTransform.cu:3056-3092): True when the population standard
+    deviation exceeds limit_std or the range exceeds limit_range."""
+    v = np.asarray(values, np.float32).ravel()
+    mean = float(np.sum(v.astype(np.float64))) / v.size
+    std = float(np.sqrt(np.sum((v.astype(np.float64) - mean) ** 2) / v.size))
+    rng = abs(np.float32(v.max()) - np.float32(v.min()))
+    return bool(std > np.float32(limit_std) or rng > np.float32(limit_range))
+
+
+def check_frame(phase, resize_flag, limit_std, limit_range):
+    """The job loop's frame check (cTDM/HilbertTransform.cu:1087-1120): the centre half
+    of the map for ResizeFlag 1, the whole map with 0.5 and 5 pi for 0."""
+    ph = np.asarray(phase, np.float32)
+    n = ph.shape[0]
+    if resize_flag == 0:
+        return check_array(ph, 0.5, 5 * np.pi)
+    return check_array(ph[n // 4:3 * n // 4, n // 4:3 * n // 4], limit_std, limit_range)
