@@ -192,6 +192,32 @@ class Context:
         check(self.lib.ctdm_positivity(self.handle, r, iterations, check_mode, k2, n_med, _ptr(F2), _ptr(counts),
                                        _ptr(out), _stream(stream)), "ctdm_positivity")
 
+    def map_fi(self, U, angx, fm0, df, dx, F2, counts=None, stream=None):
+        """Frequency-interpolation mapping of the AngX scan (BatchReconPOCS's FI)."""
+        angx = _f32(angx)
+        r = int(round(np.sqrt(U.numel() // len(angx)))) if hasattr(U, "numel") else U.shape[-1]
+        check(self.lib.ctdm_map_fi(self.handle, len(angx), r, _ptr(U), _ptr(angx), fm0, df, dx, _ptr(F2),
+                                   _ptr(counts), _stream(stream)), "ctdm_map_fi")
+
+    def pocs(self, F2, r, k2, n_med, out, params=None, history=False, stream=None, **kw):
+        """ASD-POCS from F2 into out (octant-shifted RI).  params: a PocsParams (default
+        pocs_params(**kw)).  Returns the (iterations, 4) history (Dp, Dd, Dg, TV step)
+        when history is true."""
+        p = params if params is not None else pocs_params(**kw)
+        hist = np.zeros((max(p.iterations, 1), 4), np.float64) if history else None
+        check(self.lib.ctdm_pocs(self.handle, int(r), ctypes.byref(p), float(k2), float(n_med), _ptr(F2), _ptr(out),
+                                 _ptr(hist), _stream(stream)), "ctdm_pocs")
+        return hist[:p.iterations] if history else None
+
+
+def pocs_params(**kw):
+    """ctdm_pocs_params with the reference's constants, overridden by keywords."""
+    p = _lib.PocsParams()
+    load().ctdm_pocs_defaults(ctypes.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
 
 def launch_count():
     """Kernels launched by the library in this process so far."""

@@ -43,6 +43,13 @@ class JobFile(ctypes.Structure):
     ]
 
 
+class PocsParams(ctypes.Structure):
+    """ctdm_pocs_params (include/ctdm.h)."""
+    _fields_ = [("iterations", c_int), ("tv_steps", c_int), ("beta", c_double), ("beta_red", c_double),
+                ("alpha", c_double), ("alpha_red", c_double), ("r_max", c_double), ("eps_data", c_double),
+                ("tv_eps", c_double)]
+
+
 class JobResult(ctypes.Structure):
     """ctdm_job_result (include/ctdm.h)."""
     _fields_ = [("frames", c_int), ("rejected", c_int), ("recon_frames", c_int), ("n_holo", c_int),
@@ -136,6 +143,12 @@ _SIGS = {
     "ctdm_parse_job_file": (c_int, [ctypes.c_char_p, ctypes.POINTER(JobFile)]),
     "ctdm_run_job": (c_int, [ctypes.POINTER(JobFile), ctypes.POINTER(JobResult)]),
     "scriptFileRead": (c_int, [ctypes.c_char_p]),
+    "ctdm_map_fi": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_double, c_double, c_double, c_void_p,
+                            c_void_p, c_void_p]),
+    "ctdm_pocs_defaults": (None, [ctypes.POINTER(PocsParams)]),
+    "ctdm_pocs": (c_int, [c_void_p, c_int, ctypes.POINTER(PocsParams), c_double, c_double, c_void_p, c_void_p,
+                          c_void_p, c_void_p]),
+    "BatchReconPOCS": (None, [c_void_p, c_void_p, c_void_p, c_void_p, c_int]),
     "HilbertTransform": (None, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, P_int, P_int,
                                 c_int, c_int, c_int, c_int, c_int]),
     "AngCal_GPU": (c_float, [c_void_p, c_int, c_int, c_int, c_int]),

@@ -19,7 +19,7 @@ LIB = os.path.join(OUT, "libctdm_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["ctdm_api.cu", "k_recon.cu", "k_qpi.cu", "k_dct.cu", "k_stack.cu", "k_compat.cu", "k_fastuw.cu",
            "k_gold.cu", "k_noalloc.cu", "k_grad.cu", "batch.cu", "tune.cu", "k_loop_small.cu", "k_loop_256.cu",
-           "k_loop_384.cu", "k_loop_512.cu", "k_loop_768.cu", "driver.cu"]
+           "k_loop_384.cu", "k_loop_512.cu", "k_loop_768.cu", "driver.cu", "k_pocs.cu"]
 
 
 def nvcc():

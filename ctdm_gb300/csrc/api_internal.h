@@ -27,4 +27,6 @@ void note_launches(unsigned long long n);
 // the .rimap file (the status-returning form of the reference-named BatchRecon).
 ctdm_status batch_recon(const float *PhaseStack, const float *AmpStack, const float *sampleAngleRadX,
                         const float *sampleAngleRadY, int ReconFrame);
+// dir/3D-RI-{Complex,Real,Imag}_RxRxR.<ext> from a host R^3 volume (save_mode 0, 1, 2).
+ctdm_status write_ri_volume(const std::string &dir, int R, int save_mode, const ctdm_cfloat *h_ri, const char *ext);
 }  // namespace ctdm

@@ -1,5 +1,6 @@
 // Host runtime and C ABI of libctdm_gb300: device tables, contexts, workspace,
 // the fused hologram -> RI pipeline and the reference-named entry points.
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdarg>
@@ -10,6 +11,7 @@
 #include <string>
 #include <vector>
 
+#include "api_internal.h"
 #include "ctdm.h"
 #include "ctdm_common.cuh"
 #include "kernels_front.cuh"
@@ -195,7 +197,7 @@ const float *dct_eigen(int M)
 enum BufId {
     B_PHASE, B_AMP, B_PHU, B_CHG, B_CUT, B_GOLD, B_U, B_F2, B_COUNTS, B_G, B_T1, B_S, B_BGF, B_DCT, B_MASK, B_GEOM,
     B_CARRIER, B_KEY, B_SCRATCH, B_HOLO, B_BG, B_RI, B_GSTATE, B_GLIST, B_GSTATUS, B_FASTW, B_FASTIN, B_TMP, B_GWORK,
-    B_TMASK, B_TCOUNT, B_TVALS, B_QMAG, NBUF
+    B_TMASK, B_TCOUNT, B_TVALS, B_QMAG, B_FIT, B_PV, B_PG, B_PV2, B_PG2, B_PVP, B_PPART, B_PCTL, B_PHIST, NBUF
 };
 
 // Stage boundaries recorded with CUDA events when timing is enabled.
@@ -711,7 +713,7 @@ static ctdm_status pipeline_core(ctdm_ctx *c, const ctdm_params *p, int A, int M
     const double fm0 = p->n_med / p->wavelength;
     const double df = 1.0 / (R * p->dx);
     const double k = 2.0 * CTDM_PI_D * p->n_med / p->wavelength;
-    EwaldArgs ea;
+    EwaldArgs ea = {};
     ea.U = B<float2>(c, B_U);
     ea.geom = d_geom;
     ea.A = A;
@@ -950,7 +952,7 @@ extern "C" ctdm_status ctdm_map_ewald(ctdm_ctx *c, int A, int R, const ctdm_cflo
     ctdm_status st = upload_geometry(c, h_angx, h_angy, A, fm0, df, s);
     if (st != CTDM_OK) return st;
     CK(ensure(c, B_TMP, sizeof(float2) * r3), "alloc G");
-    EwaldArgs ea;
+    EwaldArgs ea = {};
     ea.U = reinterpret_cast<const float2 *>(d_U);
     ea.geom = B<AngleGeom>(c, B_GEOM);
     ea.A = A;
@@ -965,6 +967,127 @@ extern "C" ctdm_status ctdm_map_ewald(ctdm_ctx *c, int A, int R, const ctdm_cflo
     ea.counts = d_counts;
     ea.mask = nullptr;
     CK(launch_ewald(ea, s), "ewald mapping");
+    return CTDM_OK;
+}
+
+extern "C" ctdm_status ctdm_map_fi(ctdm_ctx *c, int A, int R, const ctdm_cfloat *d_U, const float *h_angx,
+                                   double fm0, double df, double dx, ctdm_cfloat *d_F2, uint32_t *d_counts,
+                                   void *stream)
+{
+    if (!c || !d_U || !h_angx || !d_F2) return invalid("ctdm_map_fi: NULL argument");
+    if (!ok_volume(R) || A < 1 || A > kMaxAngles) return invalid("ctdm_map_fi: size unsupported");
+    for (int a = 0; a < A; a++)
+        if (!std::isfinite(h_angx[a]) || std::fabs(h_angx[a]) >= 0.5 * CTDM_PI_D)
+            return invalid("ctdm_map_fi: scan angle %d outside (-pi/2, pi/2)", a);
+    CK(cudaSetDevice(c->device), "cudaSetDevice");
+    cudaStream_t s = (cudaStream_t)stream;
+    const long r3 = (long)R * R * R;
+    // one scan axis: the tilt AngX, AngY taken as zero (FrquencyInterpolation uses AngleX only)
+    std::vector<float> zeros(A, 0.f);
+    ctdm_status st = upload_geometry(c, h_angx, zeros.data(), A, fm0, df, s);
+    if (st != CTDM_OK) return st;
+    // scan angles ascending (ties in frame order) and their frames
+    std::vector<int> order(A);
+    for (int a = 0; a < A; a++) order[a] = a;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return h_angx[x] < h_angx[y]; });
+    std::vector<unsigned char> tab(A * (sizeof(double) + sizeof(int)));
+    double *th = reinterpret_cast<double *>(tab.data());
+    int *fr = reinterpret_cast<int *>(th + A);
+    for (int k = 0; k < A; k++) {
+        th[k] = (double)h_angx[order[k]];
+        fr[k] = order[k];
+    }
+    CK(ensure(c, B_FIT, tab.size()), "alloc FI tables");
+    CK(cudaMemcpyAsync(c->buf[B_FIT], tab.data(), tab.size(), cudaMemcpyHostToDevice, s), "upload FI tables");
+    CK(ensure(c, B_TMP, sizeof(float2) * r3), "alloc G");
+    EwaldArgs ea = {};
+    ea.U = reinterpret_cast<const float2 *>(d_U);
+    ea.geom = B<AngleGeom>(c, B_GEOM);
+    ea.A = A;
+    ea.R = R;
+    ea.fm0 = fm0;
+    ea.df = df;
+    ea.fm02 = fm0 * fm0;
+    ea.fm02s = (float)((fm0 / df) * (fm0 / df));
+    ea.dx = (float)dx;
+    ea.F2 = reinterpret_cast<float2 *>(d_F2);
+    ea.G = B<float2>(c, B_TMP);
+    ea.counts = d_counts;
+    ea.fi_theta = B<double>(c, B_FIT);
+    ea.fi_frame = reinterpret_cast<const int *>(B<double>(c, B_FIT) + A);
+    CK(launch_ewald(ea, s), "frequency-interpolation mapping");
+    return CTDM_OK;
+}
+
+extern "C" void ctdm_pocs_defaults(ctdm_pocs_params *p)
+{
+    if (!p) return;
+    // BatchReconPOCS (cTDM/HilbertTransform.cu:2133-2141, 2208): 100 iterations of 20 TV steps
+    p->iterations = 100;
+    p->tv_steps = 20;
+    p->beta = 1.0;
+    p->beta_red = 0.995;
+    p->alpha = 0.2;
+    p->alpha_red = 0.95;
+    p->r_max = 0.95;
+    p->eps_data = 0.0;
+    p->tv_eps = 1e-8;
+}
+
+extern "C" ctdm_status ctdm_pocs(ctdm_ctx *c, int R, const ctdm_pocs_params *p, double k2, double n_med,
+                                 const ctdm_cfloat *d_F2, ctdm_cfloat *d_ri, double *h_hist, void *stream)
+{
+    if (!c || !p || !d_F2 || !d_ri) return invalid("ctdm_pocs: NULL argument");
+    if (!ok_volume(R)) return invalid("ctdm_pocs: volume side %d unsupported", R);
+    if (p->iterations < 0 || p->iterations > 100000 || p->tv_steps < 1 || p->tv_steps > 1000)
+        return invalid("ctdm_pocs: iterations or tv_steps out of range");
+    if (!(k2 > 0) || !(n_med > 0) || !(p->tv_eps >= 0)) return invalid("ctdm_pocs: k2, n_med and tv_eps");
+    CK(cudaSetDevice(c->device), "cudaSetDevice");
+    cudaStream_t s = (cudaStream_t)stream;
+    const long r3 = (long)R * R * R;
+    const int nh = p->iterations > 0 ? p->iterations : 1;
+    const int vol[] = {B_PV, B_PG, B_PV2, B_PG2, B_PVP};
+    for (int id : vol) CK(ensure(c, id, sizeof(float) * r3), "alloc POCS volumes");
+    CK(ensure(c, B_G, sizeof(float2) * r3), "alloc G");
+    CK(ensure(c, B_PPART, sizeof(double) * kPocsBlocks), "alloc partial sums");
+    CK(ensure(c, B_PCTL, sizeof(PocsCtl)), "alloc controller");
+    CK(ensure(c, B_PHIST, sizeof(double) * 4 * nh), "alloc history");
+    const bool want_dd = h_hist != nullptr || p->eps_data > 0;
+    PocsCtl ctl = {};
+    ctl.beta = p->beta;
+    ctl.beta_red = p->beta_red;
+    ctl.alpha = p->alpha;
+    ctl.alpha_red = p->alpha_red;
+    ctl.r_max = p->r_max;
+    ctl.eps_data = p->eps_data;
+    ctl.dd = want_dd ? 0.0 : HUGE_VAL;   // not measured: the data condition holds
+    ctl.first = 1;
+    ctl.n_hist = p->iterations;
+    PocsBufs b;
+    b.V = B<float>(c, B_PV);
+    b.g = B<float>(c, B_PG);
+    b.V2 = B<float>(c, B_PV2);
+    b.g2 = B<float>(c, B_PG2);
+    b.Vp = B<float>(c, B_PVP);
+    b.G = B<float2>(c, B_G);
+    b.F2 = reinterpret_cast<const float2 *>(d_F2);
+    b.part = B<double>(c, B_PPART);
+    b.ctl = B<PocsCtl>(c, B_PCTL);
+    b.hist = B<double>(c, B_PHIST);
+    b.R = R;
+    b.y_scale = (float)(-1.0 / k2);
+    b.tv_eps = (float)p->tv_eps;
+    CK(cudaMemcpyAsync(b.ctl, &ctl, sizeof ctl, cudaMemcpyHostToDevice, s), "upload controller");
+    CK(cudaMemsetAsync(b.V, 0, sizeof(float) * r3, s), "zero V");
+    CK(cudaMemsetAsync(b.G, 0, sizeof(float2) * r3, s), "zero G");
+    for (int it = 0; it < p->iterations; it++) CK(pocs_iteration(b, p->tv_steps, want_dd, s), "POCS iteration");
+    CK(pocs_finish(b, (float)n_med, reinterpret_cast<float2 *>(d_ri), s), "POCS output");
+    if (h_hist && p->iterations > 0) {
+        CK(cudaMemcpyAsync(h_hist, b.hist, sizeof(double) * 4 * p->iterations, cudaMemcpyDeviceToHost, s),
+           "history");
+        CK(cudaStreamSynchronize(s), "history");
+    }
+    g_err.clear();
     return CTDM_OK;
 }
 
@@ -1296,4 +1419,53 @@ extern "C" void BatchRecon(float *PhaseStack, float *AmpStack, float *sampleAngl
                            int ReconFrame)
 {
     batch_recon(PhaseStack, AmpStack, sampleAngleRadX, sampleAngleRadY, ReconFrame);
+}
+
+// BatchReconPOCS (cTDM/HilbertTransform.cu:2049-2402): the same spectra, the
+// frequency-interpolation mapping over the AngX scan and ASD-POCS with the reference's
+// constants; writes 3D-RI-{Complex,Real,Imag}_RxRxR.raw into SaveDir like the reference.
+extern "C" void BatchReconPOCS(float *PhaseStack, float *AmpStack, float *sampleAngleRadX, float *sampleAngleRadY,
+                               int ReconFrame)
+{
+    (void)sampleAngleRadY;
+    ctdm_ctx *c = default_ctx();
+    if (!c) { invalid("BatchReconPOCS: no CUDA device"); return; }
+    const int R = g_recon;
+    if (!ok_volume(R) || ReconFrame < 1 || ReconFrame > kMaxAngles) { invalid("BatchReconPOCS: size unsupported"); return; }
+    const long rr = (long)R * R, r3 = rr * R;
+    const double lambda = g_wavelength_nm * 1e-9;
+    const double fm0 = g_nmed / lambda;
+    const double dx = (g_pixel_um * 1e-6) / g_mag * 1024.0 / R;
+    const double k = 2.0 * CTDM_PI_D * g_nmed / lambda;
+    const double df = 1.0 / (R * dx);
+    float *ph = nullptr, *am = nullptr;
+    float2 *U = nullptr, *F2 = nullptr, *ri = nullptr;
+    auto cleanup = [&]() { cudaFree(ph); cudaFree(am); cudaFree(U); cudaFree(F2); cudaFree(ri); };
+    if (cudaMalloc(&ph, sizeof(float) * ReconFrame * rr) != cudaSuccess ||
+        cudaMalloc(&am, sizeof(float) * ReconFrame * rr) != cudaSuccess ||
+        cudaMalloc(&U, sizeof(float2) * ReconFrame * rr) != cudaSuccess ||
+        cudaMalloc(&F2, sizeof(float2) * r3) != cudaSuccess || cudaMalloc(&ri, sizeof(float2) * r3) != cudaSuccess) {
+        cleanup();
+        cudaGetLastError();
+        set_err("BatchReconPOCS: device allocation failed");
+        return;
+    }
+    cudaError_t e = cudaMemcpy(ph, PhaseStack, sizeof(float) * ReconFrame * rr, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(am, AmpStack, sizeof(float) * ReconFrame * rr, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) { cleanup(); cuda_fail(e, "BatchReconPOCS upload"); return; }
+    ctdm_pocs_params pp;
+    ctdm_pocs_defaults(&pp);
+    ctdm_status st = ctdm_stack_spectra(c, ReconFrame, R, ph, am, reinterpret_cast<ctdm_cfloat *>(U), 0);
+    if (st == CTDM_OK)
+        st = ctdm_map_fi(c, ReconFrame, R, reinterpret_cast<ctdm_cfloat *>(U), sampleAngleRadX, fm0, df, dx,
+                         reinterpret_cast<ctdm_cfloat *>(F2), nullptr, 0);
+    if (st == CTDM_OK)
+        st = ctdm_pocs(c, R, &pp, k * k, g_nmed, reinterpret_cast<ctdm_cfloat *>(F2), reinterpret_cast<ctdm_cfloat *>(ri),
+                       nullptr, 0);
+    if (st != CTDM_OK) { cleanup(); return; }
+    std::vector<ctdm_cfloat> host(r3);
+    e = cudaMemcpy(host.data(), ri, sizeof(float2) * r3, cudaMemcpyDeviceToHost);
+    cleanup();
+    if (e != cudaSuccess) { cuda_fail(e, "BatchReconPOCS download"); return; }
+    if (write_ri_volume(g_save_dir, R, g_recon_save, host.data(), "raw") == CTDM_OK) g_err.clear();
 }

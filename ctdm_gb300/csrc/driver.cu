@@ -377,13 +377,14 @@ extern "C" ctdm_status ctdm_read_phimap(const char *path, int *status, double *a
     return CTDM_OK;
 }
 
-extern "C" ctdm_status ctdm_write_rimap(const char *dir, int R, int save_mode, const ctdm_cfloat *h_ri)
+namespace ctdm {
+ctdm_status write_ri_volume(const std::string &dir, int R, int save_mode, const ctdm_cfloat *h_ri, const char *ext)
 {
-    if (!h_ri || R < 1 || save_mode < 0 || save_mode > 2) return fail_invalid("ctdm_write_rimap: bad argument");
+    if (!h_ri || R < 1 || save_mode < 0 || save_mode > 2) return fail_invalid("RI volume export: bad argument");
     // export (:2013-2041): complex64, or the real / imaginary part as float32
     char name[96];
     const char *kind = save_mode == 0 ? "Complex" : (save_mode == 1 ? "Real" : "Imag");
-    snprintf(name, sizeof name, "3D-RI-%s_%dx%dx%d.rimap", kind, R, R, R);
+    snprintf(name, sizeof name, "3D-RI-%s_%dx%dx%d.%s", kind, R, R, R, ext);
     const std::string path = join(dir, name);
     FILE *fp = fopen(path.c_str(), "wb");
     if (!fp) return fail_io("cannot write " + path);
@@ -400,6 +401,12 @@ extern "C" ctdm_status ctdm_write_rimap(const char *dir, int R, int save_mode, c
     if (!ok) return fail_io("short write: " + path);
     clear_error();
     return CTDM_OK;
+}
+}  // namespace ctdm
+
+extern "C" ctdm_status ctdm_write_rimap(const char *dir, int R, int save_mode, const ctdm_cfloat *h_ri)
+{
+    return write_ri_volume(dir ? dir : ".", R, save_mode, h_ri, "rimap");
 }
 
 extern "C" int ctdm_check_frame(const float *phase, int N, int resize_flag, double limit_std, double limit_range)

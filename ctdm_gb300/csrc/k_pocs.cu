@@ -1,0 +1,321 @@
+// ASD-POCS reconstruction: data consistency and positivity projections alternated with
+// total-variation steepest descent, with the step adapted from the distances each
+// part moves the volume (Sidky and Pan, Phys. Med. Biol. 53 (2008) 4777, the
+// algorithm the reference's BatchReconPOCS follows, cTDM/HilbertTransform.cu:
+// 2049-2402, kernels cTDM/Recon_kernel.cu:834-1106).  The reference's version is not
+// usable as written (complex square root with the wrong precedence, a data step that
+// copies the measured data onto itself, the fourth TV term on the x neighbour,
+// numerator minus denominator instead of their quotient, the TV result discarded by
+// the next iteration, an uninitialised data tolerance); this is the algorithm with
+// those parts written from the mathematics.
+//
+// The volume is the contrast V = n^2 / n_med^2 - 1 (the scattering potential is
+// -k^2 V), real after the positivity projection.  One iteration:
+//   F = FFT3(V); F = beta Y + (1 - beta) F where measured (Y = F2 / -k^2); V = IFFT3(F)
+//   V+ = (max(Re sqrt(1 + V), 1))^2 - 1        (n real and n >= n_med)
+//   Dp = |V+ - V_start|, Dd = |FFT3(V+) - Y| over the measured samples (optional)
+//   first iteration: dtvg = alpha Dp
+//   tv_steps times: g = grad TV(V); V -= dtvg g / |g|
+//   Dg = |V - V+|; if Dg > r_max Dp and Dd > eps: dtvg *= alpha_red; beta *= beta_red
+// TV is the isotropic total variation with backward differences and periodic
+// boundaries, sum_q sqrt(eps + |V(q) - V(q - x)|^2 + |V(q) - V(q - y)|^2 + |V(q) - V(q - z)|^2).
+//
+// Device side: every sum is a per-block partial in double followed by a last-block sum
+// in fixed order (deterministic), and the controller (PocsCtl) lives in device memory:
+// the TV step reads its size from there, the reductions' last blocks update it.  An
+// iteration is therefore a fixed launch sequence that a CUDA graph can replay.
+#include "kernels.cuh"
+
+namespace ctdm {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block sum of v in a fixed order; the result is valid in thread 0.
+__device__ double block_sum(double v)
+{
+    __shared__ double sw[kThreads / 32];
+    v = warp_sum(v);
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) sw[w] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x == 0)
+        for (int i = 0; i < kThreads / 32; i++) t += sw[i];
+    __syncthreads();
+    return t;
+}
+
+// Writes this block's partial; the last block to finish sums all partials in index
+// order and returns true in its thread 0 with *total set.
+__device__ bool grid_sum(double v, double *part, unsigned *ticket, double *total)
+{
+    __shared__ bool last;
+    const double b = block_sum(v);
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = b;
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    double s = 0.0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += kThreads) s += __ldcg(&part[i]);
+    s = block_sum(s);
+    if (threadIdx.x == 0) {
+        *total = s;
+        *ticket = 0u;
+        return true;
+    }
+    return false;
+}
+
+// Re sqrt(1 + v) - 1 without cancellation for small v.
+__device__ __forceinline__ float re_sqrt1p_m1(float2 v)
+{
+    const float zr = 1.0f + v.x;
+    const float mod = sqrtf(zr * zr + v.y * v.y);
+    const float mod_m1 = (2.0f * v.x + v.x * v.x + v.y * v.y) / (mod + 1.0f);   // |1 + v| - 1
+    const float h = 0.5f * (mod_m1 + v.x);                                      // (|z| + Re z)/2 - 1
+    return h / (sqrtf(1.0f + h) + 1.0f);
+}
+
+__global__ void __launch_bounds__(kThreads) dc_kernel(float2 *G, const float2 *__restrict__ F2, long n,
+                                                      const PocsCtl *__restrict__ ctl, float y_scale)
+{
+    const float beta = (float)ctl->beta, keep = (float)(1.0 - ctl->beta);
+    for (long i = blockIdx.x * (long)kThreads + threadIdx.x; i < n; i += (long)gridDim.x * kThreads) {
+        const float2 f = F2[i];
+        if (f.x != 0.f || f.y != 0.f) {
+            const float2 g = G[i];
+            G[i] = make_float2(beta * (f.x * y_scale) + keep * g.x, beta * (f.y * y_scale) + keep * g.y);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) project_kernel(float2 *G, float *V, float *Vp, long n, float inv_n3,
+                                                           PocsCtl *ctl, double *part, bool write_g)
+{
+    double acc = 0.0;
+    for (long i = blockIdx.x * (long)kThreads + threadIdx.x; i < n; i += (long)gridDim.x * kThreads) {
+        float2 v = G[i];
+        v = make_float2(v.x * inv_n3, v.y * inv_n3);
+        const float u = re_sqrt1p_m1(v);
+        const float vn = u > 0.f ? u * (2.0f + u) : 0.f;
+        const float d = vn - V[i];
+        acc += (double)d * d;
+        V[i] = vn;
+        Vp[i] = vn;
+        if (write_g) G[i] = make_float2(vn, 0.f);
+    }
+    double t;
+    if (grid_sum(acc, part, &ctl->ticket, &t)) ctl->dp = sqrt(t);
+}
+
+__global__ void __launch_bounds__(kThreads) dd_kernel(const float2 *__restrict__ G, const float2 *__restrict__ F2,
+                                                      long n, float y_scale, PocsCtl *ctl, double *part)
+{
+    double acc = 0.0;
+    for (long i = blockIdx.x * (long)kThreads + threadIdx.x; i < n; i += (long)gridDim.x * kThreads) {
+        const float2 f = F2[i];
+        if (f.x != 0.f || f.y != 0.f) {
+            const float2 g = G[i];
+            const float dx = g.x - f.x * y_scale, dy = g.y - f.y * y_scale;
+            acc += (double)dx * dx + (double)dy * dy;
+        }
+    }
+    double t;
+    if (grid_sum(acc, part, &ctl->ticket, &t)) ctl->dd = sqrt(t);
+}
+
+// Gradient of TV at voxel (x, y, z) of the volume val() (periodic indices).
+template <class Get>
+__device__ __forceinline__ float tv_grad(const Get &val, int x, int y, int z, int R, float eps)
+{
+    const int xm = x == 0 ? R - 1 : x - 1, xp = x == R - 1 ? 0 : x + 1;
+    const int ym = y == 0 ? R - 1 : y - 1, yp = y == R - 1 ? 0 : y + 1;
+    const int zm = z == 0 ? R - 1 : z - 1, zp = z == R - 1 ? 0 : z + 1;
+    const float v = val(x, y, z);
+    const float vxm = val(xm, y, z), vym = val(x, ym, z), vzm = val(x, y, zm);
+    const float vxp = val(xp, y, z), vyp = val(x, yp, z), vzp = val(x, y, zp);
+    const float a0 = v - vxm, b0 = v - vym, c0 = v - vzm;
+    const float d0 = sqrtf(eps + a0 * a0 + b0 * b0 + c0 * c0);
+    const float ax = vxp - v, bx = vxp - val(xp, ym, z), cx = vxp - val(xp, y, zm);
+    const float dxn = sqrtf(eps + ax * ax + bx * bx + cx * cx);
+    const float ay = vyp - val(xm, yp, z), by = vyp - v, cy = vyp - val(x, yp, zm);
+    const float dyn = sqrtf(eps + ay * ay + by * by + cy * cy);
+    const float az = vzp - val(xm, y, zp), bz = vzp - val(x, ym, zp), cz = vzp - v;
+    const float dzn = sqrtf(eps + az * az + bz * bz + cz * cz);
+    return (a0 + b0 + c0) / d0 - ax / dxn - by / dyn - cz / dzn;
+}
+
+// STEP = false: g = grad TV(Vin).  STEP = true: the volume is Vin - s gin with
+// s = dtvg / |gin| (the previous descent step, applied on the fly to every stencil
+// point), written to Vout, and gout = grad TV of it.  The last block stores |gout| and,
+// on the first iteration, sets dtvg = alpha Dp.
+template <bool STEP>
+__global__ void __launch_bounds__(kThreads) tv_kernel(const float *__restrict__ Vin, const float *__restrict__ gin,
+                                                      float *Vout, float *gout, int R, float eps, PocsCtl *ctl,
+                                                      double *part)
+{
+    float s = 0.f;
+    if constexpr (STEP) s = ctl->gnorm > 0.0 ? (float)(ctl->dtvg / ctl->gnorm) : 0.f;
+    const long n = (long)R * R * R, rr = (long)R * R;
+    auto val = [&](int x, int y, int z) -> float {
+        const long q = x + (long)R * y + rr * z;
+        if constexpr (STEP) return __ldg(&Vin[q]) - s * __ldg(&gin[q]);
+        return __ldg(&Vin[q]);
+    };
+    double acc = 0.0;
+    for (long i = blockIdx.x * (long)kThreads + threadIdx.x; i < n; i += (long)gridDim.x * kThreads) {
+        const int x = (int)(i % R), y = (int)((i / R) % R), z = (int)(i / rr);
+        const float g = tv_grad(val, x, y, z, R, eps);
+        if constexpr (STEP) Vout[i] = val(x, y, z);
+        gout[i] = g;
+        acc += (double)g * g;
+    }
+    double t;
+    if (grid_sum(acc, part, &ctl->ticket, &t)) {
+        ctl->gnorm = sqrt(t);
+        if (!STEP && ctl->first) {
+            ctl->dtvg = ctl->alpha * ctl->dp;
+            ctl->first = 0;
+        }
+    }
+}
+
+// The last descent step, Dg, the step-size rule and the history entry; G = V for the
+// next iteration's transform.
+__global__ void __launch_bounds__(kThreads) tv_final_kernel(const float *Vin, const float *gin, float *V,
+                                                            const float *__restrict__ Vp, float2 *G, long n,
+                                                            PocsCtl *ctl, double *part, double *hist)
+{
+    const float s = ctl->gnorm > 0.0 ? (float)(ctl->dtvg / ctl->gnorm) : 0.f;
+    double acc = 0.0;
+    for (long i = blockIdx.x * (long)kThreads + threadIdx.x; i < n; i += (long)gridDim.x * kThreads) {
+        const float v = Vin[i] - s * gin[i];
+        const float d = v - Vp[i];
+        acc += (double)d * d;
+        V[i] = v;
+        G[i] = make_float2(v, 0.f);
+    }
+    double t;
+    if (grid_sum(acc, part, &ctl->ticket, &t)) {
+        ctl->dg = sqrt(t);
+        if (ctl->it < ctl->n_hist) {
+            double *h = hist + 4 * ctl->it;
+            h[0] = ctl->dp;
+            h[1] = ctl->dd;
+            h[2] = ctl->dg;
+            h[3] = ctl->dtvg;
+        }
+        if (ctl->dg > ctl->r_max * ctl->dp && ctl->dd > ctl->eps_data) ctl->dtvg *= ctl->alpha_red;
+        ctl->beta *= ctl->beta_red;
+        ctl->it++;
+    }
+}
+
+// n = n_med sqrt(1 + V) (principal root, Re n >= n_med, Im n >= 0, as calculate_n3D),
+// octant shifted like cuFFT3Dshift.
+__global__ void __launch_bounds__(kThreads) pocs_n_kernel(const float2 *__restrict__ G, int R, float inv_n3,
+                                                          float n_med, float2 *ri)
+{
+    const long rr = (long)R * R, n = rr * R;
+    for (long i = blockIdx.x * (long)kThreads + threadIdx.x; i < n; i += (long)gridDim.x * kThreads) {
+        const int x = (int)(i % R), y = (int)((i / R) % R), z = (int)(i / rr);
+        const float2 g = G[i];
+        const float c = 1.0f + g.x * inv_n3, d = g.y * inv_n3;
+        const float mod = sqrtf(c * c + d * d);
+        float a = sqrtf(fmaxf(0.5f * (mod + c), 0.f)) * n_med;
+        float b = d != 0.f ? copysignf(sqrtf(fmaxf(0.5f * (mod - c), 0.f)), d) * n_med : 0.f;
+        if (a < n_med) a = n_med;
+        if (b < 0.f) b = 0.f;
+        ri[((x + R / 2) % R) + R * (long)((y + R / 2) % R) + rr * ((z + R / 2) % R)] = make_float2(a, b);
+    }
+}
+
+unsigned grid_for(long n)
+{
+    const long b = (n + kThreads - 1) / kThreads;
+    return (unsigned)(b < kPocsBlocks ? b : kPocsBlocks);
+}
+
+cudaError_t fft3_unscaled(float2 *G, int R, bool inverse, cudaStream_t s)
+{
+    const long rr = (long)R * R;
+    cudaError_t e = fft_rows(G, R, rr, inverse, s);
+    if (e == cudaSuccess) e = fft_cols(G, R, rr, R, rr, R, inverse, s);
+    if (e == cudaSuccess) e = fft_cols(G, R, rr, R, R, rr, inverse, s);
+    return e;
+}
+
+// FFT3(G) -> data step -> IFFT3 (unscaled; the 1/R^3 is applied by the consumer).
+cudaError_t data_step(const PocsBufs &b, cudaStream_t s)
+{
+    const long n = (long)b.R * b.R * b.R;
+    cudaError_t e = fft3_unscaled(b.G, b.R, false, s);
+    if (e != cudaSuccess) return e;
+    dc_kernel<<<grid_for(n), kThreads, 0, s>>>(b.G, b.F2, n, b.ctl, b.y_scale);
+    note_launch();
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    return fft3_unscaled(b.G, b.R, true, s);
+}
+
+}  // namespace
+
+cudaError_t pocs_iteration(const PocsBufs &b, int tv_steps, bool want_dd, cudaStream_t s)
+{
+    const int R = b.R;
+    const long n = (long)R * R * R;
+    const unsigned grid = grid_for(n);
+    const float inv_n3 = 1.0f / (float)n;
+    cudaError_t e = data_step(b, s);
+    if (e != cudaSuccess) return e;
+    project_kernel<<<grid, kThreads, 0, s>>>(b.G, b.V, b.Vp, n, inv_n3, b.ctl, b.part, want_dd);
+    note_launch();
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (want_dd) {
+        if ((e = fft3_unscaled(b.G, R, false, s)) != cudaSuccess) return e;
+        dd_kernel<<<grid, kThreads, 0, s>>>(b.G, b.F2, n, b.y_scale, b.ctl, b.part);
+        note_launch();
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    // TV steepest descent: gradient at the POCS result, then tv_steps - 1 fused
+    // (step, gradient) passes between two buffer pairs, then the last step
+    tv_kernel<false><<<grid, kThreads, 0, s>>>(b.V, nullptr, nullptr, b.g, R, b.tv_eps, b.ctl, b.part);
+    note_launch();
+    const float *vin = b.V, *gin = b.g;
+    float *vout = b.V2, *gout = b.g2;
+    for (int t = 1; t < tv_steps; t++) {
+        tv_kernel<true><<<grid, kThreads, 0, s>>>(vin, gin, vout, gout, R, b.tv_eps, b.ctl, b.part);
+        note_launch();
+        const float *nv = vout, *ng = gout;
+        vout = const_cast<float *>(vin);
+        gout = const_cast<float *>(gin);
+        vin = nv;
+        gin = ng;
+    }
+    tv_final_kernel<<<grid, kThreads, 0, s>>>(vin, gin, b.V, b.Vp, b.G, n, b.ctl, b.part, b.hist);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t pocs_finish(const PocsBufs &b, float n_med, float2 *ri, cudaStream_t s)
+{
+    const long n = (long)b.R * b.R * b.R;
+    cudaError_t e = data_step(b, s);
+    if (e != cudaSuccess) return e;
+    pocs_n_kernel<<<grid_for(n), kThreads, 0, s>>>(b.G, b.R, 1.0f / (float)n, n_med, ri);
+    note_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace ctdm

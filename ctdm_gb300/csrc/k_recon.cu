@@ -232,7 +232,56 @@ cudaError_t fft3d(float2 *data, int R, bool inverse, cudaStream_t s)
 }
 
 // ------------------------------------------------------------ Ewald mapping
-template <int L>
+// Frequency interpolation between scan angles (FrquencyInterpolation, FI_kernel and
+// calF, cTDM/Recon_kernel.cu:471-731, with the mathematics fixed).  A frame puts its
+// detector frequency (Fx, Fy) on the voxel of its own cap, Fz = nz df after rounding.
+// The illumination angle theta' (tilt in the y-z plane, the scan axis AngX) whose cap
+// passes through that voxel centre satisfies Fy sin(theta') + Fz cos(theta') =
+// -|K|^2 / (2 fm), i.e. theta' = atan2(Fy, Fz) +- acos(-|K|^2 / (2 fm rho)) with
+// rho = |(Fy, Fz)|; the root nearer the frame's own angle is taken.  The spectra of the
+// two scan angles around theta' are interpolated linearly in angle at the same
+// detector frequency (the detector-plane part of the reference's trilinear
+// interpolation is the identity there, since theta' maps the voxel back onto (Fx, Fy))
+// and scaled by i 4 pi fz' with fz' = Fz + fm cos(theta').  Outside the scanned range
+// the edge angle's spectrum is used; where no theta' exists, the frame's own sample.
+__device__ __forceinline__ float2 fi_sample(int ii, int jj, int nzs, double df, double fm0, double theta_own,
+                                            const double *th, const int *fr, int A, const float2 *ucol, long rr,
+                                            float2 u_own, float fz_own)
+{
+    const double Fx = ii * df, Fy = jj * df, Fz = nzs * df;
+    const double rho = sqrt(Fy * Fy + Fz * Fz);
+    const double c = -(Fx * Fx + Fy * Fy + Fz * Fz) / (2.0 * fm0 * rho);
+    const float four_pi = 4.0f * CTDM_PI_F;
+    if (!(rho > 0.0) || c < -1.0 || c > 1.0)
+        return make_float2(-fz_own * four_pi * u_own.y, fz_own * four_pi * u_own.x);
+    const double phi = atan2(Fy, Fz), dth = acos(c);
+    const double t1 = phi + dth, t2 = phi - dth;
+    const double tp = fabs(t1 - theta_own) <= fabs(t2 - theta_own) ? t1 : t2;
+    const float fzp = (float)(Fz + fm0 * cos(tp));
+    int s = 0;
+    double w = 0.0;
+    if (tp >= th[A - 1]) {
+        s = A - 1;
+    } else if (tp > th[0]) {
+        int lo = 0, hi = A - 1;   // th[lo] <= tp < th[hi]
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (th[mid] <= tp) lo = mid;
+            else hi = mid;
+        }
+        s = lo;
+        w = (tp - th[lo]) / (th[hi] - th[lo]);
+    }
+    float2 u = __ldg(&ucol[fr[s] * rr]);
+    if (w > 0.0) {
+        const float2 u2 = __ldg(&ucol[fr[s + 1] * rr]);
+        const float wf = (float)w, vf = (float)(1.0 - w);
+        u = make_float2(vf * u.x + wf * u2.x, vf * u.y + wf * u2.y);
+    }
+    return make_float2(-fzp * four_pi * u.y, fzp * four_pi * u.x);
+}
+
+template <int L, bool FI>
 __global__ void __launch_bounds__(Plan<L>::THREADS) ewald_kernel(EwaldArgs a, const float2 *__restrict__ tw)
 {
     using P = Plan<L>;
@@ -242,10 +291,18 @@ __global__ void __launch_bounds__(Plan<L>::THREADS) ewald_kernel(EwaldArgs a, co
     uint32_t *cnt = reinterpret_cast<uint32_t *>(buf + P::B * P::LP);
     float2 *stage = reinterpret_cast<float2 *>(cnt + P::B * L);              // 32 values per warp
     AngleGeom *geo = reinterpret_cast<AngleGeom *>(stage + P::THREADS);
+    double *th = reinterpret_cast<double *>(geo + a.A);   // FI: sorted scan angles
+    int *fr = reinterpret_cast<int *>(th + a.A);          // FI: their frames
     const long line0 = (long)blockIdx.x * P::B;   // line = x + R*y, B consecutive x
     for (int e = threadIdx.x; e < P::B * P::LP; e += P::THREADS) buf[e] = make_float2(0.f, 0.f);
     for (int e = threadIdx.x; e < P::B * L; e += P::THREADS) cnt[e] = 0u;
-    for (int e = threadIdx.x; e < a.A; e += P::THREADS) geo[e] = a.geom[e];
+    for (int e = threadIdx.x; e < a.A; e += P::THREADS) {
+        geo[e] = a.geom[e];
+        if constexpr (FI) {
+            th[e] = a.fi_theta[e];
+            fr[e] = a.fi_frame[e];
+        }
+    }
     __syncthreads();
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = P::THREADS >> 5;
@@ -265,10 +322,20 @@ __global__ void __launch_bounds__(Plan<L>::THREADS) ewald_kernel(EwaldArgs a, co
             float2 val = make_float2(0.f, 0.f);
             if (ang < a.A && geo[ang].valid) {
                 float fz;
-                nz = ewald_nz(ii, jj, geo[ang], a.df, a.fm02, a.fm02s, R, fz);
-                if (nz >= 0) {
-                    const float2 u = __ldg(&ucol[ang * rr]);
-                    val = make_float2(-fz * four_pi * u.y, fz * four_pi * u.x);
+                if constexpr (FI) {
+                    const int nzs = ewald_nz_signed(ii, jj, geo[ang], a.df, a.fm02, a.fm02s, fz);
+                    if (nzs != kNoSample) {
+                        nz = imod(nzs, R);
+                        const float2 u = __ldg(&ucol[ang * rr]);
+                        val = fi_sample(ii, jj, nzs, a.df, a.fm0, asin(geo[ang].fy0 / a.fm0), th, fr, a.A, ucol, rr,
+                                        u, fz);
+                    }
+                } else {
+                    nz = ewald_nz(ii, jj, geo[ang], a.df, a.fm02, a.fm02s, R, fz);
+                    if (nz >= 0) {
+                        const float2 u = __ldg(&ucol[ang * rr]);
+                        val = make_float2(-fz * four_pi * u.y, fz * four_pi * u.x);
+                    }
                 }
             }
             // angle order per voxel: lanes hitting the same voxel form a group whose
@@ -323,9 +390,10 @@ template <int L>
 static cudaError_t ewald_launch(const EwaldArgs &a, cudaStream_t s)
 {
     using P = Plan<L>;
+    const bool fi = a.fi_theta != nullptr;
     const size_t smem = fftl::smem_bytes<L>() + sizeof(uint32_t) * P::B * L + sizeof(float2) * P::THREADS +
-                        sizeof(AngleGeom) * a.A;
-    auto k = ewald_kernel<L>;
+                        sizeof(AngleGeom) * a.A + (fi ? (sizeof(double) + sizeof(int)) * a.A : 0);
+    auto k = fi ? ewald_kernel<L, true> : ewald_kernel<L, false>;
     cudaError_t e = prep_launch<L>(k, smem);
     if (e != cudaSuccess) return e;
     k<<<(unsigned)((long)L * L / P::B), P::THREADS, smem, s>>>(a, twiddles(L)); note_launch();

@@ -38,6 +38,10 @@ struct EwaldArgs {
     float2 *G;              // R^3 out (F2 after the z inverse transform)
     uint32_t *counts;       // optional R^3 hit counts
     uint8_t *mask;          // optional R^3 hit mask (1 where counts > 0)
+    // frequency interpolation between scan angles (FI mapping) when fi_theta is set:
+    // fi_theta = the A scan angles ascending (rad), fi_frame = the frame of each
+    const double *fi_theta;
+    const int *fi_frame;
 };
 
 struct LoopArgs {
@@ -107,6 +111,32 @@ int plane_clusters_256();
 // passes (plane pass register targets of 3 and 4 CTAs per SM).
 int loop_scheme(int R);
 cudaError_t launch_plane(const LoopArgs &a, bool final_pass, cudaStream_t s);
+
+// ---- ASD-POCS with total-variation steepest descent (k_pocs.cu)
+// Controller of one run in device memory: kernels read the step sizes from it and the
+// last block of each reduction updates it, so an iteration launches no host work.
+struct PocsCtl {
+    double beta, dtvg, dp, dd, dg, gnorm;
+    double alpha, alpha_red, r_max, eps_data, beta_red;
+    int first, it, n_hist, pad_;
+    unsigned int ticket;
+};
+struct PocsBufs {
+    float *V, *g, *V2, *g2, *Vp;   // real R^3 volumes (contrast, TV gradient, ping-pong, POCS result)
+    float2 *G;                     // complex R^3 work volume
+    const float2 *F2;              // measured k-space data (zero where nothing was measured)
+    double *part;                  // per-block partial sums (kPocsBlocks)
+    PocsCtl *ctl;
+    double *hist;                  // 4 doubles per iteration: Dp, Dd, Dg, the TV step used
+    int R;
+    float y_scale;                 // -1 / k^2: F2 -> spectrum of the contrast
+    float tv_eps;
+};
+constexpr int kPocsBlocks = 1216;  // 8 CTAs of 256 threads per SM on 152 SMs
+cudaError_t pocs_iteration(const PocsBufs &b, int tv_steps, bool want_dd, cudaStream_t s);
+// After the last iteration: one more data-consistency step, then n = n_med sqrt(1 + V)
+// with Re n >= n_med, Im n >= 0, octant shifted into ri.
+cudaError_t pocs_finish(const PocsBufs &b, float n_med, float2 *ri, cudaStream_t s);
 
 // Generic batched transforms.  rows: nlines contiguous lines of length L.
 // cols: lines of length L with element p at (l % nx) + (l / nx) * plane + p * ld.

@@ -74,36 +74,42 @@ __device__ __forceinline__ float2 modify_f(float2 n, float k2, float nm2)
 // contraction.  A float evaluation in units of df decides it whenever the result
 // is farther from a decision boundary than 20x its worst-case rounding error
 // (radicand >= 4 df^2, fraction more than 0.02 away from one half); otherwise the
-// double rule runs.  Returns -1 for no sample; fz (1/m) for the value.
-__device__ __forceinline__ int ewald_nz(int ii, int jj, const AngleGeom &g, double df, double fm02, float fm02s,
-                                        int R, float &fz)
+// double rule runs.  ewald_nz_signed returns the unwrapped index (kNoSample where the
+// radicand is negative) and fz (1/m) for the value; ewald_nz wraps it into [0, R).
+constexpr int kNoSample = -0x40000000;
+__device__ __forceinline__ int ewald_nz_signed(int ii, int jj, const AngleGeom &g, double df, double fm02,
+                                               float fm02s, float &fz)
 {
     const float fxs = (float)ii + g.fx0s, fys = (float)jj + g.fy0s;
     const float rads = fm02s - (fxs * fxs + fys * fys);
-    if (rads < -1.0f) return -1;
+    if (rads < -1.0f) return kNoSample;
     if (rads >= 4.0f) {
         const float fzs = sqrtf(rads);
         const float t = fzs - g.fz0s;
         const float fl = floorf(t);
         const float fr = t - fl;
         if (fabsf(fr - 0.5f) > 0.02f) {
-            const int nz = (fr > 0.5f) ? (int)fl + 1 : (int)fl;
             fz = fzs * (float)df;
-            return imod(nz, R);
+            return (fr > 0.5f) ? (int)fl + 1 : (int)fl;
         }
     }
     const double fx = __dadd_rn(__dmul_rn((double)ii, df), g.fx0);
     const double fy = __dadd_rn(__dmul_rn((double)jj, df), g.fy0);
     const double s = __dadd_rn(__dmul_rn(fx, fx), __dmul_rn(fy, fy));
     const double rad = __dsub_rn(fm02, s);
-    if (rad < 0.0) return -1;
+    if (rad < 0.0) return kNoSample;
     const double fzd = __dsqrt_rn(rad);
     const double t = __ddiv_rn(__dsub_rn(fzd, g.fz0), df);
     const double rn = t > 0.0 ? floor(__dadd_rn(t, 0.5)) : ceil(__dsub_rn(t, 0.5));
     fz = (float)fzd;
-    long nz = (long)rn % R;
-    if (nz < 0) nz += R;
-    return (int)nz;
+    return (int)rn;
+}
+
+__device__ __forceinline__ int ewald_nz(int ii, int jj, const AngleGeom &g, double df, double fm02, float fm02s,
+                                        int R, float &fz)
+{
+    const int nz = ewald_nz_signed(ii, jj, g, df, fm02, fm02s, fz);
+    return nz == kNoSample ? -1 : imod(nz, R);
 }
 
 }  // namespace ctdm

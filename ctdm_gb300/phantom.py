@@ -159,13 +159,21 @@ def random_cell(rng, fov):
     return ells
 
 
+def scan_angles(count, na, n_med):
+    """A one-axis scan: AngX evenly over [-asin(NA / n_med), asin(NA / n_med)], AngY = 0
+    (the scan the frequency-interpolation mapping of BatchReconPOCS assumes)."""
+    t = np.arcsin(na / n_med)
+    return np.linspace(-t, t, count).astype(np.float32), np.zeros(count, np.float32)
+
+
 def acquisition(n, r, angles, na=0.9, seed=0, pixel=0.1e-6, wavelength=532e-9, n_med=1.337,
-                photons=1000.0, ells=None, scale=1.0, carrier=(0.125, 0.125), **cell):
-    """One tomogram: `angles` SP holograms of N x N plus one background."""
+                photons=1000.0, ells=None, scale=1.0, carrier=(0.125, 0.125), scan="cone", **cell):
+    """One tomogram: `angles` SP holograms of N x N plus one background; scan "cone"
+    (illumination on a circular cone) or "line" (a one-axis AngX scan)."""
     rng = np.random.default_rng(seed)
     if ells is None:
         ells = cell_phantom(rng, scale=scale, **cell)
-    ax, ay = cone_angles(angles, na, n_med)
+    ax, ay = (cone_angles if scan == "cone" else scan_angles)(angles, na, n_med)
     fields = np.stack([rytov_field(ells, n_med, wavelength, n, pixel, ax[a], ay[a]) for a in range(angles)])
     holo = holograms_from_fields(fields, photons, rng, carrier)
     bg = holograms_from_fields(np.zeros((1, n, n), np.complex128), photons, rng, carrier)[0]

@@ -221,6 +221,30 @@ CTDM_API ctdm_status ctdm_map_ewald(ctdm_ctx *ctx, int A, int R, const ctdm_cflo
  * d_counts required for CTDM_CHECK_MASK (else may be NULL). */
 CTDM_API ctdm_status ctdm_positivity(ctdm_ctx *ctx, int R, int iterations, int check_mode, double k2, double n_med,
                             const ctdm_cfloat *d_F2, const uint32_t *d_counts, ctdm_cfloat *d_ri, void *stream);
+/* --- ASD-POCS with total variation (BatchReconPOCS, cTDM/HilbertTransform.cu:2049-2402,
+ * cTDM/Recon_kernel.cu:414-1106, with its mathematics fixed) -------------------------
+ * Frequency-interpolation mapping: like ctdm_map_ewald for a one-axis scan of tilts
+ * h_angx (AngY taken as zero), each voxel's value interpolated linearly in angle
+ * between the two scan angles around the angle whose cap passes exactly through the
+ * voxel centre (FrquencyInterpolation / FI_kernel). */
+CTDM_API ctdm_status ctdm_map_fi(ctdm_ctx *ctx, int A, int R, const ctdm_cfloat *d_U, const float *h_angx, double fm0,
+                                 double df, double dx, ctdm_cfloat *d_F2, uint32_t *d_counts, void *stream);
+typedef struct {
+    int iterations;                  /* outer iterations (reference 100) */
+    int tv_steps;                    /* TV steepest-descent steps per iteration (20) */
+    double beta, beta_red;           /* data-step relaxation and its decay (1.0, 0.995) */
+    double alpha, alpha_red, r_max;  /* TV step = alpha Dp, reduced by alpha_red when Dg > r_max Dp */
+    double eps_data;                 /* data tolerance of the reduction rule (0) */
+    double tv_eps;                   /* TV smoothing in contrast units (1e-8) */
+} ctdm_pocs_params;
+CTDM_API void ctdm_pocs_defaults(ctdm_pocs_params *p);
+/* ASD-POCS from F2 (zero where nothing was measured): octant-shifted RI volume like
+ * ctdm_positivity.  h_hist (may be NULL; synchronises when given): 4 doubles per
+ * iteration, the data-step distance Dp, the data residual Dd, the TV distance Dg and
+ * the TV step used. */
+CTDM_API ctdm_status ctdm_pocs(ctdm_ctx *ctx, int R, const ctdm_pocs_params *p, double k2, double n_med,
+                               const ctdm_cfloat *d_F2, ctdm_cfloat *d_ri, double *h_hist, void *stream);
+
 /* --- differentiable form (no reference counterpart) ---------------------------------
  * Measurement operator A = P F~: unitary 3-D FFT (F / R^{3/2}) then sampling at the
  * measured voxels of the Ewald caps.  V is the contrast f / (-k^2) of the reference's
@@ -382,6 +406,11 @@ CTDM_API void check_F_3D(ctdm_cfloat *F, ctdm_cfloat *F2, int Image_Width, int I
 CTDM_API void cuFFT3D(ctdm_cfloat *ImgArray, int sizeX, int sizeY, int sizeZ, int dir);
 /* cTDM/FFT.cuh:25 -- dir -1 forward, +1 inverse scaled by 1/(XY) and conjugated. */
 CTDM_API void cuFFT2D(ctdm_cfloat *ImgArray, int sizeX, int sizeY, int dir);
+/* cTDM/HilbertTransform.cuh:133 (defined at HilbertTransform.cu:2049) --
+ * host stacks and AngX scan angles; ASD-POCS with the reference's constants; writes
+ * 3D-RI-*.raw into SaveDir as the reference does. */
+CTDM_API void BatchReconPOCS(float *PhaseStack, float *AmpStack, float *sampleAngleRadX, float *sampleAngleRadY,
+                             int ReconFrame);
 /* cTDM/HilbertTransform.cu:70 -- each white-space separated entry of the job list is a
  * parameter file, parsed and run in turn.  Returns 0 when the list cannot be opened,
  * else 1; a failed job leaves its message in ctdm_last_error and the next job runs. */

@@ -1095,3 +1095,214 @@ void or_pipeline(const or_params *p, const float *sp, const float *bg, int na, i
     or_positivity(F2, C, r, p->iters, p->k2, p->n_med, p->check_mode, n_out);
     free(ph); free(am); free(U); free(F2); free(C);
 }
+
+/* ------------------------------------------------------------------------- */
+/* ASD-POCS with total variation (BatchReconPOCS, cTDM/HilbertTransform.cu:    */
+/* 2049-2402; FrquencyInterpolation / FI_kernel / calF and the POCS kernels,   */
+/* cTDM/Recon_kernel.cu:414-1106), with the mathematics fixed as the product   */
+/* defines it: see ctdm_gb300/csrc/k_pocs.cu and the FI notes of k_recon.cu.   */
+/* ------------------------------------------------------------------------- */
+
+/* Frequency-interpolation mapping for a one-axis scan of tilts angx (AngY = 0).
+ * Voxel rule of or_ewald_index (unwrapped z index kept for Fz = nz df); the angle
+ * theta' whose cap passes through the voxel centre, Fy sin t + Fz cos t =
+ * -|K|^2 / (2 fm), root nearer the frame's own angle; spectra of the two scan angles
+ * around theta' interpolated linearly in angle; value i 4 pi fz' u,
+ * fz' = Fz + fm cos(theta'); per-voxel mean over frames, / dx. */
+void or_fi_map(const cplx *U, const float *angx, int na, int r, double fm0, double df, double dx, cplx *F2,
+               uint32_t *counts)
+{
+    long n3 = (long)r * r * r, n2 = (long)r * r;
+    uint32_t *C = counts ? counts : (uint32_t *)malloc(sizeof(uint32_t) * n3);
+    memset(C, 0, sizeof(uint32_t) * n3);
+    for (long i = 0; i < n3; i++) F2[i] = 0;
+    int *order = (int *)malloc(sizeof(int) * na);
+    double *th = (double *)malloc(sizeof(double) * na);
+    for (int a = 0; a < na; a++) order[a] = a;
+    for (int a = 1; a < na; a++) {   /* stable insertion sort by angle */
+        int v = order[a], b = a - 1;
+        while (b >= 0 && angx[order[b]] > angx[v]) { order[b + 1] = order[b]; b--; }
+        order[b + 1] = v;
+    }
+    for (int k = 0; k < na; k++) th[k] = (double)angx[order[k]];
+    double fm02 = fm0 * fm0;
+    for (int a = 0; a < na; a++) {
+        double fx0 = fm0 * sin(0.0), fy0 = fm0 * sin((double)angx[a]);
+        double rad0 = fm02 - fx0 * fx0;
+        rad0 = rad0 - fy0 * fy0;
+        if (rad0 < 0) continue;
+        double fz0 = sqrt(rad0);
+        double theta_own = asin(fy0 / fm0);
+        for (int j = 0; j < r; j++)
+            for (int i = 0; i < r; i++) {
+                int ii = i - r / 2, jj = j - r / 2;
+                double fx = (double)ii * df;
+                fx = fx + fx0;
+                double fy = (double)jj * df;
+                fy = fy + fy0;
+                double s = fx * fx;
+                s = s + fy * fy;
+                double rad = fm02 - s;
+                if (rad < 0) continue;
+                double fz = sqrt(rad);
+                double t = (fz - fz0) / df;
+                double rn = t > 0.0 ? floor(t + 0.5) : ceil(t - 0.5);
+                long nzs = (long)rn;
+                int nx = ((ii % r) + r) % r, ny = ((jj % r) + r) % r;
+                long nzm = ((nzs % r) + r) % r;
+                long q = nx + (long)r * ny;
+                long vox = q + n2 * nzm;
+                cplx u_own = U[(long)a * n2 + q];
+                double Fx = ii * df, Fy = jj * df, Fz = (double)nzs * df;
+                double rho = sqrt(Fy * Fy + Fz * Fz);
+                double c = -(Fx * Fx + Fy * Fy + Fz * Fz) / (2.0 * fm0 * rho);
+                cplx val;
+                if (!(rho > 0.0) || c < -1.0 || c > 1.0) {
+                    val = I * (4 * OR_PI * fz) * u_own;
+                } else {
+                    double phi = atan2(Fy, Fz), dth = acos(c);
+                    double t1 = phi + dth, t2 = phi - dth;
+                    double tp = fabs(t1 - theta_own) <= fabs(t2 - theta_own) ? t1 : t2;
+                    double fzp = Fz + fm0 * cos(tp);
+                    int sidx = 0;
+                    double w = 0.0;
+                    if (tp >= th[na - 1]) {
+                        sidx = na - 1;
+                    } else if (tp > th[0]) {
+                        int lo = 0, hi = na - 1;
+                        while (hi - lo > 1) {
+                            int mid = (lo + hi) / 2;
+                            if (th[mid] <= tp) lo = mid;
+                            else hi = mid;
+                        }
+                        sidx = lo;
+                        w = (tp - th[lo]) / (th[hi] - th[lo]);
+                    }
+                    cplx u = U[(long)order[sidx] * n2 + q];
+                    if (w > 0.0) u = (1.0 - w) * u + w * U[(long)order[sidx + 1] * n2 + q];
+                    val = I * (4 * OR_PI * fzp) * u;
+                }
+                F2[vox] += val;
+                C[vox] += 1;
+            }
+    }
+    for (long i = 0; i < n3; i++) {
+        cplx f = F2[i];
+        if (C[i] != 0) f = f / (double)C[i];
+        F2[i] = f / dx;
+    }
+    free(order);
+    free(th);
+    if (!counts) free(C);
+}
+
+typedef struct {
+    int iterations, tv_steps;
+    double beta, beta_red, alpha, alpha_red, r_max, eps_data, tv_eps;
+} or_pocs_params;
+
+/* Gradient of the isotropic TV (backward differences, periodic) of V at every voxel. */
+static void tv_gradient(const double *V, int r, double eps, double *g)
+{
+    long rr = (long)r * r;
+#pragma omp parallel for schedule(static)
+    for (int z = 0; z < r; z++)
+        for (int y = 0; y < r; y++)
+            for (int x = 0; x < r; x++) {
+                int xm = (x + r - 1) % r, xp = (x + 1) % r, ym = (y + r - 1) % r, yp = (y + 1) % r;
+                int zm = (z + r - 1) % r, zp = (z + 1) % r;
+#define VV(a, b, c) V[(a) + (long)r * (b) + rr * (c)]
+                double v = VV(x, y, z);
+                double a0 = v - VV(xm, y, z), b0 = v - VV(x, ym, z), c0 = v - VV(x, y, zm);
+                double d0 = sqrt(eps + a0 * a0 + b0 * b0 + c0 * c0);
+                double vxp = VV(xp, y, z), vyp = VV(x, yp, z), vzp = VV(x, y, zp);
+                double ax = vxp - v, bx = vxp - VV(xp, ym, z), cx = vxp - VV(xp, y, zm);
+                double ay = vyp - VV(xm, yp, z), by = vyp - v, cy = vyp - VV(x, yp, zm);
+                double az = vzp - VV(xm, y, zp), bz = vzp - VV(x, ym, zp), cz = vzp - v;
+#undef VV
+                double dx = sqrt(eps + ax * ax + bx * bx + cx * cx);
+                double dy = sqrt(eps + ay * ay + by * by + cy * cy);
+                double dz = sqrt(eps + az * az + bz * bz + cz * cz);
+                g[x + (long)r * y + rr * z] = (a0 + b0 + c0) / d0 - ax / dx - by / dy - cz / dz;
+            }
+}
+
+static double norm2(const double *a, long n)
+{
+    double s = 0;
+    for (long i = 0; i < n; i++) s += a[i] * a[i];
+    return sqrt(s);
+}
+
+/* ASD-POCS on the contrast V = n^2 / n_med^2 - 1 from F2 (zero where unmeasured):
+ * data step F = beta Y + (1 - beta) F at the measured voxels (Y = F2 / -k^2),
+ * projection V+ = max(Re sqrt(1 + V), 1)^2 - 1, Dp = |V+ - V_start|,
+ * Dd = |FFT3(V+) - Y| over the measured voxels (want_dd, else +inf), TV steepest
+ * descent (dtvg = alpha Dp on the first iteration; tv_steps normalised-gradient steps),
+ * Dg = |V - V+|, dtvg *= alpha_red when Dg > r_max Dp and Dd > eps_data,
+ * beta *= beta_red.  Output: one more data step, n = est_n, octant shifted.
+ * hist: 4 doubles per iteration (Dp, Dd, Dg, dtvg used). */
+void or_pocs(const cplx *F2, int r, const or_pocs_params *p, double k2, double nmed, int want_dd, cplx *n_out,
+             double *hist)
+{
+    long n3 = (long)r * r * r;
+    double *V = (double *)calloc(n3, sizeof(double)), *Vp = (double *)malloc(sizeof(double) * n3);
+    double *g = (double *)malloc(sizeof(double) * n3), *d = (double *)malloc(sizeof(double) * n3);
+    cplx *G = (cplx *)malloc(sizeof(cplx) * n3);
+    double beta = p->beta, dtvg = 0;
+    int first = 1;
+    for (int it = 0; it <= p->iterations; it++) {
+        for (long i = 0; i < n3; i++) G[i] = V[i];
+        or_fft3d(G, r, r, r, -1);
+        for (long i = 0; i < n3; i++)
+            if (creal(F2[i]) != 0.0 || cimag(F2[i]) != 0.0) G[i] = beta * (F2[i] / (-k2)) + (1 - beta) * G[i];
+        or_fft3d(G, r, r, r, +1);
+        if (it == p->iterations) break;   /* the output's data step */
+        double dp = 0;
+        for (long i = 0; i < n3; i++) {
+            double u = creal(csqrt(1.0 + G[i])) - 1.0;
+            double vn = u > 0 ? u * (2 + u) : 0;
+            dp += (vn - V[i]) * (vn - V[i]);
+            V[i] = vn;
+            Vp[i] = vn;
+        }
+        dp = sqrt(dp);
+        double dd = HUGE_VAL;
+        if (want_dd) {
+            for (long i = 0; i < n3; i++) G[i] = Vp[i];
+            or_fft3d(G, r, r, r, -1);
+            double s = 0;
+            for (long i = 0; i < n3; i++)
+                if (creal(F2[i]) != 0.0 || cimag(F2[i]) != 0.0) {
+                    cplx e = G[i] - F2[i] / (-k2);
+                    s += creal(e) * creal(e) + cimag(e) * cimag(e);
+                }
+            dd = sqrt(s);
+        }
+        tv_gradient(V, r, p->tv_eps, g);
+        double gn = norm2(g, n3);
+        if (first) { dtvg = p->alpha * dp; first = 0; }
+        for (int t = 0; t < p->tv_steps; t++) {
+            double s = gn > 0 ? dtvg / gn : 0;
+            for (long i = 0; i < n3; i++) V[i] -= s * g[i];
+            if (t + 1 < p->tv_steps) {
+                tv_gradient(V, r, p->tv_eps, g);
+                gn = norm2(g, n3);
+            }
+        }
+        for (long i = 0; i < n3; i++) d[i] = V[i] - Vp[i];
+        double dg = norm2(d, n3);
+        if (hist) {
+            hist[4 * it] = dp;
+            hist[4 * it + 1] = dd;
+            hist[4 * it + 2] = dg;
+            hist[4 * it + 3] = dtvg;
+        }
+        if (dg > p->r_max * dp && dd > p->eps_data) dtvg *= p->alpha_red;
+        beta *= p->beta_red;
+    }
+    cplx *n = (cplx *)malloc(sizeof(cplx) * n3);
+    for (long i = 0; i < n3; i++) n[i] = est_n(G[i] * (-k2), k2, nmed);
+    or_shift3d(n, n_out, r, r, r);
+    free(V); free(Vp); free(g); free(d); free(G); free(n);
+}

@@ -332,3 +332,38 @@ def check_frame(phase, resize_flag, limit_std, limit_range):
     if resize_flag == 0:
         return check_array(ph, 0.5, 5 * np.pi)
     return check_array(ph[n // 4:3 * n // 4, n // 4:3 * n // 4], limit_std, limit_range)
+
+
+# ---- frequency interpolation and ASD-POCS ------------------------------------------
+class PocsParams(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int), ("tv_steps", ctypes.c_int), ("beta", ctypes.c_double),
+                ("beta_red", ctypes.c_double), ("alpha", ctypes.c_double), ("alpha_red", ctypes.c_double),
+                ("r_max", ctypes.c_double), ("eps_data", ctypes.c_double), ("tv_eps", ctypes.c_double)]
+
+
+def pocs_params(iterations=100, tv_steps=20, beta=1.0, beta_red=0.995, alpha=0.2, alpha_red=0.95, r_max=0.95,
+                eps_data=0.0, tv_eps=1e-8):
+    return PocsParams(iterations, tv_steps, beta, beta_red, alpha, alpha_red, r_max, eps_data, tv_eps)
+
+
+def fi_map(U, angx, fm0, df, dx):
+    """Frequency-interpolation mapping of A spectra (A, R, R) for the AngX scan."""
+    U = _c128(U)
+    na, r = U.shape[0], U.shape[1]
+    F2 = np.zeros((r, r, r), np.complex128)
+    C = np.zeros((r, r, r), np.uint32)
+    angx = _f32(angx)
+    lib().or_fi_map(_p(U), _p(angx), na, r, ctypes.c_double(fm0), ctypes.c_double(df), ctypes.c_double(dx),
+                    _p(F2), _p(C))
+    return F2, C
+
+
+def pocs(F2, params, k2, n_med, want_dd=True):
+    """ASD-POCS from F2; returns (octant-shifted n, history (iterations, 4))."""
+    F2 = _c128(F2)
+    r = F2.shape[0]
+    out = np.zeros_like(F2)
+    hist = np.zeros((max(params.iterations, 1), 4), np.float64)
+    lib().or_pocs(_p(F2), r, ctypes.byref(params), ctypes.c_double(k2), ctypes.c_double(n_med), int(want_dd),
+                  _p(out), _p(hist))
+    return out, hist[:params.iterations]
