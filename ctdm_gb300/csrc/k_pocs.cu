@@ -25,6 +25,7 @@
 // the TV step reads its size from there, the reductions' last blocks update it.  An
 // iteration is therefore a fixed launch sequence that a CUDA graph can replay.
 #include "kernels.cuh"
+#include "point_ops.cuh"
 
 namespace ctdm {
 
@@ -231,14 +232,8 @@ __global__ void __launch_bounds__(kThreads) pocs_n_kernel(const float2 *__restri
     const long rr = (long)R * R, n = rr * R;
     for (long i = blockIdx.x * (long)kThreads + threadIdx.x; i < n; i += (long)gridDim.x * kThreads) {
         const int x = (int)(i % R), y = (int)((i / R) % R), z = (int)(i / rr);
-        const float2 g = G[i];
-        const float c = 1.0f + g.x * inv_n3, d = g.y * inv_n3;
-        const float mod = sqrtf(c * c + d * d);
-        float a = sqrtf(fmaxf(0.5f * (mod + c), 0.f)) * n_med;
-        float b = d != 0.f ? copysignf(sqrtf(fmaxf(0.5f * (mod - c), 0.f)), d) * n_med : 0.f;
-        if (a < n_med) a = n_med;
-        if (b < 0.f) b = 0.f;
-        ri[((x + R / 2) % R) + R * (long)((y + R / 2) % R) + rr * ((z + R / 2) % R)] = make_float2(a, b);
+        ri[((x + R / 2) % R) + R * (long)((y + R / 2) % R) + rr * ((z + R / 2) % R)] =
+            est_n_scaled(G[i], inv_n3, n_med);
     }
 }
 
