@@ -1049,7 +1049,7 @@ extern "C" ctdm_status ctdm_pocs(ctdm_ctx *c, int R, const ctdm_pocs_params *p, 
     const int vol[] = {B_PV, B_PG, B_PV2, B_PG2, B_PVP};
     for (int id : vol) CK(ensure(c, id, sizeof(float) * r3), "alloc POCS volumes");
     CK(ensure(c, B_G, sizeof(float2) * r3), "alloc G");
-    CK(ensure(c, B_PPART, sizeof(double) * kPocsBlocks), "alloc partial sums");
+    CK(ensure(c, B_PPART, sizeof(double) * pocs_partials(R)), "alloc partial sums");
     CK(ensure(c, B_PCTL, sizeof(PocsCtl)), "alloc controller");
     CK(ensure(c, B_PHIST, sizeof(double) * 4 * nh), "alloc history");
     const bool want_dd = h_hist != nullptr || p->eps_data > 0;

@@ -137,51 +137,81 @@ __global__ void __launch_bounds__(kThreads) dd_kernel(const float2 *__restrict__
     if (grid_sum(acc, part, &ctl->ticket, &t)) ctl->dd = sqrt(t);
 }
 
-// Gradient of TV at voxel (x, y, z) of the volume val() (periodic indices).
-template <class Get>
-__device__ __forceinline__ float tv_grad(const Get &val, int x, int y, int z, int R, float eps)
+// Gradient of TV at a voxel from the 13 values of its stencil (c: the voxel, xm / xp
+// the x neighbours, and so on; "xp_ym" the voxel at (+1, -1, 0)).
+__device__ __forceinline__ float tv_grad(float v, float vxm, float vym, float vzm, float vxp, float vyp, float vzp,
+                                         float xp_ym, float xp_zm, float xm_yp, float yp_zm, float xm_zp, float ym_zp,
+                                         float eps)
 {
-    const int xm = x == 0 ? R - 1 : x - 1, xp = x == R - 1 ? 0 : x + 1;
-    const int ym = y == 0 ? R - 1 : y - 1, yp = y == R - 1 ? 0 : y + 1;
-    const int zm = z == 0 ? R - 1 : z - 1, zp = z == R - 1 ? 0 : z + 1;
-    const float v = val(x, y, z);
-    const float vxm = val(xm, y, z), vym = val(x, ym, z), vzm = val(x, y, zm);
-    const float vxp = val(xp, y, z), vyp = val(x, yp, z), vzp = val(x, y, zp);
     const float a0 = v - vxm, b0 = v - vym, c0 = v - vzm;
     const float d0 = sqrtf(eps + a0 * a0 + b0 * b0 + c0 * c0);
-    const float ax = vxp - v, bx = vxp - val(xp, ym, z), cx = vxp - val(xp, y, zm);
+    const float ax = vxp - v, bx = vxp - xp_ym, cx = vxp - xp_zm;
     const float dxn = sqrtf(eps + ax * ax + bx * bx + cx * cx);
-    const float ay = vyp - val(xm, yp, z), by = vyp - v, cy = vyp - val(x, yp, zm);
+    const float ay = vyp - xm_yp, by = vyp - v, cy = vyp - yp_zm;
     const float dyn = sqrtf(eps + ay * ay + by * by + cy * cy);
-    const float az = vzp - val(xm, y, zp), bz = vzp - val(x, ym, zp), cz = vzp - v;
+    const float az = vzp - xm_zp, bz = vzp - ym_zp, cz = vzp - v;
     const float dzn = sqrtf(eps + az * az + bz * bz + cz * cz);
     return (a0 + b0 + c0) / d0 - ax / dxn - by / dyn - cz / dzn;
 }
 
+// TV tile: 32 x 8 voxels of a plane per CTA, marching through kZc planes along z with
+// the planes z - 1, z, z + 1 (each with a one-voxel periodic halo) in shared memory,
+// so every input element is read from memory about 1.4 times (halo and chunk ends).
+constexpr int kTx = 32, kTy = 8, kZc = 32;
+
+int tv_blocks(int R) { return (R / kTx) * (R / kTy) * (R / kZc); }
+
 // STEP = false: g = grad TV(Vin).  STEP = true: the volume is Vin - s gin with
-// s = dtvg / |gin| (the previous descent step, applied on the fly to every stencil
-// point), written to Vout, and gout = grad TV of it.  The last block stores |gout| and,
-// on the first iteration, sets dtvg = alpha Dp.
+// s = dtvg / |gin| (the previous descent step, applied while the planes are loaded),
+// written to Vout, and gout = grad TV of it.  The last block stores |gout| and, on the
+// first iteration, sets dtvg = alpha Dp.
 template <bool STEP>
 __global__ void __launch_bounds__(kThreads) tv_kernel(const float *__restrict__ Vin, const float *__restrict__ gin,
                                                       float *Vout, float *gout, int R, float eps, PocsCtl *ctl,
                                                       double *part)
 {
+    static_assert(kTx * kTy == kThreads, "one voxel of the tile per thread");
+    __shared__ float pl[3][kTy + 2][kTx + 2];
     float s = 0.f;
     if constexpr (STEP) s = ctl->gnorm > 0.0 ? (float)(ctl->dtvg / ctl->gnorm) : 0.f;
-    const long n = (long)R * R * R, rr = (long)R * R;
-    auto val = [&](int x, int y, int z) -> float {
-        const long q = x + (long)R * y + rr * z;
-        if constexpr (STEP) return __ldg(&Vin[q]) - s * __ldg(&gin[q]);
-        return __ldg(&Vin[q]);
+    const int nbx = R / kTx, nby = R / kTy;
+    int bi = blockIdx.x;
+    const int x0 = (bi % nbx) * kTx;
+    bi /= nbx;
+    const int y0 = (bi % nby) * kTy, z0 = (bi / nby) * kZc;
+    const long rr = (long)R * R;
+    auto load_plane = [&](int slot, int z) {
+        const int zw = z < 0 ? z + R : (z >= R ? z - R : z);
+        for (int e = threadIdx.x; e < (kTx + 2) * (kTy + 2); e += kThreads) {
+            const int lx = e % (kTx + 2), ly = e / (kTx + 2);
+            int gx = x0 - 1 + lx, gy = y0 - 1 + ly;
+            gx = gx < 0 ? gx + R : (gx >= R ? gx - R : gx);
+            gy = gy < 0 ? gy + R : (gy >= R ? gy - R : gy);
+            const long q = gx + (long)R * gy + rr * zw;
+            float v = __ldg(&Vin[q]);
+            if constexpr (STEP) v = v - s * __ldg(&gin[q]);
+            pl[slot][ly][lx] = v;
+        }
     };
+    const int tx = threadIdx.x % kTx, ty = threadIdx.x / kTx, lx = tx + 1, ly = ty + 1;
+    load_plane(0, z0 - 1);
+    load_plane(1, z0);
     double acc = 0.0;
-    for (long i = blockIdx.x * (long)kThreads + threadIdx.x; i < n; i += (long)gridDim.x * kThreads) {
-        const int x = (int)(i % R), y = (int)((i / R) % R), z = (int)(i / rr);
-        const float g = tv_grad(val, x, y, z, R, eps);
-        if constexpr (STEP) Vout[i] = val(x, y, z);
-        gout[i] = g;
+    for (int k = 0; k < kZc; k++) {
+        load_plane((k + 2) % 3, z0 + k + 1);
+        __syncthreads();
+        const float(*pm)[kTx + 2] = pl[k % 3];
+        const float(*pc)[kTx + 2] = pl[(k + 1) % 3];
+        const float(*pp)[kTx + 2] = pl[(k + 2) % 3];
+        const float v = pc[ly][lx];
+        const float g = tv_grad(v, pc[ly][lx - 1], pc[ly - 1][lx], pm[ly][lx], pc[ly][lx + 1], pc[ly + 1][lx],
+                                pp[ly][lx], pc[ly - 1][lx + 1], pm[ly][lx + 1], pc[ly + 1][lx - 1], pm[ly + 1][lx],
+                                pp[ly][lx - 1], pp[ly - 1][lx], eps);
+        const long q = (x0 + tx) + (long)R * (y0 + ty) + rr * (z0 + k);
+        if constexpr (STEP) Vout[q] = v;
+        gout[q] = g;
         acc += (double)g * g;
+        __syncthreads();
     }
     double t;
     if (grid_sum(acc, part, &ctl->ticket, &t)) {
@@ -266,6 +296,12 @@ cudaError_t data_step(const PocsBufs &b, cudaStream_t s)
 
 }  // namespace
 
+int pocs_partials(int R)
+{
+    const int t = tv_blocks(R);
+    return t > kPocsBlocks ? t : kPocsBlocks;
+}
+
 cudaError_t pocs_iteration(const PocsBufs &b, int tv_steps, bool want_dd, cudaStream_t s)
 {
     const int R = b.R;
@@ -285,12 +321,13 @@ cudaError_t pocs_iteration(const PocsBufs &b, int tv_steps, bool want_dd, cudaSt
     }
     // TV steepest descent: gradient at the POCS result, then tv_steps - 1 fused
     // (step, gradient) passes between two buffer pairs, then the last step
-    tv_kernel<false><<<grid, kThreads, 0, s>>>(b.V, nullptr, nullptr, b.g, R, b.tv_eps, b.ctl, b.part);
+    const unsigned tvg = (unsigned)tv_blocks(R);
+    tv_kernel<false><<<tvg, kThreads, 0, s>>>(b.V, nullptr, nullptr, b.g, R, b.tv_eps, b.ctl, b.part);
     note_launch();
     const float *vin = b.V, *gin = b.g;
     float *vout = b.V2, *gout = b.g2;
     for (int t = 1; t < tv_steps; t++) {
-        tv_kernel<true><<<grid, kThreads, 0, s>>>(vin, gin, vout, gout, R, b.tv_eps, b.ctl, b.part);
+        tv_kernel<true><<<tvg, kThreads, 0, s>>>(vin, gin, vout, gout, R, b.tv_eps, b.ctl, b.part);
         note_launch();
         const float *nv = vout, *ng = gout;
         vout = const_cast<float *>(vin);

@@ -125,7 +125,7 @@ struct PocsBufs {
     float *V, *g, *V2, *g2, *Vp;   // real R^3 volumes (contrast, TV gradient, ping-pong, POCS result)
     float2 *G;                     // complex R^3 work volume
     const float2 *F2;              // measured k-space data (zero where nothing was measured)
-    double *part;                  // per-block partial sums (kPocsBlocks)
+    double *part;                  // per-block partial sums (pocs_partials(R))
     PocsCtl *ctl;
     double *hist;                  // 4 doubles per iteration: Dp, Dd, Dg, the TV step used
     int R;
@@ -133,6 +133,8 @@ struct PocsBufs {
     float tv_eps;
 };
 constexpr int kPocsBlocks = 1216;  // 8 CTAs of 256 threads per SM on 152 SMs
+// Partial-sum slots a run of side R needs.
+int pocs_partials(int R);
 cudaError_t pocs_iteration(const PocsBufs &b, int tv_steps, bool want_dd, cudaStream_t s);
 // After the last iteration: one more data-consistency step, then n = n_med sqrt(1 + V)
 // with Re n >= n_med, Im n >= 0, octant shifted into ri.
