@@ -89,15 +89,24 @@ __device__ __forceinline__ float re_sqrt1p_m1(float2 v)
     return h / (sqrtf(1.0f + h) + 1.0f);
 }
 
+// Elementwise kernels: each CTA owns kPer * kThreads consecutive elements and each
+// thread issues its kPer loads before it uses any of them (R^3 is a multiple of 1024).
+constexpr int kPer = 4;
+
 __global__ void __launch_bounds__(kThreads) dc_kernel(float2 *G, const float2 *__restrict__ F2, long n,
                                                       const PocsCtl *__restrict__ ctl, float y_scale)
 {
     const float beta = (float)ctl->beta, keep = (float)(1.0 - ctl->beta);
-    for (long i = blockIdx.x * (long)kThreads + threadIdx.x; i < n; i += (long)gridDim.x * kThreads) {
-        const float2 f = F2[i];
-        if (f.x != 0.f || f.y != 0.f) {
+    const long i0 = (long)blockIdx.x * (kPer * kThreads) + threadIdx.x;
+    float2 f[kPer];
+#pragma unroll
+    for (int k = 0; k < kPer; k++) f[k] = i0 + k * kThreads < n ? F2[i0 + k * kThreads] : make_float2(0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < kPer; k++) {
+        if (f[k].x != 0.f || f[k].y != 0.f) {
+            const long i = i0 + k * kThreads;
             const float2 g = G[i];
-            G[i] = make_float2(beta * (f.x * y_scale) + keep * g.x, beta * (f.y * y_scale) + keep * g.y);
+            G[i] = make_float2(beta * (f[k].x * y_scale) + keep * g.x, beta * (f[k].y * y_scale) + keep * g.y);
         }
     }
 }
@@ -105,14 +114,24 @@ __global__ void __launch_bounds__(kThreads) dc_kernel(float2 *G, const float2 *_
 __global__ void __launch_bounds__(kThreads) project_kernel(float2 *G, float *V, float *Vp, long n, float inv_n3,
                                                            PocsCtl *ctl, double *part, bool write_g)
 {
-    double acc = 0.0;
-    for (long i = blockIdx.x * (long)kThreads + threadIdx.x; i < n; i += (long)gridDim.x * kThreads) {
-        float2 v = G[i];
-        v = make_float2(v.x * inv_n3, v.y * inv_n3);
-        const float u = re_sqrt1p_m1(v);
+    const long i0 = (long)blockIdx.x * (kPer * kThreads) + threadIdx.x;
+    float2 g[kPer];
+    float v0[kPer];
+#pragma unroll
+    for (int k = 0; k < kPer; k++) {
+        const long i = i0 + k * kThreads;
+        g[k] = i < n ? G[i] : make_float2(0.f, 0.f);
+        v0[k] = i < n ? V[i] : 0.f;
+    }
+    float acc = 0.f;
+#pragma unroll
+    for (int k = 0; k < kPer; k++) {
+        const long i = i0 + k * kThreads;
+        if (i >= n) continue;
+        const float u = re_sqrt1p_m1(make_float2(g[k].x * inv_n3, g[k].y * inv_n3));
         const float vn = u > 0.f ? u * (2.0f + u) : 0.f;
-        const float d = vn - V[i];
-        acc += (double)d * d;
+        const float d = vn - v0[k];
+        acc = fmaf(d, d, acc);
         V[i] = vn;
         Vp[i] = vn;
         if (write_g) G[i] = make_float2(vn, 0.f);
@@ -124,13 +143,17 @@ __global__ void __launch_bounds__(kThreads) project_kernel(float2 *G, float *V, 
 __global__ void __launch_bounds__(kThreads) dd_kernel(const float2 *__restrict__ G, const float2 *__restrict__ F2,
                                                       long n, float y_scale, PocsCtl *ctl, double *part)
 {
-    double acc = 0.0;
-    for (long i = blockIdx.x * (long)kThreads + threadIdx.x; i < n; i += (long)gridDim.x * kThreads) {
-        const float2 f = F2[i];
-        if (f.x != 0.f || f.y != 0.f) {
-            const float2 g = G[i];
-            const float dx = g.x - f.x * y_scale, dy = g.y - f.y * y_scale;
-            acc += (double)dx * dx + (double)dy * dy;
+    const long i0 = (long)blockIdx.x * (kPer * kThreads) + threadIdx.x;
+    float2 f[kPer];
+#pragma unroll
+    for (int k = 0; k < kPer; k++) f[k] = i0 + k * kThreads < n ? F2[i0 + k * kThreads] : make_float2(0.f, 0.f);
+    float acc = 0.f;
+#pragma unroll
+    for (int k = 0; k < kPer; k++) {
+        if (f[k].x != 0.f || f[k].y != 0.f) {
+            const float2 g = G[i0 + k * kThreads];
+            const float dx = g.x - f[k].x * y_scale, dy = g.y - f[k].y * y_scale;
+            acc = fmaf(dx, dx, fmaf(dy, dy, acc));
         }
     }
     double t;
@@ -171,6 +194,7 @@ __global__ void __launch_bounds__(kThreads) tv_kernel(const float *__restrict__ 
                                                       double *part)
 {
     static_assert(kTx * kTy == kThreads, "one voxel of the tile per thread");
+    constexpr int kPlane = (kTx + 2) * (kTy + 2), kLoads = (kPlane + kThreads - 1) / kThreads;
     __shared__ float pl[3][kTy + 2][kTx + 2];
     float s = 0.f;
     if constexpr (STEP) s = ctl->gnorm > 0.0 ? (float)(ctl->dtvg / ctl->gnorm) : 0.f;
@@ -180,26 +204,47 @@ __global__ void __launch_bounds__(kThreads) tv_kernel(const float *__restrict__ 
     bi /= nbx;
     const int y0 = (bi % nby) * kTy, z0 = (bi / nby) * kZc;
     const long rr = (long)R * R;
-    auto load_plane = [&](int slot, int z) {
-        const int zw = z < 0 ? z + R : (z >= R ? z - R : z);
-        for (int e = threadIdx.x; e < (kTx + 2) * (kTy + 2); e += kThreads) {
-            const int lx = e % (kTx + 2), ly = e / (kTx + 2);
-            int gx = x0 - 1 + lx, gy = y0 - 1 + ly;
-            gx = gx < 0 ? gx + R : (gx >= R ? gx - R : gx);
-            gy = gy < 0 ? gy + R : (gy >= R ? gy - R : gy);
-            const long q = gx + (long)R * gy + rr * zw;
-            float v = __ldg(&Vin[q]);
-            if constexpr (STEP) v = v - s * __ldg(&gin[q]);
-            pl[slot][ly][lx] = v;
+    // the plane elements this thread loads: offsets within a plane (periodic halo)
+    long off[kLoads];
+    int slot_idx[kLoads];
+#pragma unroll
+    for (int j = 0; j < kLoads; j++) {
+        const int e = threadIdx.x + j * kThreads;
+        slot_idx[j] = e < kPlane ? e : -1;
+        const int lx = e % (kTx + 2), ly = e / (kTx + 2);
+        int gx = x0 - 1 + lx, gy = y0 - 1 + ly;
+        gx = gx < 0 ? gx + R : (gx >= R ? gx - R : gx);
+        gy = gy < 0 ? gy + R : (gy >= R ? gy - R : gy);
+        off[j] = e < kPlane ? gx + (long)R * gy : 0;
+    }
+    auto fetch = [&](int z, float *r) {
+        const long base = rr * (z < 0 ? z + R : (z >= R ? z - R : z));
+#pragma unroll
+        for (int j = 0; j < kLoads; j++) {
+            if (slot_idx[j] < 0) continue;
+            float v = __ldg(&Vin[base + off[j]]);
+            if constexpr (STEP) v = v - s * __ldg(&gin[base + off[j]]);
+            r[j] = v;
         }
     };
+    auto put = [&](int slot, const float *r) {
+        float *p = &pl[slot][0][0];
+#pragma unroll
+        for (int j = 0; j < kLoads; j++)
+            if (slot_idx[j] >= 0) p[slot_idx[j]] = r[j];
+    };
     const int tx = threadIdx.x % kTx, ty = threadIdx.x / kTx, lx = tx + 1, ly = ty + 1;
-    load_plane(0, z0 - 1);
-    load_plane(1, z0);
-    double acc = 0.0;
+    float nxt[kLoads];
+    fetch(z0 - 1, nxt);
+    put(0, nxt);
+    fetch(z0, nxt);
+    put(1, nxt);
+    fetch(z0 + 1, nxt);
+    float acc = 0.f;
     for (int k = 0; k < kZc; k++) {
-        load_plane((k + 2) % 3, z0 + k + 1);
+        put((k + 2) % 3, nxt);   // plane z0 + k + 1
         __syncthreads();
+        if (k + 1 < kZc) fetch(z0 + k + 2, nxt);   // in flight while this plane is computed
         const float(*pm)[kTx + 2] = pl[k % 3];
         const float(*pc)[kTx + 2] = pl[(k + 1) % 3];
         const float(*pp)[kTx + 2] = pl[(k + 2) % 3];
@@ -210,7 +255,7 @@ __global__ void __launch_bounds__(kThreads) tv_kernel(const float *__restrict__ 
         const long q = (x0 + tx) + (long)R * (y0 + ty) + rr * (z0 + k);
         if constexpr (STEP) Vout[q] = v;
         gout[q] = g;
-        acc += (double)g * g;
+        acc = fmaf(g, g, acc);
         __syncthreads();
     }
     double t;
@@ -230,11 +275,23 @@ __global__ void __launch_bounds__(kThreads) tv_final_kernel(const float *Vin, co
                                                             PocsCtl *ctl, double *part, double *hist)
 {
     const float s = ctl->gnorm > 0.0 ? (float)(ctl->dtvg / ctl->gnorm) : 0.f;
-    double acc = 0.0;
-    for (long i = blockIdx.x * (long)kThreads + threadIdx.x; i < n; i += (long)gridDim.x * kThreads) {
-        const float v = Vin[i] - s * gin[i];
-        const float d = v - Vp[i];
-        acc += (double)d * d;
+    const long i0 = (long)blockIdx.x * (kPer * kThreads) + threadIdx.x;
+    float vi[kPer], gi[kPer], pi[kPer];
+#pragma unroll
+    for (int k = 0; k < kPer; k++) {
+        const long i = i0 + k * kThreads;
+        vi[k] = i < n ? Vin[i] : 0.f;
+        gi[k] = i < n ? gin[i] : 0.f;
+        pi[k] = i < n ? Vp[i] : 0.f;
+    }
+    float acc = 0.f;
+#pragma unroll
+    for (int k = 0; k < kPer; k++) {
+        const long i = i0 + k * kThreads;
+        if (i >= n) continue;
+        const float v = vi[k] - s * gi[k];
+        const float d = v - pi[k];
+        acc = fmaf(d, d, acc);
         V[i] = v;
         G[i] = make_float2(v, 0.f);
     }
@@ -260,18 +317,21 @@ __global__ void __launch_bounds__(kThreads) pocs_n_kernel(const float2 *__restri
                                                           float n_med, float2 *ri)
 {
     const long rr = (long)R * R, n = rr * R;
-    for (long i = blockIdx.x * (long)kThreads + threadIdx.x; i < n; i += (long)gridDim.x * kThreads) {
+    const long i0 = (long)blockIdx.x * (kPer * kThreads) + threadIdx.x;
+    float2 g[kPer];
+#pragma unroll
+    for (int k = 0; k < kPer; k++) g[k] = i0 + k * kThreads < n ? G[i0 + k * kThreads] : make_float2(0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < kPer; k++) {
+        const long i = i0 + k * kThreads;
+        if (i >= n) continue;
         const int x = (int)(i % R), y = (int)((i / R) % R), z = (int)(i / rr);
         ri[((x + R / 2) % R) + R * (long)((y + R / 2) % R) + rr * ((z + R / 2) % R)] =
-            est_n_scaled(G[i], inv_n3, n_med);
+            est_n_scaled(g[k], inv_n3, n_med);
     }
 }
 
-unsigned grid_for(long n)
-{
-    const long b = (n + kThreads - 1) / kThreads;
-    return (unsigned)(b < kPocsBlocks ? b : kPocsBlocks);
-}
+unsigned grid_for(long n) { return (unsigned)((n + kPer * kThreads - 1) / (kPer * kThreads)); }
 
 cudaError_t fft3_unscaled(float2 *G, int R, bool inverse, cudaStream_t s)
 {
@@ -298,8 +358,8 @@ cudaError_t data_step(const PocsBufs &b, cudaStream_t s)
 
 int pocs_partials(int R)
 {
-    const int t = tv_blocks(R);
-    return t > kPocsBlocks ? t : kPocsBlocks;
+    const int t = tv_blocks(R), e = (int)grid_for((long)R * R * R);
+    return t > e ? t : e;
 }
 
 cudaError_t pocs_iteration(const PocsBufs &b, int tv_steps, bool want_dd, cudaStream_t s)

@@ -132,7 +132,6 @@ struct PocsBufs {
     float y_scale;                 // -1 / k^2: F2 -> spectrum of the contrast
     float tv_eps;
 };
-constexpr int kPocsBlocks = 1216;  // 8 CTAs of 256 threads per SM on 152 SMs
 // Partial-sum slots a run of side R needs.
 int pocs_partials(int R);
 cudaError_t pocs_iteration(const PocsBufs &b, int tv_steps, bool want_dd, cudaStream_t s);
