@@ -161,20 +161,23 @@ __global__ void __launch_bounds__(kThreads) dd_kernel(const float2 *__restrict__
 }
 
 // Gradient of TV at a voxel from the 13 values of its stencil (c: the voxel, xm / xp
-// the x neighbours, and so on; "xp_ym" the voxel at (+1, -1, 0)).
+// the x neighbours, and so on; "xp_ym" the voxel at (+1, -1, 0)).  Each term is a
+// difference over the local gradient magnitude, taken with the hardware reciprocal
+// square root (a few ulp; the correctly rounded square root and division cost most of
+// the kernel's instructions).
 __device__ __forceinline__ float tv_grad(float v, float vxm, float vym, float vzm, float vxp, float vyp, float vzp,
                                          float xp_ym, float xp_zm, float xm_yp, float yp_zm, float xm_zp, float ym_zp,
                                          float eps)
 {
     const float a0 = v - vxm, b0 = v - vym, c0 = v - vzm;
-    const float d0 = sqrtf(eps + a0 * a0 + b0 * b0 + c0 * c0);
+    const float r0 = rsqrtf(eps + a0 * a0 + b0 * b0 + c0 * c0);
     const float ax = vxp - v, bx = vxp - xp_ym, cx = vxp - xp_zm;
-    const float dxn = sqrtf(eps + ax * ax + bx * bx + cx * cx);
+    const float rx = rsqrtf(eps + ax * ax + bx * bx + cx * cx);
     const float ay = vyp - xm_yp, by = vyp - v, cy = vyp - yp_zm;
-    const float dyn = sqrtf(eps + ay * ay + by * by + cy * cy);
+    const float ry = rsqrtf(eps + ay * ay + by * by + cy * cy);
     const float az = vzp - xm_zp, bz = vzp - ym_zp, cz = vzp - v;
-    const float dzn = sqrtf(eps + az * az + bz * bz + cz * cz);
-    return (a0 + b0 + c0) / d0 - ax / dxn - by / dyn - cz / dzn;
+    const float rz = rsqrtf(eps + az * az + bz * bz + cz * cz);
+    return (a0 + b0 + c0) * r0 - ax * rx - by * ry - cz * rz;
 }
 
 // TV tile: 32 x 8 voxels of a plane per CTA, marching through kZc planes along z with
