@@ -68,9 +68,17 @@ __device__ bool grid_sum(double v, double *part, unsigned *ticket, double *total
     __syncthreads();
     if (!last) return false;
     __threadfence();
-    double s = 0.0;
-    for (int i = threadIdx.x; i < (int)gridDim.x; i += kThreads) s += __ldcg(&part[i]);
-    s = block_sum(s);
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;   // four chains: the loads overlap
+    const int n = (int)gridDim.x;
+    int i = threadIdx.x;
+    for (; i + 3 * kThreads < n; i += 4 * kThreads) {
+        s0 += __ldcg(&part[i]);
+        s1 += __ldcg(&part[i + kThreads]);
+        s2 += __ldcg(&part[i + 2 * kThreads]);
+        s3 += __ldcg(&part[i + 3 * kThreads]);
+    }
+    for (; i < n; i += kThreads) s0 += __ldcg(&part[i]);
+    double s = block_sum((s0 + s1) + (s2 + s3));
     if (threadIdx.x == 0) {
         *total = s;
         *ticket = 0u;
@@ -160,110 +168,150 @@ __global__ void __launch_bounds__(kThreads) dd_kernel(const float2 *__restrict__
     if (grid_sum(acc, part, &ctl->ticket, &t)) ctl->dd = sqrt(t);
 }
 
+// 1 / sqrt(x) by the hardware approximation (rsqrt.approx.ftz; x >= eps > 0 here, so
+// flushing subnormal inputs changes nothing).
+__device__ __forceinline__ float rsqrt_approx(float x)
+{
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 // Gradient of TV at a voxel from the 13 values of its stencil (c: the voxel, xm / xp
 // the x neighbours, and so on; "xp_ym" the voxel at (+1, -1, 0)).  Each term is a
-// difference over the local gradient magnitude, taken with the hardware reciprocal
-// square root (a few ulp; the correctly rounded square root and division cost most of
-// the kernel's instructions).
+// difference over the local gradient magnitude, taken with the reciprocal square root.
 __device__ __forceinline__ float tv_grad(float v, float vxm, float vym, float vzm, float vxp, float vyp, float vzp,
                                          float xp_ym, float xp_zm, float xm_yp, float yp_zm, float xm_zp, float ym_zp,
                                          float eps)
 {
     const float a0 = v - vxm, b0 = v - vym, c0 = v - vzm;
-    const float r0 = rsqrtf(eps + a0 * a0 + b0 * b0 + c0 * c0);
+    const float r0 = rsqrt_approx(eps + a0 * a0 + b0 * b0 + c0 * c0);
     const float ax = vxp - v, bx = vxp - xp_ym, cx = vxp - xp_zm;
-    const float rx = rsqrtf(eps + ax * ax + bx * bx + cx * cx);
+    const float rx = rsqrt_approx(eps + ax * ax + bx * bx + cx * cx);
     const float ay = vyp - xm_yp, by = vyp - v, cy = vyp - yp_zm;
-    const float ry = rsqrtf(eps + ay * ay + by * by + cy * cy);
+    const float ry = rsqrt_approx(eps + ay * ay + by * by + cy * cy);
     const float az = vzp - xm_zp, bz = vzp - ym_zp, cz = vzp - v;
-    const float rz = rsqrtf(eps + az * az + bz * bz + cz * cz);
+    const float rz = rsqrt_approx(eps + az * az + bz * bz + cz * cz);
     return (a0 + b0 + c0) * r0 - ax * rx - by * ry - cz * rz;
 }
 
-// TV tile: 32 x 8 voxels of a plane per CTA, marching through kZc planes along z with
-// the planes z - 1, z, z + 1 (each with a one-voxel periodic halo) in shared memory,
-// so every input element is read from memory about 1.4 times (halo and chunk ends).
-constexpr int kTx = 32, kTy = 8, kZc = 32;
+// TV tile: 32 x 16 voxels of a plane per CTA (two rows per thread, eight apart),
+// marching through kZc planes along z with the planes z - 1, z, z + 1 (each with a
+// one-voxel periodic halo) in shared memory; the next plane's loads are issued before
+// the current plane is computed.  Every input element is read about 1.3 times.
+constexpr int kTx = 32, kTy = 16, kZc = 32;
+constexpr int kPw = kTx + 2, kPh = kTy + 2, kPlane = kPw * kPh, kLoads = (kPlane + kThreads - 1) / kThreads;
 
 int tv_blocks(int R) { return (R / kTx) * (R / kTy) * (R / kZc); }
+
+template <bool STEP>
+struct TvTile {
+    const float *__restrict__ Vin;
+    const float *__restrict__ gin;
+    float s;
+    int off[kLoads];    // plane offsets of this thread's tile elements (periodic halo)
+    int sidx[kLoads];   // their shared-memory index, -1 when unused
+
+    __device__ __forceinline__ void fetch(int base, float *r) const
+    {
+#pragma unroll
+        for (int j = 0; j < kLoads; j++) {
+            if (sidx[j] < 0) continue;
+            float v = __ldg(&Vin[base + off[j]]);
+            if constexpr (STEP) v = v - s * __ldg(&gin[base + off[j]]);
+            r[j] = v;
+        }
+    }
+    __device__ __forceinline__ void put(float *plane, const float *r) const
+    {
+#pragma unroll
+        for (int j = 0; j < kLoads; j++)
+            if (sidx[j] >= 0) plane[sidx[j]] = r[j];
+    }
+};
+
+// The two voxels of this thread on plane pc (rows ly and ly + 8).
+__device__ __forceinline__ void tv_two(const float (*pm)[kPw], const float (*pc)[kPw], const float (*pp)[kPw], int lx,
+                                       int ly, float eps, float *v, float *g)
+{
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const int y = ly + 8 * h;
+        v[h] = pc[y][lx];
+        g[h] = tv_grad(v[h], pc[y][lx - 1], pc[y - 1][lx], pm[y][lx], pc[y][lx + 1], pc[y + 1][lx], pp[y][lx],
+                       pc[y - 1][lx + 1], pm[y][lx + 1], pc[y + 1][lx - 1], pm[y + 1][lx], pp[y][lx - 1],
+                       pp[y - 1][lx], eps);
+    }
+}
 
 // STEP = false: g = grad TV(Vin).  STEP = true: the volume is Vin - s gin with
 // s = dtvg / |gin| (the previous descent step, applied while the planes are loaded),
 // written to Vout, and gout = grad TV of it.  The last block stores |gout| and, on the
-// first iteration, sets dtvg = alpha Dp.
+// first iteration, sets dtvg = alpha Dp.  Offsets are 32-bit (R^3 < 2^31 for R <= 768).
 template <bool STEP>
 __global__ void __launch_bounds__(kThreads) tv_kernel(const float *__restrict__ Vin, const float *__restrict__ gin,
                                                       float *Vout, float *gout, int R, float eps, PocsCtl *ctl,
                                                       double *part)
 {
-    static_assert(kTx * kTy == kThreads, "one voxel of the tile per thread");
-    constexpr int kPlane = (kTx + 2) * (kTy + 2), kLoads = (kPlane + kThreads - 1) / kThreads;
-    __shared__ float pl[3][kTy + 2][kTx + 2];
-    float s = 0.f;
-    if constexpr (STEP) s = ctl->gnorm > 0.0 ? (float)(ctl->dtvg / ctl->gnorm) : 0.f;
+    static_assert(kTx * kTy == 2 * kThreads, "two voxels of the tile per thread");
+    __shared__ float pl[3][kPh][kPw];
+    TvTile<STEP> t;
+    t.Vin = Vin;
+    t.gin = gin;
+    t.s = 0.f;
+    if constexpr (STEP) t.s = ctl->gnorm > 0.0 ? (float)(ctl->dtvg / ctl->gnorm) : 0.f;
     const int nbx = R / kTx, nby = R / kTy;
     int bi = blockIdx.x;
     const int x0 = (bi % nbx) * kTx;
     bi /= nbx;
     const int y0 = (bi % nby) * kTy, z0 = (bi / nby) * kZc;
-    const long rr = (long)R * R;
-    // the plane elements this thread loads: offsets within a plane (periodic halo)
-    long off[kLoads];
-    int slot_idx[kLoads];
+    const int rr = R * R;
 #pragma unroll
     for (int j = 0; j < kLoads; j++) {
         const int e = threadIdx.x + j * kThreads;
-        slot_idx[j] = e < kPlane ? e : -1;
-        const int lx = e % (kTx + 2), ly = e / (kTx + 2);
+        const int lx = e % kPw, ly = e / kPw;
         int gx = x0 - 1 + lx, gy = y0 - 1 + ly;
         gx = gx < 0 ? gx + R : (gx >= R ? gx - R : gx);
         gy = gy < 0 ? gy + R : (gy >= R ? gy - R : gy);
-        off[j] = e < kPlane ? gx + (long)R * gy : 0;
+        t.sidx[j] = e < kPlane ? e : -1;
+        t.off[j] = e < kPlane ? gx + R * gy : 0;
     }
-    auto fetch = [&](int z, float *r) {
-        const long base = rr * (z < 0 ? z + R : (z >= R ? z - R : z));
-#pragma unroll
-        for (int j = 0; j < kLoads; j++) {
-            if (slot_idx[j] < 0) continue;
-            float v = __ldg(&Vin[base + off[j]]);
-            if constexpr (STEP) v = v - s * __ldg(&gin[base + off[j]]);
-            r[j] = v;
-        }
-    };
-    auto put = [&](int slot, const float *r) {
-        float *p = &pl[slot][0][0];
-#pragma unroll
-        for (int j = 0; j < kLoads; j++)
-            if (slot_idx[j] >= 0) p[slot_idx[j]] = r[j];
-    };
+    auto zbase = [&](int z) { return rr * (z < 0 ? z + R : (z >= R ? z - R : z)); };
     const int tx = threadIdx.x % kTx, ty = threadIdx.x / kTx, lx = tx + 1, ly = ty + 1;
+    const int out0 = (x0 + tx) + R * (y0 + ty);
     float nxt[kLoads];
-    fetch(z0 - 1, nxt);
-    put(0, nxt);
-    fetch(z0, nxt);
-    put(1, nxt);
-    fetch(z0 + 1, nxt);
+    t.fetch(zbase(z0 - 1), nxt);
+    t.put(&pl[0][0][0], nxt);
+    t.fetch(zbase(z0), nxt);
+    t.put(&pl[1][0][0], nxt);
+    t.fetch(zbase(z0 + 1), nxt);
     float acc = 0.f;
+    auto plane_step = [&](int k, float *pnew, const float (*pm)[kPw], const float (*pc)[kPw],
+                          const float (*pp)[kPw]) {
+        t.put(pnew, nxt);   // plane z0 + k + 1
+        __syncthreads();
+        if (k + 1 < kZc) t.fetch(zbase(z0 + k + 2), nxt);   // in flight while this plane is computed
+        float v[2], g[2];
+        tv_two(pm, pc, pp, lx, ly, eps, v, g);
+        const int q = out0 + rr * (z0 + k);
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            if constexpr (STEP) Vout[q + 8 * R * h] = v[h];
+            gout[q + 8 * R * h] = g[h];
+            acc = fmaf(g[h], g[h], acc);
+        }
+        __syncthreads();
+    };
     for (int k = 0; k < kZc; k++) {
-        put((k + 2) % 3, nxt);   // plane z0 + k + 1
-        __syncthreads();
-        if (k + 1 < kZc) fetch(z0 + k + 2, nxt);   // in flight while this plane is computed
-        const float(*pm)[kTx + 2] = pl[k % 3];
-        const float(*pc)[kTx + 2] = pl[(k + 1) % 3];
-        const float(*pp)[kTx + 2] = pl[(k + 2) % 3];
-        const float v = pc[ly][lx];
-        const float g = tv_grad(v, pc[ly][lx - 1], pc[ly - 1][lx], pm[ly][lx], pc[ly][lx + 1], pc[ly + 1][lx],
-                                pp[ly][lx], pc[ly - 1][lx + 1], pm[ly][lx + 1], pc[ly + 1][lx - 1], pm[ly + 1][lx],
-                                pp[ly][lx - 1], pp[ly - 1][lx], eps);
-        const long q = (x0 + tx) + (long)R * (y0 + ty) + rr * (z0 + k);
-        if constexpr (STEP) Vout[q] = v;
-        gout[q] = g;
-        acc = fmaf(g, g, acc);
-        __syncthreads();
+        switch (k % 3) {   // plane slots as constants: z - 1, z, z + 1
+        case 0: plane_step(k, &pl[2][0][0], pl[0], pl[1], pl[2]); break;
+        case 1: plane_step(k, &pl[0][0][0], pl[1], pl[2], pl[0]); break;
+        default: plane_step(k, &pl[1][0][0], pl[2], pl[0], pl[1]); break;
+        }
     }
-    double t;
-    if (grid_sum(acc, part, &ctl->ticket, &t)) {
-        ctl->gnorm = sqrt(t);
+    double tot;
+    if (grid_sum(acc, part, &ctl->ticket, &tot)) {
+        ctl->gnorm = sqrt(tot);
         if (!STEP && ctl->first) {
             ctl->dtvg = ctl->alpha * ctl->dp;
             ctl->first = 0;
@@ -319,18 +367,20 @@ __global__ void __launch_bounds__(kThreads) tv_final_kernel(const float *Vin, co
 __global__ void __launch_bounds__(kThreads) pocs_n_kernel(const float2 *__restrict__ G, int R, float inv_n3,
                                                           float n_med, float2 *ri)
 {
-    const long rr = (long)R * R, n = rr * R;
-    const long i0 = (long)blockIdx.x * (kPer * kThreads) + threadIdx.x;
+    // 32-bit index arithmetic: R^3 < 2^31 for R <= 768
+    const unsigned ur = (unsigned)R, rr = ur * ur, n = rr * ur, h = ur / 2;
+    const unsigned i0 = blockIdx.x * (kPer * kThreads) + threadIdx.x;
     float2 g[kPer];
 #pragma unroll
     for (int k = 0; k < kPer; k++) g[k] = i0 + k * kThreads < n ? G[i0 + k * kThreads] : make_float2(0.f, 0.f);
 #pragma unroll
     for (int k = 0; k < kPer; k++) {
-        const long i = i0 + k * kThreads;
+        const unsigned i = i0 + k * kThreads;
         if (i >= n) continue;
-        const int x = (int)(i % R), y = (int)((i / R) % R), z = (int)(i / rr);
-        ri[((x + R / 2) % R) + R * (long)((y + R / 2) % R) + rr * ((z + R / 2) % R)] =
-            est_n_scaled(g[k], inv_n3, n_med);
+        const unsigned x = i % ur, yz = i / ur, y = yz % ur, z = yz / ur;
+        const unsigned xs = x + h >= ur ? x + h - ur : x + h, ys = y + h >= ur ? y + h - ur : y + h,
+                       zs = z + h >= ur ? z + h - ur : z + h;
+        ri[xs + ur * ys + rr * zs] = est_n_scaled(g[k], inv_n3, n_med);
     }
 }
 
