@@ -122,27 +122,29 @@ __global__ void __launch_bounds__(kThreads) dc_kernel(float2 *G, const float2 *_
 __global__ void __launch_bounds__(kThreads) project_kernel(float2 *G, float *V, float *Vp, long n, float inv_n3,
                                                            PocsCtl *ctl, double *part, bool write_g)
 {
-    const long i0 = (long)blockIdx.x * (kPer * kThreads) + threadIdx.x;
-    float2 g[kPer];
-    float v0[kPer];
-#pragma unroll
-    for (int k = 0; k < kPer; k++) {
-        const long i = i0 + k * kThreads;
-        g[k] = i < n ? G[i] : make_float2(0.f, 0.f);
-        v0[k] = i < n ? V[i] : 0.f;
-    }
     float acc = 0.f;
+    for (long c = blockIdx.x; c * (kPer * kThreads) < n; c += gridDim.x) {
+        const long i0 = c * (kPer * kThreads) + threadIdx.x;
+        float2 g[kPer];
+        float v0[kPer];
 #pragma unroll
-    for (int k = 0; k < kPer; k++) {
-        const long i = i0 + k * kThreads;
-        if (i >= n) continue;
-        const float u = re_sqrt1p_m1(make_float2(g[k].x * inv_n3, g[k].y * inv_n3));
-        const float vn = u > 0.f ? u * (2.0f + u) : 0.f;
-        const float d = vn - v0[k];
-        acc = fmaf(d, d, acc);
-        V[i] = vn;
-        Vp[i] = vn;
-        if (write_g) G[i] = make_float2(vn, 0.f);
+        for (int k = 0; k < kPer; k++) {
+            const long i = i0 + k * kThreads;
+            g[k] = i < n ? G[i] : make_float2(0.f, 0.f);
+            v0[k] = i < n ? V[i] : 0.f;
+        }
+#pragma unroll
+        for (int k = 0; k < kPer; k++) {
+            const long i = i0 + k * kThreads;
+            if (i >= n) continue;
+            const float u = re_sqrt1p_m1(make_float2(g[k].x * inv_n3, g[k].y * inv_n3));
+            const float vn = u > 0.f ? u * (2.0f + u) : 0.f;
+            const float d = vn - v0[k];
+            acc = fmaf(d, d, acc);
+            V[i] = vn;
+            Vp[i] = vn;
+            if (write_g) G[i] = make_float2(vn, 0.f);
+        }
     }
     double t;
     if (grid_sum(acc, part, &ctl->ticket, &t)) ctl->dp = sqrt(t);
@@ -151,17 +153,19 @@ __global__ void __launch_bounds__(kThreads) project_kernel(float2 *G, float *V, 
 __global__ void __launch_bounds__(kThreads) dd_kernel(const float2 *__restrict__ G, const float2 *__restrict__ F2,
                                                       long n, float y_scale, PocsCtl *ctl, double *part)
 {
-    const long i0 = (long)blockIdx.x * (kPer * kThreads) + threadIdx.x;
-    float2 f[kPer];
-#pragma unroll
-    for (int k = 0; k < kPer; k++) f[k] = i0 + k * kThreads < n ? F2[i0 + k * kThreads] : make_float2(0.f, 0.f);
     float acc = 0.f;
+    for (long c = blockIdx.x; c * (kPer * kThreads) < n; c += gridDim.x) {
+        const long i0 = c * (kPer * kThreads) + threadIdx.x;
+        float2 f[kPer];
 #pragma unroll
-    for (int k = 0; k < kPer; k++) {
-        if (f[k].x != 0.f || f[k].y != 0.f) {
-            const float2 g = G[i0 + k * kThreads];
-            const float dx = g.x - f[k].x * y_scale, dy = g.y - f[k].y * y_scale;
-            acc = fmaf(dx, dx, fmaf(dy, dy, acc));
+        for (int k = 0; k < kPer; k++) f[k] = i0 + k * kThreads < n ? F2[i0 + k * kThreads] : make_float2(0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < kPer; k++) {
+            if (f[k].x != 0.f || f[k].y != 0.f) {
+                const float2 g = G[i0 + k * kThreads];
+                const float dx = g.x - f[k].x * y_scale, dy = g.y - f[k].y * y_scale;
+                acc = fmaf(dx, dx, fmaf(dy, dy, acc));
+            }
         }
     }
     double t;
@@ -326,25 +330,27 @@ __global__ void __launch_bounds__(kThreads) tv_final_kernel(const float *Vin, co
                                                             PocsCtl *ctl, double *part, double *hist)
 {
     const float s = ctl->gnorm > 0.0 ? (float)(ctl->dtvg / ctl->gnorm) : 0.f;
-    const long i0 = (long)blockIdx.x * (kPer * kThreads) + threadIdx.x;
-    float vi[kPer], gi[kPer], pi[kPer];
-#pragma unroll
-    for (int k = 0; k < kPer; k++) {
-        const long i = i0 + k * kThreads;
-        vi[k] = i < n ? Vin[i] : 0.f;
-        gi[k] = i < n ? gin[i] : 0.f;
-        pi[k] = i < n ? Vp[i] : 0.f;
-    }
     float acc = 0.f;
+    for (long c = blockIdx.x; c * (kPer * kThreads) < n; c += gridDim.x) {
+        const long i0 = c * (kPer * kThreads) + threadIdx.x;
+        float vi[kPer], gi[kPer], pi[kPer];
 #pragma unroll
-    for (int k = 0; k < kPer; k++) {
-        const long i = i0 + k * kThreads;
-        if (i >= n) continue;
-        const float v = vi[k] - s * gi[k];
-        const float d = v - pi[k];
-        acc = fmaf(d, d, acc);
-        V[i] = v;
-        G[i] = make_float2(v, 0.f);
+        for (int k = 0; k < kPer; k++) {
+            const long i = i0 + k * kThreads;
+            vi[k] = i < n ? Vin[i] : 0.f;
+            gi[k] = i < n ? gin[i] : 0.f;
+            pi[k] = i < n ? Vp[i] : 0.f;
+        }
+#pragma unroll
+        for (int k = 0; k < kPer; k++) {
+            const long i = i0 + k * kThreads;
+            if (i >= n) continue;
+            const float v = vi[k] - s * gi[k];
+            const float d = v - pi[k];
+            acc = fmaf(d, d, acc);
+            V[i] = v;
+            G[i] = make_float2(v, 0.f);
+        }
     }
     double t;
     if (grid_sum(acc, part, &ctl->ticket, &t)) {
@@ -386,6 +392,15 @@ __global__ void __launch_bounds__(kThreads) pocs_n_kernel(const float2 *__restri
 
 unsigned grid_for(long n) { return (unsigned)((n + kPer * kThreads - 1) / (kPer * kThreads)); }
 
+// Reducing elementwise kernels: at most 8 CTAs per SM of 152, each looping over chunks
+// (one ticket atomic per CTA).
+constexpr unsigned kReduceGrid = 8 * 152;
+unsigned grid_reduce(long n)
+{
+    const unsigned g = grid_for(n);
+    return g < kReduceGrid ? g : kReduceGrid;
+}
+
 cudaError_t fft3_unscaled(float2 *G, int R, bool inverse, cudaStream_t s)
 {
     const long rr = (long)R * R;
@@ -419,16 +434,15 @@ cudaError_t pocs_iteration(const PocsBufs &b, int tv_steps, bool want_dd, cudaSt
 {
     const int R = b.R;
     const long n = (long)R * R * R;
-    const unsigned grid = grid_for(n);
     const float inv_n3 = 1.0f / (float)n;
     cudaError_t e = data_step(b, s);
     if (e != cudaSuccess) return e;
-    project_kernel<<<grid, kThreads, 0, s>>>(b.G, b.V, b.Vp, n, inv_n3, b.ctl, b.part, want_dd);
+    project_kernel<<<grid_reduce(n), kThreads, 0, s>>>(b.G, b.V, b.Vp, n, inv_n3, b.ctl, b.part, want_dd);
     note_launch();
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if (want_dd) {
         if ((e = fft3_unscaled(b.G, R, false, s)) != cudaSuccess) return e;
-        dd_kernel<<<grid, kThreads, 0, s>>>(b.G, b.F2, n, b.y_scale, b.ctl, b.part);
+        dd_kernel<<<grid_reduce(n), kThreads, 0, s>>>(b.G, b.F2, n, b.y_scale, b.ctl, b.part);
         note_launch();
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
@@ -448,7 +462,7 @@ cudaError_t pocs_iteration(const PocsBufs &b, int tv_steps, bool want_dd, cudaSt
         vin = nv;
         gin = ng;
     }
-    tv_final_kernel<<<grid, kThreads, 0, s>>>(vin, gin, b.V, b.Vp, b.G, n, b.ctl, b.part, b.hist);
+    tv_final_kernel<<<grid_reduce(n), kThreads, 0, s>>>(vin, gin, b.V, b.Vp, b.G, n, b.ctl, b.part, b.hist);
     note_launch();
     return cudaGetLastError();
 }
