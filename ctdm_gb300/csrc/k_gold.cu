@@ -38,6 +38,22 @@ __device__ __forceinline__ float res_term(float a, float b)
     return __double2float_rn(__dsub_rn((double)r, CTDM_PI_D));
 }
 
+// The same wrapped difference in float alone, with `sure` cleared when a - b + pi lies
+// within 1e-4 (relative to 2 pi) of a multiple of 2 pi, where the rounding of the exact
+// expression decides between -pi and +pi.  Elsewhere the two differ by a few ulp.
+__device__ __forceinline__ float res_term_fast(float a, float b, bool &sure)
+{
+    const float m = (float)(CTDM_PI_D * 2);
+    const float x = (a - b) + (float)CTDM_PI_D;
+    const float q = x * (float)(1.0 / (CTDM_PI_D * 2));
+    const float k = floorf(q), f = q - k;
+    if (f < 1e-4f || f > 1.0f - 1e-4f) sure = false;
+    return fmaf(-k, m, x) - (float)CTDM_PI_D;
+}
+
+// Charges: the float evaluation decides every pixel whose terms are clear of the wrap
+// boundaries and whose sum is more than 1e-3 from +-6 (its error is below 1e-5); the
+// exact expression of cudaPhaseResidues runs for the rest, so the charges are the same.
 __global__ void residues_kernel(const float *__restrict__ phi, int W, int H, int8_t *q)
 {
     const int a = blockIdx.z;
@@ -47,12 +63,19 @@ __global__ void residues_kernel(const float *__restrict__ phi, int W, int H, int
     const float *p = phi + a * n;
     int8_t v = 0;
     if (x != W - 1 && y != H - 1) {
-        const float r1 = res_term(p[x + (long)W * y], p[(x + 1) + (long)W * y]);
-        const float r2 = res_term(p[(x + 1) + (long)W * y], p[(x + 1) + (long)W * (y + 1)]);
-        const float r3 = res_term(p[(x + 1) + (long)W * (y + 1)], p[x + (long)W * (y + 1)]);
-        const float r4 = res_term(p[x + (long)W * (y + 1)], p[x + (long)W * y]);
-        const float t = __fadd_rn(__fadd_rn(__fadd_rn(r1, r2), r3), r4);
-        v = t >= 6.0f ? 1 : (t <= -6.0f ? -1 : 0);
+        const float p00 = p[x + (long)W * y], p10 = p[(x + 1) + (long)W * y];
+        const float p11 = p[(x + 1) + (long)W * (y + 1)], p01 = p[x + (long)W * (y + 1)];
+        bool sure = true;
+        const float t0 = res_term_fast(p00, p10, sure) + res_term_fast(p10, p11, sure) +
+                         res_term_fast(p11, p01, sure) + res_term_fast(p01, p00, sure);
+        if (sure && fabsf(fabsf(t0) - 6.0f) > 1e-3f) {
+            v = t0 >= 6.0f ? 1 : (t0 <= -6.0f ? -1 : 0);
+        } else {
+            const float r1 = res_term(p00, p10), r2 = res_term(p10, p11);
+            const float r3 = res_term(p11, p01), r4 = res_term(p01, p00);
+            const float t = __fadd_rn(__fadd_rn(__fadd_rn(r1, r2), r3), r4);
+            v = t >= 6.0f ? 1 : (t <= -6.0f ? -1 : 0);
+        }
     }
     q[a * n + x + (long)W * y] = v;
 }
