@@ -584,14 +584,24 @@ def run_ours(args):
         return
 
     r3 = float(r) ** 3
-    bytes_per = {"x_pass": 16 * r3, "y_forward": 16 * r3, "y_inverse": 16 * r3, "z_pass": 24 * r3,
-                 "ewald": A * 8.0 * r * r + 16 * r3}
+    # Algorithmic HBM bytes per launch of each timed stage.  With the plane scheme the
+    # x-pass stage is the plane pass (whole planes' x and y transforms, 16 R^3 bytes);
+    # the z pass reads the measured samples packed per tile (G in and out, the kept
+    # values, one mask word per (tile of 16 lines, z)).
+    scheme = C.loop_scheme(r, device=local)
+    F2 = ctx.read_buffer(7, np.complex64)
+    measured = int(np.count_nonzero((F2.real != 0) & (F2.imag != 0)))
+    del F2
+    bytes_per = {"x_pass": 16 * r3, "y_forward": 16 * r3, "y_inverse": 16 * r3,
+                 "z_pass": 16 * r3 + 8.0 * measured + 4 * r3 / 16, "ewald": A * 8.0 * r * r + 16 * r3}
+    kernel_of = {"x_pass": "plane_pass" if scheme in (1, 2) else "x_pass", "y_forward": "y_forward",
+                 "y_inverse": "y_inverse", "z_pass": "z_pass_packed", "ewald": "ewald"}
     best = max(bytes_per, key=lambda k: stages[k][0])
     ms_total, cnt = stages[best]
     avg_ms = ms_total / max(cnt, 1)
     achieved = bytes_per[best] / (avg_ms * 1e-3) / 1e9
     peak, peak_kind = measured_peaks()
-    traffic = ncu_traffic(best, args.config)
+    traffic = ncu_traffic(kernel_of[best], args.config)
     cpu_s, cores, text = cpu_sample(acq, cfg["iterations"], cfg["goldstein"])
     tomos = world * args.steps
     line = {
@@ -614,7 +624,8 @@ def run_ours(args):
                 "h2d_bytes_per_step": int(acq.holograms.nbytes + acq.background.nbytes),
                 "d2h_bytes_per_step": int(r3 * 8)},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "kernel": best, "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "roofline": {"bound": "hbm", "kernel": kernel_of[best], "stage": best, "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "loop_scheme": scheme, "measured_voxels": measured,
                      "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
                      "bytes_per_launch": bytes_per[best], "avg_launch_ms": avg_ms},
         "stages_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in stages.items()},
