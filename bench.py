@@ -507,6 +507,8 @@ def run_ours(args):
     cfg = CONFIGS[args.config]
     acq = make_workload(args.config, seed=1000 + rank)
     A = len(acq.ang_x)
+    if args.loop_scheme >= 0:
+        C.set_loop_scheme(acq.r_vol, args.loop_scheme, device=local)
     p = C.params_for(acq, cfg["iterations"], run_goldstein=int(cfg["goldstein"]))
     ctx = C.Context(local)
     holo = torch.from_numpy(acq.holograms).to(dev)
@@ -688,6 +690,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="wrap_heavy", choices=sorted(CONFIGS))
+    ap.add_argument("--loop-scheme", type=int, default=-1, choices=[-1, 0, 1, 2],
+                    help="positivity-loop scheme of the volume side (-1: the autotuner's choice)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
