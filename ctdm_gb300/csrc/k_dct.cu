@@ -21,12 +21,25 @@ namespace ctdm {
 
 using fftl::Plan;
 
-// NumericDerivative1 wrap: t - 2 pi sign(t) floor(|pi sign(t) + t| / 2 pi),
-// evaluated in double as the reference expression is; it is exactly t when
-// |t| < pi, so the double path only runs on wrapped differences.
+// NumericDerivative1 wrap: t - 2 pi sign(t) floor(|pi sign(t) + t| / 2 pi), which
+// the reference evaluates in double; it is exactly t when |t| < pi.  For a wrapped
+// difference (|t| < 4 pi, so the floor q is 0, 1 or 2) the float form
+// |t| - q fl(2 pi) is exact (Sterbenz) and subtracting q (2 pi - fl(2 pi)) rounds
+// once, which is the double expression's value; the double expression itself runs
+// only where q is in doubt (the quotient within 1e-5 of an integer).  GB300's FP64
+// rate made the double form the most expensive part of the row pass.
 __device__ __forceinline__ float wrap_grad(float t)
 {
     if (fabsf(t) < 3.14159f) return t;
+    const float u = fabsf(t);
+    const float v = (u + (float)CTDM_PI_D) * (float)(0.5 / CTDM_PI_D);
+    const float q = floorf(v), f = v - q;
+    if (u < 15.0f && f > 1e-5f && f < 1.0f - 1e-5f) {
+        const float p1 = (float)(2 * CTDM_PI_D);
+        const float p2 = (float)(2 * CTDM_PI_D - (double)(float)(2 * CTDM_PI_D));
+        const float r = (u - q * p1) - q * p2;
+        return t < 0.f ? -r : r;
+    }
     const double s = t > 0.f ? 1.0 : (t < 0.f ? -1.0 : 0.0);
     const double td = (double)t;
     const double q = floor(fabs(__dadd_rn(CTDM_PI_D * s, td)) / (CTDM_PI_D * 2));

@@ -265,10 +265,22 @@ __device__ __forceinline__ bool ub_at_visit(const uint8_t *st, int nb, int p)
 }
 
 // ref + atan2(sin D, cos D), D = phi - ref: the wrap of D into (-pi, pi] computed
-// as D - 2 pi round(D / 2 pi) in double, then rounded to float.
+// as D - 2 pi round(D / 2 pi) in double, then rounded to float.  In float: with
+// k = rint(D / 2 pi) decided away from the halfway points, D - k fl(2 pi) is a multiple
+// of 2^-21 below pi in magnitude, so the first fma is exact and the second rounds
+// D - k 2 pi once, the double expression's value; the double form runs only near the
+// halfway points (GB300's FP64 divide made it most of the fill's arithmetic).
 __device__ __forceinline__ float unwrap_from(float ref, float ph)
 {
     const float d = __fsub_rn(ph, ref);
+    const float qf = d * (float)(0.5 / CTDM_PI_D);
+    const float kf = rintf(qf);
+    if (fabsf(fabsf(qf - kf) - 0.5f) > 1e-5f && fabsf(d) < 1e6f) {
+        const float p1 = (float)(2 * CTDM_PI_D);
+        const float p2 = (float)(2 * CTDM_PI_D - (double)(float)(2 * CTDM_PI_D));
+        const float a = fmaf(-kf, p1, d);
+        return __fadd_rn(ref, fmaf(-kf, p2, a));
+    }
     const double dd = (double)d;
     const double k = rint(__ddiv_rn(dd, 2.0 * CTDM_PI_D));
     const float dp = __double2float_rn(__dsub_rn(dd, __dmul_rn(k, 2.0 * CTDM_PI_D)));
