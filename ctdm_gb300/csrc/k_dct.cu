@@ -33,11 +33,11 @@ __device__ __forceinline__ float wrap_grad(float t)
     if (fabsf(t) < 3.14159f) return t;
     const float u = fabsf(t);
     const float v = (u + (float)CTDM_PI_D) * (float)(0.5 / CTDM_PI_D);
-    const float q = floorf(v), f = v - q;
+    const float qf = floorf(v), f = v - qf;
     if (u < 15.0f && f > 1e-5f && f < 1.0f - 1e-5f) {
         const float p1 = (float)(2 * CTDM_PI_D);
         const float p2 = (float)(2 * CTDM_PI_D - (double)(float)(2 * CTDM_PI_D));
-        const float r = (u - q * p1) - q * p2;
+        const float r = (u - qf * p1) - qf * p2;
         return t < 0.f ? -r : r;
     }
     const double s = t > 0.f ? 1.0 : (t < 0.f ? -1.0 : 0.0);
