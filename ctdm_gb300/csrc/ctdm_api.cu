@@ -249,8 +249,20 @@ struct ctdm_ctx {
     // side stream for work whose result the reconstruction does not consume
     cudaStream_t side = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr;
+    // host-buffer uploads: a copy stream and one event per chunk of angles
+    static const int kChunks = 16;
+    cudaStream_t copy = nullptr;
+    cudaEvent_t ready[kChunks + 1] = {};
     // device status word (bounded device-side waits record a code here)
     int *d_err = nullptr;
+};
+
+// Angles [k per, (k + 1) per) of the hologram stack become valid on the device at
+// event ready[k] (host-buffer calls upload them in chunks while the front end of the
+// earlier chunks runs).
+struct ChunkFeed {
+    const cudaEvent_t *ready;
+    int per;
 };
 
 static cudaError_t ensure(ctdm_ctx *c, int id, size_t bytes)
@@ -300,6 +312,9 @@ extern "C" ctdm_status ctdm_ctx_create(int device, ctdm_ctx **out)
     if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, prio_lo);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->copy, cudaStreamNonBlocking);
+    for (int k = 0; k <= ctdm_ctx::kChunks && e == cudaSuccess; k++)
+        e = cudaEventCreateWithFlags(&c->ready[k], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_err, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(c->d_err, 0, sizeof(int));
     if (e != cudaSuccess) {
@@ -322,6 +337,9 @@ extern "C" void ctdm_ctx_destroy(ctdm_ctx *c)
     for (int i = 0; i < 2 * StageTimer::kSide; i++)
         if (c->timer.side[i]) cudaEventDestroy(c->timer.side[i]);
     if (c->side) cudaStreamDestroy(c->side);
+    if (c->copy) cudaStreamDestroy(c->copy);
+    for (cudaEvent_t e : c->ready)
+        if (e) cudaEventDestroy(e);
     if (c->d_err) cudaFree(c->d_err);
     for (cudaEvent_t e : {c->fork, c->join})
         if (e) cudaEventDestroy(e);
@@ -446,8 +464,17 @@ static ctdm_status upload_geometry(ctdm_ctx *c, const float *angx, const float *
 // ---------------------------------------------------------------- stage helpers
 static const int kMaxAngles = 512;
 
-static ctdm_status do_qpi(ctdm_ctx *c, int N, int M, int A, const float *holo, const float *bg, int bg_per_angle,
-                          const int *carrier_in, float *phase, float *amp, cudaStream_t s)
+// QPI Algorithm A, first part: window side checks, the carrier (given or detected from
+// the first background) and the background field(s).
+static long qpi_chunk(int N, int M, int A)
+{
+    long chunk = (64l << 20) / ((long)N * M * 8);   // window chunk: T1 <= 64 MB
+    if (chunk < 2) chunk = 2;
+    return chunk > A ? A : chunk;
+}
+
+static ctdm_status qpi_setup(ctdm_ctx *c, int N, int M, int A, const float *bg, int bg_per_angle,
+                             const int *carrier_in, cudaStream_t s)
 {
     if (N < 64 || N > 2048 || (N & (N - 1))) return invalid("hologram side %d unsupported", N);
     if (!ok_length(M) || M > N) return invalid("window side %d unsupported", M);
@@ -465,10 +492,7 @@ static ctdm_status do_qpi(ctdm_ctx *c, int N, int M, int A, const float *holo, c
         CK(qpi_find_carrier(bg, N, B<float2>(c, B_SCRATCH), B<unsigned long long>(c, B_KEY), car, s),
            "carrier search");
     }
-    // window chunk: T1 <= 64 MB
-    long chunk = (64l << 20) / ((long)N * M * 8);
-    if (chunk < 2) chunk = 2;
-    if (chunk > A) chunk = A;
+    const long chunk = qpi_chunk(N, M, A);
     const long mm = (long)M * M, nn = (long)N * N;
     CK(ensure(c, B_T1, sizeof(float2) * chunk * N * M), "alloc T1");
     CK(ensure(c, B_S, sizeof(float2) * chunk * mm), "alloc S");
@@ -481,8 +505,19 @@ static ctdm_status do_qpi(ctdm_ctx *c, int N, int M, int A, const float *holo, c
                               s),
            "qpi bg inv");
     }
-    for (long a0 = 0; a0 < A; a0 += chunk) {
-        const int ac = (int)std::min<long>(chunk, A - a0);
+    return CTDM_OK;
+}
+
+// Second part: phase and amplitude of angles [first, first + count) (holo: the whole
+// stack; the background fields of qpi_setup).
+static ctdm_status qpi_angles(ctdm_ctx *c, int N, int M, int A, int first, int count, const float *holo,
+                              int bg_per_angle, float *phase, float *amp, cudaStream_t s)
+{
+    const long chunk = qpi_chunk(N, M, A);
+    const long mm = (long)M * M, nn = (long)N * N;
+    const int *car = B<int>(c, B_CARRIER);
+    for (long a0 = first; a0 < first + count; a0 += chunk) {
+        const int ac = (int)std::min<long>(chunk, first + count - a0);
         CK(qpi_forward_window(holo + a0 * nn, ac, N, M, car, B<float2>(c, B_T1), B<float2>(c, B_S), s), "qpi fwd");
         const float2 *bgf = B<float2>(c, B_BGF) + (bg_per_angle ? a0 * mm : 0);
         CK(qpi_inverse_window(B<float2>(c, B_S), ac, M, nullptr, bgf, bg_per_angle ? mm : 0, phase + a0 * mm,
@@ -490,6 +525,14 @@ static ctdm_status do_qpi(ctdm_ctx *c, int N, int M, int A, const float *holo, c
            "qpi inv");
     }
     return CTDM_OK;
+}
+
+static ctdm_status do_qpi(ctdm_ctx *c, int N, int M, int A, const float *holo, const float *bg, int bg_per_angle,
+                          const int *carrier_in, float *phase, float *amp, cudaStream_t s)
+{
+    ctdm_status st = qpi_setup(c, N, M, A, bg, bg_per_angle, carrier_in, s);
+    if (st != CTDM_OK) return st;
+    return qpi_angles(c, N, M, A, 0, A, holo, bg_per_angle, phase, amp, s);
 }
 
 static ctdm_status do_positivity(ctdm_ctx *c, int R, int iters, int check_mode, double k2, double n_med,
@@ -630,7 +673,8 @@ static ctdm_status validate(const ctdm_params *p, int A, int &M)
 // makes no host-synchronous call once the context's workspace has grown to the
 // call's sizes, so a warmed-up call can be captured into a CUDA graph.
 static ctdm_status pipeline_core(ctdm_ctx *c, const ctdm_params *p, int A, int M, const float *d_holo,
-                                 const float *d_bg, const AngleGeom *d_geom, ctdm_cfloat *d_ri, cudaStream_t s)
+                                 const float *d_bg, const AngleGeom *d_geom, ctdm_cfloat *d_ri, cudaStream_t s,
+                                 const ChunkFeed *feed = nullptr)
 {
     ctdm_status st;
     const int N = p->n_holo, R = p->r_vol;
@@ -649,16 +693,22 @@ static ctdm_status pipeline_core(ctdm_ctx *c, const ctdm_params *p, int A, int M
     StageTimer &tm = c->timer;
     tm.start(s);
     const int car_in[3] = {p->carrier_r, p->carrier_c, p->carrier_radius};
-    if (p->qpi_method == CTDM_QPI_B) {
+    const bool alg_b = p->qpi_method == CTDM_QPI_B;
+    const int per = feed ? feed->per : A;
+    const int nchunks = (A + per - 1) / per;
+    if (alg_b) {
+        // Algorithm B takes its carrier columns from frame 1 and the background and then
+        // runs on the whole stack: it waits for every chunk
+        for (int k = 0; feed && k < nchunks; k++) CK(cudaStreamWaitEvent(s, feed->ready[k], 0), "wait for holograms");
         const int cen_in[2] = {p->carrier_c, p->carrier_c};
         st = do_qpi_b(c, N, A, d_holo, d_bg, p->bg_per_angle, cen_in, B<float>(c, B_PHASE), B<float>(c, B_AMP), s);
+        if (st != CTDM_OK) return st;
+        tm.mark(S_QPI, s);
     } else {
-        st = do_qpi(c, N, M, A, d_holo, d_bg, p->bg_per_angle, car_in, B<float>(c, B_PHASE), B<float>(c, B_AMP), s);
+        st = qpi_setup(c, N, M, A, d_bg, p->bg_per_angle, car_in, s);
+        if (st != CTDM_OK) return st;
     }
-    if (st != CTDM_OK) return st;
-    tm.mark(S_QPI, s);
 
-    const float *unwrapped = B<float>(c, B_PHU);
     // Goldstein: when its phase does not feed the reconstruction it runs on the side
     // stream (latency-bound, one CTA per map) beside the memory-bound passes, and the
     // call's stream joins it at the end.
@@ -672,43 +722,66 @@ static ctdm_status pipeline_core(ctdm_ctx *c, const ctdm_params *p, int A, int M
         CK(ensure(c, B_GLIST, sizeof(int) * 5 * A * mm), "alloc goldstein lists");
         CK(ensure(c, B_GSTATUS, sizeof(int) * A), "alloc goldstein status");
         CK(ensure(c, B_GWORK, A * mm), "alloc goldstein work");
-        cudaStream_t gs = s;
-        if (gold_side) {
-            CK(cudaEventRecord(c->fork, s), "fork");
-            CK(cudaStreamWaitEvent(c->side, c->fork, 0), "fork wait");
-            gs = c->side;
-            tm.side_mark(gs);
-        }
-        CK(goldstein_residues(B<float>(c, B_PHASE), A, M, M, B<int8_t>(c, B_CHG), gs), "goldstein residues");
-        CK(goldstein_cuts(B<int8_t>(c, B_CHG), A, M, M, B<uint8_t>(c, B_CUT), B<int8_t>(c, B_GWORK), gs),
-           "goldstein cuts");
-        CK(goldstein_floodfill(B<uint8_t>(c, B_CUT), B<float>(c, B_PHASE), A, M, M, B<float>(c, B_GOLD),
-                               B<uint8_t>(c, B_GSTATE), B<int>(c, B_GLIST), B<int>(c, B_GSTATUS), gs),
-           "goldstein flood fill");
-        if (gold_side) {
-            tm.side_mark(gs);
-            CK(cudaEventRecord(c->join, gs), "join");
-        } else {
-            tm.mark(S_GOLD, s);
-        }
     }
-    if (p->unwrap_method == CTDM_METHOD_DCT) {
-        CK(dct_unwrap(B<float>(c, B_PHASE), B<float>(c, B_PHU), B<float>(c, B_DCT), A, M, p->unwrap_mode, s),
-           "dct unwrap");
-    } else if (p->unwrap_method == CTDM_METHOD_FAST) {
+    if (p->unwrap_method == CTDM_METHOD_FAST) {
         CK(ensure(c, B_FASTIN, sizeof(float) * A * mm), "alloc fast-unwrap input");
         CK(ensure(c, B_FASTW, sizeof(float2) * 3 * 4 * mm), "alloc fast-unwrap work");
-        CK(cudaMemcpyAsync(c->buf[B_FASTIN], c->buf[B_PHASE], sizeof(float) * A * mm, cudaMemcpyDeviceToDevice, s),
-           "copy phase");
-        CK(fast_unwrap(B<float>(c, B_FASTIN), B<float>(c, B_PHU), B<float2>(c, B_FASTW), A, M, s), "fast unwrap");
-    } else {
-        unwrapped = B<float>(c, B_GOLD);
     }
-    tm.mark(S_UNWRAP, s);
-    CK(prep_rytov(unwrapped, B<float>(c, B_AMP), A, M, N, R, B<float2>(c, B_U), s), "prep");
-    CK(fft_rows(B<float2>(c, B_U), R, (long)A * R, false, s), "spectra rows");
-    CK(fft_cols(B<float2>(c, B_U), R, (long)A * R, R, rr, R, false, s), "spectra cols");
-    tm.mark(S_SPECTRA, s);
+    const float *unwrapped =
+        p->unwrap_method == CTDM_METHOD_GOLDSTEIN ? B<float>(c, B_GOLD) : B<float>(c, B_PHU);
+    // Front end per chunk of angles (one chunk unless the holograms arrive in chunks):
+    // QPI, Goldstein, unwrapping, spectra.
+    for (int k = 0; k < nchunks; k++) {
+        const int a0 = k * per, ac = std::min(per, A - a0);
+        const long o = (long)a0 * mm;
+        float *phase = B<float>(c, B_PHASE) + o;
+        if (!alg_b) {
+            if (feed) CK(cudaStreamWaitEvent(s, feed->ready[k], 0), "wait for holograms");
+            st = qpi_angles(c, N, M, A, a0, ac, d_holo, p->bg_per_angle, B<float>(c, B_PHASE), B<float>(c, B_AMP),
+                            s);
+            if (st != CTDM_OK) return st;
+            tm.mark(S_QPI, s);
+        }
+        if (run_gold) {
+            cudaStream_t gs = s;
+            if (gold_side) {
+                CK(cudaEventRecord(c->fork, s), "fork");
+                CK(cudaStreamWaitEvent(c->side, c->fork, 0), "fork wait");
+                gs = c->side;
+                tm.side_mark(gs);
+            }
+            CK(goldstein_residues(phase, ac, M, M, B<int8_t>(c, B_CHG) + o, gs), "goldstein residues");
+            CK(goldstein_cuts(B<int8_t>(c, B_CHG) + o, ac, M, M, B<uint8_t>(c, B_CUT) + o, B<int8_t>(c, B_GWORK) + o,
+                              gs),
+               "goldstein cuts");
+            CK(goldstein_floodfill(B<uint8_t>(c, B_CUT) + o, phase, ac, M, M, B<float>(c, B_GOLD) + o,
+                                   B<uint8_t>(c, B_GSTATE) + o, B<int>(c, B_GLIST) + 5 * o, B<int>(c, B_GSTATUS) + a0,
+                                   gs),
+               "goldstein flood fill");
+            if (gold_side) {
+                tm.side_mark(gs);
+                if (k == nchunks - 1) CK(cudaEventRecord(c->join, gs), "join");
+            } else {
+                tm.mark(S_GOLD, s);
+            }
+        }
+        if (p->unwrap_method == CTDM_METHOD_DCT) {
+            CK(dct_unwrap(phase, B<float>(c, B_PHU) + o, B<float>(c, B_DCT) + o, ac, M, p->unwrap_mode, s),
+               "dct unwrap");
+        } else if (p->unwrap_method == CTDM_METHOD_FAST) {
+            CK(cudaMemcpyAsync(B<float>(c, B_FASTIN) + o, phase, sizeof(float) * ac * mm, cudaMemcpyDeviceToDevice,
+                               s),
+               "copy phase");
+            CK(fast_unwrap(B<float>(c, B_FASTIN) + o, B<float>(c, B_PHU) + o, B<float2>(c, B_FASTW), ac, M, s),
+               "fast unwrap");
+        }
+        tm.mark(S_UNWRAP, s);
+        float2 *U = B<float2>(c, B_U) + (long)a0 * rr;
+        CK(prep_rytov(unwrapped + o, B<float>(c, B_AMP) + o, ac, M, N, R, U, s), "prep");
+        CK(fft_rows(U, R, (long)ac * R, false, s), "spectra rows");
+        CK(fft_cols(U, R, (long)ac * R, R, rr, R, false, s), "spectra cols");
+        tm.mark(S_SPECTRA, s);
+    }
 
     const double fm0 = p->n_med / p->wavelength;
     const double df = 1.0 / (R * p->dx);
@@ -737,6 +810,19 @@ static ctdm_status pipeline_core(ctdm_ctx *c, const ctdm_params *p, int A, int M
     return CTDM_OK;
 }
 
+// The whole path with host angles: geometry upload, pipeline, carrier readback.
+static ctdm_status reconstruct_core(ctdm_ctx *c, const ctdm_params *p, int A, int M, const float *d_holo,
+                                    const float *d_bg, const float *h_angx, const float *h_angy, ctdm_cfloat *d_ri,
+                                    cudaStream_t s, const ChunkFeed *feed)
+{
+    ctdm_status st = upload_geometry(c, h_angx, h_angy, A, p->n_med / p->wavelength, 1.0 / (p->r_vol * p->dx), s);
+    if (st != CTDM_OK) return st;
+    st = pipeline_core(c, p, A, M, d_holo, d_bg, B<AngleGeom>(c, B_GEOM), d_ri, s, feed);
+    if (st != CTDM_OK) return st;
+    CK(cudaMemcpyAsync(c->carrier, c->buf[B_CARRIER], sizeof(int) * 3, cudaMemcpyDeviceToHost, s), "carrier readback");
+    return CTDM_OK;
+}
+
 extern "C" ctdm_status ctdm_reconstruct_device(ctdm_ctx *c, const ctdm_params *p, int A, const float *d_holo,
                                                const float *d_bg, const float *h_angx, const float *h_angy,
                                                ctdm_cfloat *d_ri, void *stream)
@@ -746,12 +832,8 @@ extern "C" ctdm_status ctdm_reconstruct_device(ctdm_ctx *c, const ctdm_params *p
     ctdm_status st = validate(p, A, M);
     if (st != CTDM_OK) return st;
     CK(cudaSetDevice(c->device), "cudaSetDevice");
-    cudaStream_t s = (cudaStream_t)stream;
-    st = upload_geometry(c, h_angx, h_angy, A, p->n_med / p->wavelength, 1.0 / (p->r_vol * p->dx), s);
+    st = reconstruct_core(c, p, A, M, d_holo, d_bg, h_angx, h_angy, d_ri, (cudaStream_t)stream, nullptr);
     if (st != CTDM_OK) return st;
-    st = pipeline_core(c, p, A, M, d_holo, d_bg, B<AngleGeom>(c, B_GEOM), d_ri, s);
-    if (st != CTDM_OK) return st;
-    CK(cudaMemcpyAsync(c->carrier, c->buf[B_CARRIER], sizeof(int) * 3, cudaMemcpyDeviceToHost, s), "carrier readback");
     g_err.clear();
     return CTDM_OK;
 }
@@ -798,10 +880,27 @@ extern "C" ctdm_status ctdm_reconstruct(ctdm_ctx *c, const ctdm_params *p, int A
     CK(ensure(c, B_BG, sizeof(float) * nbg * nn), "alloc background");
     CK(ensure(c, B_RI, sizeof(float2) * r3), "alloc volume");
     cudaStream_t s = 0;
-    CK(cudaMemcpyAsync(c->buf[B_BG], h_bg, sizeof(float) * nbg * nn, cudaMemcpyHostToDevice, s), "upload background");
-    CK(cudaMemcpyAsync(c->buf[B_HOLO], h_holo, sizeof(float) * A * nn, cudaMemcpyHostToDevice, s), "upload holograms");
-    st = ctdm_reconstruct_device(c, p, A, B<float>(c, B_HOLO), B<float>(c, B_BG), h_angx, h_angy,
-                                 B<ctdm_cfloat>(c, B_RI), s);
+    // the backgrounds first, then the holograms in chunks of angles on the copy stream:
+    // the front end of a chunk (QPI, unwrapping, Goldstein, spectra) runs while the
+    // later chunks are still in flight over the host link
+    const int per = std::max(8, (A + ctdm_ctx::kChunks - 1) / ctdm_ctx::kChunks);
+    const int nchunks = (A + per - 1) / per;
+    CK(cudaEventRecord(c->ready[ctdm_ctx::kChunks], s), "copy start");
+    CK(cudaStreamWaitEvent(c->copy, c->ready[ctdm_ctx::kChunks], 0), "copy start");
+    CK(cudaMemcpyAsync(c->buf[B_BG], h_bg, sizeof(float) * nbg * nn, cudaMemcpyHostToDevice, c->copy),
+       "upload background");
+    CK(cudaEventRecord(c->ready[ctdm_ctx::kChunks], c->copy), "background uploaded");
+    for (int k = 0; k < nchunks; k++) {
+        const long a0 = (long)k * per, ac = std::min<long>(per, A - a0);
+        CK(cudaMemcpyAsync(B<float>(c, B_HOLO) + a0 * nn, h_holo + a0 * nn, sizeof(float) * ac * nn,
+                           cudaMemcpyHostToDevice, c->copy),
+           "upload holograms");
+        CK(cudaEventRecord(c->ready[k], c->copy), "holograms uploaded");
+    }
+    CK(cudaStreamWaitEvent(s, c->ready[ctdm_ctx::kChunks], 0), "wait for the background");
+    const ChunkFeed feed = {c->ready, per};
+    st = reconstruct_core(c, p, A, M, B<float>(c, B_HOLO), B<float>(c, B_BG), h_angx, h_angy, B<ctdm_cfloat>(c, B_RI),
+                          s, &feed);
     if (st != CTDM_OK) return st;
     CK(cudaMemcpyAsync(h_ri, c->buf[B_RI], sizeof(float2) * r3, cudaMemcpyDeviceToHost, s), "download volume");
     int derr = 0;
