@@ -730,7 +730,19 @@ static ctdm_status pipeline_core(ctdm_ctx *c, const ctdm_params *p, int A, int M
     const float *unwrapped =
         p->unwrap_method == CTDM_METHOD_GOLDSTEIN ? B<float>(c, B_GOLD) : B<float>(c, B_PHU);
     // Front end per chunk of angles (one chunk unless the holograms arrive in chunks):
-    // QPI, Goldstein, unwrapping, spectra.
+    // QPI, unwrapping, spectra.  Goldstein runs once over all maps after the last
+    // chunk's QPI (its kernels are latency-bound per map, so chunks would repeat that
+    // latency); when its phase feeds the reconstruction the spectra follow it.
+    const bool gold_feeds = p->unwrap_method == CTDM_METHOD_GOLDSTEIN;
+    auto spectra = [&](int a0, int ac) -> ctdm_status {
+        const long o = (long)a0 * mm;
+        float2 *U = B<float2>(c, B_U) + (long)a0 * rr;
+        CK(prep_rytov(unwrapped + o, B<float>(c, B_AMP) + o, ac, M, N, R, U, s), "prep");
+        CK(fft_rows(U, R, (long)ac * R, false, s), "spectra rows");
+        CK(fft_cols(U, R, (long)ac * R, R, rr, R, false, s), "spectra cols");
+        tm.mark(S_SPECTRA, s);
+        return CTDM_OK;
+    };
     for (int k = 0; k < nchunks; k++) {
         const int a0 = k * per, ac = std::min(per, A - a0);
         const long o = (long)a0 * mm;
@@ -742,7 +754,7 @@ static ctdm_status pipeline_core(ctdm_ctx *c, const ctdm_params *p, int A, int M
             if (st != CTDM_OK) return st;
             tm.mark(S_QPI, s);
         }
-        if (run_gold) {
+        if (run_gold && k == nchunks - 1) {
             cudaStream_t gs = s;
             if (gold_side) {
                 CK(cudaEventRecord(c->fork, s), "fork");
@@ -750,25 +762,25 @@ static ctdm_status pipeline_core(ctdm_ctx *c, const ctdm_params *p, int A, int M
                 gs = c->side;
                 tm.side_mark(gs);
             }
-            CK(goldstein_residues(phase, ac, M, M, B<int8_t>(c, B_CHG) + o, gs), "goldstein residues");
-            CK(goldstein_cuts(B<int8_t>(c, B_CHG) + o, ac, M, M, B<uint8_t>(c, B_CUT) + o, B<int8_t>(c, B_GWORK) + o,
-                              gs),
+            const float *ph_all = B<float>(c, B_PHASE);
+            CK(goldstein_residues(ph_all, A, M, M, B<int8_t>(c, B_CHG), gs), "goldstein residues");
+            CK(goldstein_cuts(B<int8_t>(c, B_CHG), A, M, M, B<uint8_t>(c, B_CUT), B<int8_t>(c, B_GWORK), gs),
                "goldstein cuts");
-            CK(goldstein_floodfill(B<uint8_t>(c, B_CUT) + o, phase, ac, M, M, B<float>(c, B_GOLD) + o,
-                                   B<uint8_t>(c, B_GSTATE) + o, B<int>(c, B_GLIST) + 5 * o, B<int>(c, B_GSTATUS) + a0,
-                                   gs),
+            CK(goldstein_floodfill(B<uint8_t>(c, B_CUT), ph_all, A, M, M, B<float>(c, B_GOLD), B<uint8_t>(c, B_GSTATE),
+                                   B<int>(c, B_GLIST), B<int>(c, B_GSTATUS), gs),
                "goldstein flood fill");
             if (gold_side) {
                 tm.side_mark(gs);
-                if (k == nchunks - 1) CK(cudaEventRecord(c->join, gs), "join");
+                CK(cudaEventRecord(c->join, gs), "join");
             } else {
                 tm.mark(S_GOLD, s);
             }
         }
+        if (gold_feeds) continue;
         if (p->unwrap_method == CTDM_METHOD_DCT) {
             CK(dct_unwrap(phase, B<float>(c, B_PHU) + o, B<float>(c, B_DCT) + o, ac, M, p->unwrap_mode, s),
                "dct unwrap");
-        } else if (p->unwrap_method == CTDM_METHOD_FAST) {
+        } else {
             CK(cudaMemcpyAsync(B<float>(c, B_FASTIN) + o, phase, sizeof(float) * ac * mm, cudaMemcpyDeviceToDevice,
                                s),
                "copy phase");
@@ -776,12 +788,9 @@ static ctdm_status pipeline_core(ctdm_ctx *c, const ctdm_params *p, int A, int M
                "fast unwrap");
         }
         tm.mark(S_UNWRAP, s);
-        float2 *U = B<float2>(c, B_U) + (long)a0 * rr;
-        CK(prep_rytov(unwrapped + o, B<float>(c, B_AMP) + o, ac, M, N, R, U, s), "prep");
-        CK(fft_rows(U, R, (long)ac * R, false, s), "spectra rows");
-        CK(fft_cols(U, R, (long)ac * R, R, rr, R, false, s), "spectra cols");
-        tm.mark(S_SPECTRA, s);
+        if ((st = spectra(a0, ac)) != CTDM_OK) return st;
     }
+    if (gold_feeds && (st = spectra(0, A)) != CTDM_OK) return st;
 
     const double fm0 = p->n_med / p->wavelength;
     const double df = 1.0 / (R * p->dx);
