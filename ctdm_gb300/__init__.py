@@ -87,13 +87,19 @@ class Context:
               "ctdm_reconstruct_device")
 
     def reconstruct(self, params, holo, bg, angx, angy, out=None):
-        """Host arrays in, host RI volume (R, R, R) complex64 out."""
-        holo, bg, angx, angy = _f32(holo), _f32(bg), _f32(angx), _f32(angy)
+        """Host arrays in, host RI volume (R, R, R) complex64 out.  uint16 / uint8 holograms
+        (camera counts) are uploaded as they are and converted on the GPU."""
+        kind = np.asarray(holo).dtype
+        fn = {np.dtype(np.uint16): ("ctdm_reconstruct_u16", np.uint16),
+              np.dtype(np.uint8): ("ctdm_reconstruct_u8", np.uint8)}.get(kind, ("ctdm_reconstruct", np.float32))
+        holo = np.ascontiguousarray(holo, fn[1])
+        bg = np.ascontiguousarray(bg, fn[1])
+        angx, angy = _f32(angx), _f32(angy)
         r = params.r_vol
         if out is None:
             out = np.empty((r, r, r), np.complex64)
-        check(self.lib.ctdm_reconstruct(self.handle, ctypes.byref(params), len(angx), _ptr(holo), _ptr(bg),
-                                        _ptr(angx), _ptr(angy), _ptr(out)), "ctdm_reconstruct")
+        check(getattr(self.lib, fn[0])(self.handle, ctypes.byref(params), len(angx), _ptr(holo), _ptr(bg),
+                                       _ptr(angx), _ptr(angy), _ptr(out)), fn[0])
         return out
 
     def carrier(self):

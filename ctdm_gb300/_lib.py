@@ -75,6 +75,10 @@ _SIGS = {
                                         c_void_p, c_void_p, c_void_p]),
     "ctdm_reconstruct": (c_int, [c_void_p, ctypes.POINTER(Params), c_int, c_void_p, c_void_p, c_void_p, c_void_p,
                                  c_void_p]),
+    "ctdm_reconstruct_u16": (c_int, [c_void_p, ctypes.POINTER(Params), c_int, c_void_p, c_void_p, c_void_p,
+                                     c_void_p, c_void_p]),
+    "ctdm_reconstruct_u8": (c_int, [c_void_p, ctypes.POINTER(Params), c_int, c_void_p, c_void_p, c_void_p,
+                                    c_void_p, c_void_p]),
     "ctdm_qpi": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_int, P_int, c_void_p, c_void_p,
                          c_void_p]),
     "ctdm_qpi_b": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_int, P_int, c_void_p, c_void_p, c_void_p]),

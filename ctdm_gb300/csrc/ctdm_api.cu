@@ -197,7 +197,7 @@ const float *dct_eigen(int M)
 enum BufId {
     B_PHASE, B_AMP, B_PHU, B_CHG, B_CUT, B_GOLD, B_U, B_F2, B_COUNTS, B_G, B_T1, B_S, B_BGF, B_DCT, B_MASK, B_GEOM,
     B_CARRIER, B_KEY, B_SCRATCH, B_HOLO, B_BG, B_RI, B_GSTATE, B_GLIST, B_GSTATUS, B_FASTW, B_FASTIN, B_TMP, B_GWORK,
-    B_TMASK, B_TCOUNT, B_TVALS, B_QMAG, B_FIT, B_PV, B_PG, B_PV2, B_PG2, B_PVP, B_PPART, B_PCTL, B_PHIST, NBUF
+    B_TMASK, B_TCOUNT, B_TVALS, B_QMAG, B_FIT, B_PV, B_PG, B_PV2, B_PG2, B_PVP, B_PPART, B_PCTL, B_PHIST, B_STAGE, B_STAGEBG, NBUF
 };
 
 // Stage boundaries recorded with CUDA events when timing is enabled.
@@ -874,9 +874,10 @@ void clear_error() { g_err.clear(); }
 int max_angles() { return kMaxAngles; }
 }  // namespace ctdm
 
-extern "C" ctdm_status ctdm_reconstruct(ctdm_ctx *c, const ctdm_params *p, int A, const float *h_holo,
-                                        const float *h_bg, const float *h_angx, const float *h_angy,
-                                        ctdm_cfloat *h_ri)
+// Host-buffer reconstruction.  bpc: bytes per hologram value, 4 (float) or 1 / 2 (integer
+// camera counts, uploaded as they are and widened to float on the copy stream).
+static ctdm_status reconstruct_host(ctdm_ctx *c, const ctdm_params *p, int A, const void *h_holo, const void *h_bg,
+                                    int bpc, const float *h_angx, const float *h_angy, ctdm_cfloat *h_ri)
 {
     if (!c || !p || !h_holo || !h_bg || !h_ri) return invalid("ctdm_reconstruct: NULL argument");
     int M;
@@ -888,21 +889,32 @@ extern "C" ctdm_status ctdm_reconstruct(ctdm_ctx *c, const ctdm_params *p, int A
     CK(ensure(c, B_HOLO, sizeof(float) * A * nn), "alloc holograms");
     CK(ensure(c, B_BG, sizeof(float) * nbg * nn), "alloc background");
     CK(ensure(c, B_RI, sizeof(float2) * r3), "alloc volume");
-    cudaStream_t s = 0;
+    const bool counts = bpc != 4;
+    if (counts) {
+        CK(ensure(c, B_STAGE, (size_t)bpc * A * nn), "alloc hologram staging");
+        CK(ensure(c, B_STAGEBG, (size_t)bpc * nbg * nn), "alloc background staging");
+    }
     // the backgrounds first, then the holograms in chunks of angles on the copy stream:
-    // the front end of a chunk (QPI, unwrapping, Goldstein, spectra) runs while the
-    // later chunks are still in flight over the host link
+    // the front end of a chunk (QPI, unwrapping, spectra) runs while the later chunks are
+    // still in flight over the host link
+    auto upload = [&](void *dst_stage, float *dst, const void *src, long count) -> cudaError_t {
+        if (!counts) return cudaMemcpyAsync(dst, src, sizeof(float) * count, cudaMemcpyHostToDevice, c->copy);
+        cudaError_t e = cudaMemcpyAsync(dst_stage, src, (size_t)bpc * count, cudaMemcpyHostToDevice, c->copy);
+        return e == cudaSuccess ? widen_counts(dst_stage, bpc, count, dst, c->copy) : e;
+    };
+    cudaStream_t s = 0;
     const int per = std::max(8, (A + ctdm_ctx::kChunks - 1) / ctdm_ctx::kChunks);
     const int nchunks = (A + per - 1) / per;
     CK(cudaEventRecord(c->ready[ctdm_ctx::kChunks], s), "copy start");
     CK(cudaStreamWaitEvent(c->copy, c->ready[ctdm_ctx::kChunks], 0), "copy start");
-    CK(cudaMemcpyAsync(c->buf[B_BG], h_bg, sizeof(float) * nbg * nn, cudaMemcpyHostToDevice, c->copy),
-       "upload background");
+    CK(upload(c->buf[B_STAGEBG], B<float>(c, B_BG), h_bg, nbg * nn), "upload background");
     CK(cudaEventRecord(c->ready[ctdm_ctx::kChunks], c->copy), "background uploaded");
+    const char *hsrc = static_cast<const char *>(h_holo);
+    char *stage = static_cast<char *>(c->buf[B_STAGE]);
     for (int k = 0; k < nchunks; k++) {
         const long a0 = (long)k * per, ac = std::min<long>(per, A - a0);
-        CK(cudaMemcpyAsync(B<float>(c, B_HOLO) + a0 * nn, h_holo + a0 * nn, sizeof(float) * ac * nn,
-                           cudaMemcpyHostToDevice, c->copy),
+        CK(upload(counts ? stage + (size_t)bpc * a0 * nn : nullptr, B<float>(c, B_HOLO) + a0 * nn,
+                  hsrc + (size_t)bpc * a0 * nn, ac * nn),
            "upload holograms");
         CK(cudaEventRecord(c->ready[k], c->copy), "holograms uploaded");
     }
@@ -920,7 +932,29 @@ extern "C" ctdm_status ctdm_reconstruct(ctdm_ctx *c, const ctdm_params *p, int A
         g_err = "a bounded device-side wait ran out (code " + std::to_string(derr) + ")";
         return CTDM_ERR_TIMEOUT;
     }
+    g_err.clear();
     return CTDM_OK;
+}
+
+extern "C" ctdm_status ctdm_reconstruct(ctdm_ctx *c, const ctdm_params *p, int A, const float *h_holo,
+                                        const float *h_bg, const float *h_angx, const float *h_angy,
+                                        ctdm_cfloat *h_ri)
+{
+    return reconstruct_host(c, p, A, h_holo, h_bg, 4, h_angx, h_angy, h_ri);
+}
+
+extern "C" ctdm_status ctdm_reconstruct_u16(ctdm_ctx *c, const ctdm_params *p, int A, const uint16_t *h_holo,
+                                            const uint16_t *h_bg, const float *h_angx, const float *h_angy,
+                                            ctdm_cfloat *h_ri)
+{
+    return reconstruct_host(c, p, A, h_holo, h_bg, 2, h_angx, h_angy, h_ri);
+}
+
+extern "C" ctdm_status ctdm_reconstruct_u8(ctdm_ctx *c, const ctdm_params *p, int A, const uint8_t *h_holo,
+                                           const uint8_t *h_bg, const float *h_angx, const float *h_angy,
+                                           ctdm_cfloat *h_ri)
+{
+    return reconstruct_host(c, p, A, h_holo, h_bg, 1, h_angx, h_angy, h_ri);
 }
 
 // ---------------------------------------------------------------- stage API

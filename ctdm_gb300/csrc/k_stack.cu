@@ -147,6 +147,35 @@ cudaError_t resize_maps(const float *ph, const float *am, int A, int M, int N, f
     return cudaGetLastError();
 }
 
+// Camera counts (8- or 16-bit) to float, four per thread (n a multiple of 4, both
+// buffers 16-byte aligned); the host-buffer entries upload integer frames and widen
+// them here.
+template <class T>
+__global__ void __launch_bounds__(256) widen_kernel(const T *__restrict__ in, float *out, long n4)
+{
+    for (long i = blockIdx.x * 256l + threadIdx.x; i < n4; i += (long)gridDim.x * 256) {
+        if constexpr (sizeof(T) == 1) {
+            const uchar4 v = reinterpret_cast<const uchar4 *>(in)[i];
+            reinterpret_cast<float4 *>(out)[i] = make_float4(v.x, v.y, v.z, v.w);
+        } else {
+            const ushort4 v = reinterpret_cast<const ushort4 *>(in)[i];
+            reinterpret_cast<float4 *>(out)[i] = make_float4(v.x, v.y, v.z, v.w);
+        }
+    }
+}
+
+cudaError_t widen_counts(const void *in, int bytes_per_count, long n, float *out, cudaStream_t s)
+{
+    if (n % 4 != 0 || (bytes_per_count != 1 && bytes_per_count != 2)) return cudaErrorInvalidValue;
+    const long n4 = n / 4;
+    long blocks = (n4 + 255) / 256;
+    if (blocks > 8 * 152) blocks = 8 * 152;
+    if (bytes_per_count == 1) widen_kernel<uint8_t><<<(unsigned)blocks, 256, 0, s>>>((const uint8_t *)in, out, n4);
+    else widen_kernel<uint16_t><<<(unsigned)blocks, 256, 0, s>>>((const uint16_t *)in, out, n4);
+    note_launch();
+    return cudaGetLastError();
+}
+
 cudaError_t prep_rytov(const float *phase, const float *amp, int A, int M, int N, int R, float2 *U0, cudaStream_t s)
 {
     dim3 grid((R + 31) / 32, (R + 31) / 32, A), block(32, 8);

@@ -31,6 +31,8 @@ cudaError_t qpib_inverse(const float2 *T, int A, int M, float2 *field_out, const
 // Angle camera: index of the spectrum peak of AngCal_GPU in *key's low word
 // (complemented; see angcal_peak).  scratch: N*N complex.
 cudaError_t angcal_peak(const float *img, int N, float2 *scratch, unsigned long long *key, cudaStream_t s);
+// Integer camera counts (1 or 2 bytes each, n a multiple of 4) to float.
+cudaError_t widen_counts(const void *in, int bytes_per_count, long n, float *out, cudaStream_t s);
 // Whole-map bilinear resize M -> N of phase and amplitude stacks.
 cudaError_t resize_maps(const float *ph, const float *am, int A, int M, int N, float *ph_out, float *am_out,
                         cudaStream_t s);

@@ -124,9 +124,20 @@ CTDM_API unsigned long long ctdm_launch_count(void);
 CTDM_API ctdm_status ctdm_reconstruct_device(ctdm_ctx *ctx, const ctdm_params *p, int n_angles, const float *d_holo,
                                     const float *d_bg, const float *h_angx, const float *h_angy,
                                     ctdm_cfloat *d_ri, void *stream);
-/* Same with host buffers: copies in, reconstructs, copies the volume out, syncs. */
+/* Same with host buffers: copies in, reconstructs, copies the volume out, syncs.  The
+ * holograms go over the host link in chunks of angles while the front end of the
+ * earlier chunks runs; pinned host memory lets the copies overlap. */
 CTDM_API ctdm_status ctdm_reconstruct(ctdm_ctx *ctx, const ctdm_params *p, int n_angles, const float *h_holo,
                              const float *h_bg, const float *h_angx, const float *h_angy, ctdm_cfloat *h_ri);
+/* The same for integer camera frames (16- or 8-bit counts, as the reference's BMP frames
+ * are): uploaded as they are (a half or a quarter of the float bytes) and converted to
+ * float on the GPU; the result equals ctdm_reconstruct on the same values as floats. */
+CTDM_API ctdm_status ctdm_reconstruct_u16(ctdm_ctx *ctx, const ctdm_params *p, int n_angles, const uint16_t *h_holo,
+                                          const uint16_t *h_bg, const float *h_angx, const float *h_angy,
+                                          ctdm_cfloat *h_ri);
+CTDM_API ctdm_status ctdm_reconstruct_u8(ctdm_ctx *ctx, const ctdm_params *p, int n_angles, const uint8_t *h_holo,
+                                         const uint8_t *h_bg, const float *h_angx, const float *h_angy,
+                                         ctdm_cfloat *h_ri);
 
 /* --- batched reconstruction (no reference counterpart) ----------------------------
  * Many independent tomograms, each with its own sizes and angle count, scheduled over

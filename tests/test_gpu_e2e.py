@@ -23,3 +23,22 @@ def test_host_chunks_equal_device_path(ctx, dev, method, gold, qpi):
     want = out.cpu().numpy()
     got = ctx.reconstruct(p, acq.holograms, acq.background, acq.ang_x, acq.ang_y)
     assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("kind", ["u16", "u8"])
+def test_integer_counts_equal_float_path(ctx, dev, kind):
+    """16- and 8-bit camera frames (uploaded as integers, widened on the GPU) give the
+    float path's volume bit for bit."""
+    import ctdm_gb300 as C
+    from ctdm_gb300 import phantom
+    acq = phantom.acquisition(128, 64, 19, seed=23, pixel=0.2e-6, photons=1e4)
+    if kind == "u16":
+        holo, bg = acq.holograms.astype(np.uint16), acq.background.astype(np.uint16)
+    else:
+        scale = 250.0 / max(acq.holograms.max(), acq.background.max())
+        holo = np.rint(acq.holograms * scale).astype(np.uint8)
+        bg = np.rint(acq.background * scale).astype(np.uint8)
+    p = C.params_for(acq, 2, run_goldstein=1)
+    want = ctx.reconstruct(p, holo.astype(np.float32), bg.astype(np.float32), acq.ang_x, acq.ang_y)
+    got = ctx.reconstruct(p, holo, bg, acq.ang_x, acq.ang_y)
+    assert np.array_equal(got, want)
