@@ -249,6 +249,15 @@ struct ctdm_ctx {
     // side stream for work whose result the reconstruction does not consume
     cudaStream_t side = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr;
+    // pinned staging of the per-call angle geometry and the carrier readback, so that
+    // neither copy blocks the calling thread behind copies in flight (a pageable copy
+    // would); the events mark when the staging may be reused / read
+    struct Pinned {
+        AngleGeom geom[512];
+        int carrier[4];
+    } *pin = nullptr;
+    cudaEvent_t geom_done = nullptr, carrier_done = nullptr;
+    bool carrier_pending = false;
     // host-buffer uploads: a copy stream and one event per chunk of angles
     static const int kChunks = 16;
     cudaStream_t copy = nullptr;
@@ -313,6 +322,9 @@ extern "C" ctdm_status ctdm_ctx_create(int device, ctdm_ctx **out)
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->copy, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMallocHost(&c->pin, sizeof(ctdm_ctx::Pinned));
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->geom_done, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->carrier_done, cudaEventDisableTiming);
     for (int k = 0; k <= ctdm_ctx::kChunks && e == cudaSuccess; k++)
         e = cudaEventCreateWithFlags(&c->ready[k], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_err, sizeof(int));
@@ -338,6 +350,9 @@ extern "C" void ctdm_ctx_destroy(ctdm_ctx *c)
         if (c->timer.side[i]) cudaEventDestroy(c->timer.side[i]);
     if (c->side) cudaStreamDestroy(c->side);
     if (c->copy) cudaStreamDestroy(c->copy);
+    if (c->pin) cudaFreeHost(c->pin);
+    for (cudaEvent_t e : {c->geom_done, c->carrier_done})
+        if (e) cudaEventDestroy(e);
     for (cudaEvent_t e : c->ready)
         if (e) cudaEventDestroy(e);
     if (c->d_err) cudaFree(c->d_err);
@@ -400,6 +415,11 @@ extern "C" ctdm_status ctdm_ctx_device_status(ctdm_ctx *c, int *status)
 extern "C" ctdm_status ctdm_ctx_carrier(ctdm_ctx *c, int *carrier3)
 {
     if (!c || !carrier3) return invalid("ctdm_ctx_carrier: NULL argument");
+    if (c->carrier_pending) {
+        CK(cudaEventSynchronize(c->carrier_done), "carrier readback");
+        std::memcpy(c->carrier, c->pin->carrier, sizeof c->carrier);
+        c->carrier_pending = false;
+    }
     std::memcpy(carrier3, c->carrier, sizeof c->carrier);
     return CTDM_OK;
 }
@@ -456,8 +476,18 @@ static ctdm_status upload_geometry(ctdm_ctx *c, const float *angx, const float *
     std::vector<AngleGeom> g;
     angle_geometry(angx, angy, A, fm0, df, g);
     CK(ensure(c, B_GEOM, sizeof(AngleGeom) * A), "alloc geometry");
-    // pageable source: the copy is staged before the call returns
-    CK(cudaMemcpyAsync(c->buf[B_GEOM], g.data(), sizeof(AngleGeom) * A, cudaMemcpyHostToDevice, s), "upload geometry");
+    if (A <= (int)(sizeof c->pin->geom / sizeof(AngleGeom))) {
+        // pinned staging: the previous call's copy has left it once geom_done fired
+        CK(cudaEventSynchronize(c->geom_done), "geometry staging");
+        std::memcpy(c->pin->geom, g.data(), sizeof(AngleGeom) * A);
+        CK(cudaMemcpyAsync(c->buf[B_GEOM], c->pin->geom, sizeof(AngleGeom) * A, cudaMemcpyHostToDevice, s),
+           "upload geometry");
+        CK(cudaEventRecord(c->geom_done, s), "geometry staging");
+    } else {
+        // pageable source: the copy is staged before the call returns
+        CK(cudaMemcpyAsync(c->buf[B_GEOM], g.data(), sizeof(AngleGeom) * A, cudaMemcpyHostToDevice, s),
+           "upload geometry");
+    }
     return CTDM_OK;
 }
 
@@ -643,6 +673,7 @@ extern "C" ctdm_status ctdm_qpi_b(ctdm_ctx *c, int N, int A, const float *d_holo
     if (st != CTDM_OK) return st;
     CK(cudaMemcpyAsync(c->carrier, c->buf[B_CARRIER], sizeof(int) * 3, cudaMemcpyDeviceToHost, s), "carrier");
     CK(cudaStreamSynchronize(s), "carrier");
+    c->carrier_pending = false;
     if (center2) {
         center2[0] = c->carrier[0];
         center2[1] = c->carrier[1];
@@ -828,7 +859,11 @@ static ctdm_status reconstruct_core(ctdm_ctx *c, const ctdm_params *p, int A, in
     if (st != CTDM_OK) return st;
     st = pipeline_core(c, p, A, M, d_holo, d_bg, B<AngleGeom>(c, B_GEOM), d_ri, s, feed);
     if (st != CTDM_OK) return st;
-    CK(cudaMemcpyAsync(c->carrier, c->buf[B_CARRIER], sizeof(int) * 3, cudaMemcpyDeviceToHost, s), "carrier readback");
+    // the carrier comes back into pinned staging without blocking; ctdm_ctx_carrier waits for it
+    CK(cudaMemcpyAsync(c->pin->carrier, c->buf[B_CARRIER], sizeof(int) * 3, cudaMemcpyDeviceToHost, s),
+       "carrier readback");
+    CK(cudaEventRecord(c->carrier_done, s), "carrier readback");
+    c->carrier_pending = true;
     return CTDM_OK;
 }
 
@@ -968,6 +1003,7 @@ extern "C" ctdm_status ctdm_qpi(ctdm_ctx *c, int N, int M, int A, const float *d
     if (st != CTDM_OK) return st;
     CK(cudaMemcpyAsync(c->carrier, c->buf[B_CARRIER], sizeof(int) * 3, cudaMemcpyDeviceToHost, s), "carrier");
     CK(cudaStreamSynchronize(s), "synchronise");
+    c->carrier_pending = false;
     if (carrier3) std::memcpy(carrier3, c->carrier, sizeof c->carrier);
     return CTDM_OK;
 }
