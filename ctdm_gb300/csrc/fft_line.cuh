@@ -179,6 +179,18 @@ __device__ __forceinline__ void scatter(float2 *buf, const float2 *v, int b, int
     }
 }
 
+// Barrier between the shared-memory exchanges of a transform.  Under the row mapping a
+// line's T threads are consecutive, so with T dividing 32 a line lies inside one warp and
+// touches only its own slots: a warp barrier orders its exchanges.  The column mapping
+// spreads a line over the CTA and needs the CTA barrier.  (Exchanges with data written
+// or read by another mapping, GATHER0 / SCATTER_LAST, keep the CTA barrier.)
+template <bool TF, int T, bool LOCAL>
+__device__ __forceinline__ void line_sync()
+{
+    if constexpr (TF && LOCAL && T <= 32 && (32 % T) == 0) __syncwarp();
+    else __syncthreads();
+}
+
 // Stages in the order given.  GATHER0: the first stage reads shared memory
 // (else its inputs are already in v).  SCATTER_LAST: the last stage writes shared
 // memory (else its outputs stay in v).
@@ -189,12 +201,12 @@ __device__ __forceinline__ void stages(float2 *buf, float2 *v, const float2 *__r
     constexpr bool last = (sizeof...(REST) == 0);
     if constexpr (!first || GATHER0) {
         gather<L, T, LP, R, TF>(buf, v, b, t);
-        __syncthreads();
+        line_sync<TF, T, !(first && GATHER0)>();
     }
     compute<L, T, INV, NS, R>(v, tw, t);
     if constexpr (!last || SCATTER_LAST) {
         scatter<L, T, LP, NS, R, TF>(buf, v, b, t);
-        __syncthreads();
+        line_sync<TF, T, !(last && SCATTER_LAST)>();
     }
     if constexpr (!last) stages<L, T, LP, INV, GATHER0, SCATTER_LAST, TF, NS * R, REST...>(buf, v, tw, b, t);
 }
