@@ -197,7 +197,7 @@ const float *dct_eigen(int M)
 enum BufId {
     B_PHASE, B_AMP, B_PHU, B_CHG, B_CUT, B_GOLD, B_U, B_F2, B_COUNTS, B_G, B_T1, B_S, B_BGF, B_DCT, B_MASK, B_GEOM,
     B_CARRIER, B_KEY, B_SCRATCH, B_HOLO, B_BG, B_RI, B_GSTATE, B_GLIST, B_GSTATUS, B_FASTW, B_FASTIN, B_TMP, B_GWORK,
-    B_TMASK, B_TCOUNT, B_TVALS, B_QMAG, B_FIT, B_PV, B_PG, B_PV2, B_PG2, B_PVP, B_PPART, B_PCTL, B_PHIST, B_STAGE, B_STAGEBG, NBUF
+    B_TMASK, B_TCOUNT, B_TVALS, B_QMAG, B_FIT, B_PV, B_PG, B_PV2, B_PG2, B_PVP, B_PPART, B_PCTL, B_PHIST, B_STAGE, B_STAGEBG, B_TPRE, NBUF
 };
 
 // Stage boundaries recorded with CUDA events when timing is enabled.
@@ -589,12 +589,14 @@ static ctdm_status do_positivity(ctdm_ctx *c, int R, int iters, int check_mode, 
         const long r3 = (long)R * R * R, tiles = (long)R * R / TB;
         CK(ensure(c, B_TMASK, sizeof(uint32_t) * tiles * R), "alloc packed masks");
         CK(ensure(c, B_TCOUNT, sizeof(int) * tiles), "alloc packed counts");
+        CK(ensure(c, B_TPRE, sizeof(int) * tiles * R), "alloc packed prefixes");
         CK(ensure(c, B_TVALS, sizeof(float2) * r3), "alloc packed values");
         CK(pack_measured(F2, check_mode == CTDM_CHECK_MASK ? mask : nullptr, R, TB, B<uint32_t>(c, B_TMASK),
-                         B<int>(c, B_TCOUNT), B<float2>(c, B_TVALS), s),
+                         B<int>(c, B_TCOUNT), B<int>(c, B_TPRE), B<float2>(c, B_TVALS), s),
            "pack measured samples");
         la.tmask = B<uint32_t>(c, B_TMASK);
         la.tcount = B<int>(c, B_TCOUNT);
+        la.tprefix = B<int>(c, B_TPRE);
         la.tvals = B<float2>(c, B_TVALS);
         la.packed = 1;
     }

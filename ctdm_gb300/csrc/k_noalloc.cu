@@ -29,6 +29,7 @@ namespace {
 // Capacity: maps of side M in {16, 32, 64, 128, 256}, A * M * M <= 4194304 points.
 constexpr long kScratchFloats = 4194304;
 constexpr int kMinM = 16, kMaxM = 256;
+static_assert(kMinM << (5 - 1) == kMaxM, "five sides, 16 to 256");
 constexpr int kSides = 5;                     // 16, 32, 64, 128, 256
 constexpr int kTwTotal = 32 + 64 + 128 + 256 + 512;          // FFT tables of length 2M
 constexpr int kDctTotal = 33 + 65 + 129 + 257 + 513;         // cos/sin(k pi / 2M), k = 0..2M

@@ -407,7 +407,7 @@ static cudaError_t ewald_launch(const EwaldArgs &a, cudaStream_t s)
 template <int TB>
 __global__ void __launch_bounds__(256) pack_measured_kernel(const float2 *__restrict__ F2,
                                                            const uint8_t *__restrict__ mask, int R, uint32_t *tmask,
-                                                           int *tcount, float2 *tvals)
+                                                           int *tcount, int *tprefix, float2 *tvals)
 {
     extern __shared__ int spre[];   // R prefixes, then 8 warp totals
     int *swarp = spre + R;
@@ -468,6 +468,7 @@ __global__ void __launch_bounds__(256) pack_measured_kernel(const float2 *__rest
     }
     if (threadIdx.x == 255) tcount[tile] = run;
     __syncthreads();
+    for (int z = threadIdx.x; z < R; z += 256) tprefix[tile * R + z] = spre[z];
     float2 *tv = tvals + tile * (long)TB * R;
     const uint32_t below = (1u << b) - 1u;
     for (int z0 = 0; z0 < R; z0 += ZR) {
@@ -480,15 +481,15 @@ __global__ void __launch_bounds__(256) pack_measured_kernel(const float2 *__rest
 }
 
 cudaError_t pack_measured(const float2 *F2, const uint8_t *mask, int R, int TB, uint32_t *tmask, int *tcount,
-                          float2 *tvals, cudaStream_t s)
+                          int *tprefix, float2 *tvals, cudaStream_t s)
 {
     if (R > 768) return cudaErrorInvalidValue;
     const unsigned tiles = (unsigned)((long)R * R / TB);
     const size_t smem = sizeof(int) * (R + 8);
     switch (TB) {
-    case 8: pack_measured_kernel<8><<<tiles, 256, smem, s>>>(F2, mask, R, tmask, tcount, tvals); break;
-    case 16: pack_measured_kernel<16><<<tiles, 256, smem, s>>>(F2, mask, R, tmask, tcount, tvals); break;
-    case 32: pack_measured_kernel<32><<<tiles, 256, smem, s>>>(F2, mask, R, tmask, tcount, tvals); break;
+    case 8: pack_measured_kernel<8><<<tiles, 256, smem, s>>>(F2, mask, R, tmask, tcount, tprefix, tvals); break;
+    case 16: pack_measured_kernel<16><<<tiles, 256, smem, s>>>(F2, mask, R, tmask, tcount, tprefix, tvals); break;
+    case 32: pack_measured_kernel<32><<<tiles, 256, smem, s>>>(F2, mask, R, tmask, tcount, tprefix, tvals); break;
     default: return cudaErrorInvalidValue;
     }
     note_launch();

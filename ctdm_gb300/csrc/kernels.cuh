@@ -61,14 +61,15 @@ struct LoopArgs {
     // order.  packed = 0: the z pass reads F2 / mask instead.
     const uint32_t *tmask;
     const int *tcount;
+    const int *tprefix;     // tprefix[tile * R + z]: kept samples of the tile before row z
     const float2 *tvals;
     int packed;
 };
 
 // Packs F2 (mode 0: re != 0 && im != 0; mode 1: mask != 0) into per-tile masks,
-// counts and values for the z pass (TB lines per tile, 8, 16 or 32).
+// counts, row prefixes and values for the z pass (TB lines per tile, 8, 16 or 32).
 cudaError_t pack_measured(const float2 *F2, const uint8_t *mask, int R, int TB, uint32_t *tmask, int *tcount,
-                          float2 *tvals, cudaStream_t s);
+                          int *tprefix, float2 *tvals, cudaStream_t s);
 
 cudaError_t launch_ewald(const EwaldArgs &a, cudaStream_t s);
 cudaError_t launch_xpass(const LoopArgs &a, bool final_pass, cudaStream_t s);

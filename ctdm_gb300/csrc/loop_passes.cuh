@@ -214,9 +214,8 @@ __global__ void __launch_bounds__(P::THREADS, fftl::plan_min_ctas<P>(3))
     char *al = base0 + ((128 - (tma::smem_addr(base0) & 127)) & 127);
     float2 *svals = reinterpret_cast<float2 *>(al);                          // P::B * L
     uint32_t *smask = reinterpret_cast<uint32_t *>(svals + P::B * L);        // L
-    int *spre = reinterpret_cast<int *>(smask + L);                          // L
-    int *swarp = spre + L;                                                   // 16
-    float2 *buf = reinterpret_cast<float2 *>(swarp + 16);
+    int *spre = reinterpret_cast<int *>(smask + L);                          // L (+16 spare)
+    float2 *buf = reinterpret_cast<float2 *>(spre + L + 16);
     uint64_t *bar = reinterpret_cast<uint64_t *>(buf + P::B * P::LP);
     const long nl = (long)L * L;
     const long line0 = (long)blockIdx.x * P::B;   // line = x + L y; tile = line0 / B
@@ -229,8 +228,9 @@ __global__ void __launch_bounds__(P::THREADS, fftl::plan_min_ctas<P>(3))
     if (threadIdx.x == 0) {
         const int cnt = a.tcount[tile];
         const uint32_t vbytes = (uint32_t)(((cnt + 1) & ~1) * sizeof(float2));
-        tma::mbar_expect_tx(bar, (uint32_t)(L * sizeof(uint32_t)) + vbytes);
+        tma::mbar_expect_tx(bar, (uint32_t)(2 * L * sizeof(uint32_t)) + vbytes);
         tma::bulk_load(smask, a.tmask + tile * L, (uint32_t)(L * sizeof(uint32_t)), bar);
+        tma::bulk_load(spre, a.tprefix + tile * L, (uint32_t)(L * sizeof(int)), bar);
         if (vbytes) tma::bulk_load(svals, a.tvals + tile * (long)P::B * L, vbytes, bar);
     }
     const int b = threadIdx.x % P::B, t = threadIdx.x / P::B;
@@ -239,36 +239,7 @@ __global__ void __launch_bounds__(P::THREADS, fftl::plan_min_ctas<P>(3))
 #pragma unroll
     for (int i = 0; i < P::E; i++) v[i] = __ldcs(&a.G[base + (long)fftl::slot_pos<L, P::T, P::F0>(i, t) * nl]);
     P::template seq<false, false, false>(buf, v, tw);
-    tma::mbar_wait(bar, 0, a.err, 3);
-    // exclusive prefix over z of the kept counts (two z per thread at most)
-    {
-        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-        const int z0 = 2 * threadIdx.x;
-        const int c0 = z0 < L ? __popc(smask[z0]) : 0, c1 = z0 + 1 < L ? __popc(smask[z0 + 1]) : 0;
-        int incl = c0 + c1;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int n = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += n;
-        }
-        if (lane == 31) swarp[warp] = incl;
-        __syncthreads();
-        if (threadIdx.x < 32) {
-            const int nw = P::THREADS / 32;
-            int w = threadIdx.x < nw ? swarp[threadIdx.x] : 0;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int n = __shfl_up_sync(0xffffffffu, w, o);
-                if (threadIdx.x >= o) w += n;
-            }
-            if (threadIdx.x < nw) swarp[threadIdx.x] = w;   // inclusive warp totals
-        }
-        __syncthreads();
-        const int excl = incl - (c0 + c1) + (warp > 0 ? swarp[warp - 1] : 0);
-        if (z0 < L) spre[z0] = excl;
-        if (z0 + 1 < L) spre[z0 + 1] = excl + c0;
-        __syncthreads();
-    }
+    tma::mbar_wait(bar, 0, a.err, 3);   // masks, row prefixes (from the packing) and values
     const uint32_t below = (1u << b) - 1u;
 #pragma unroll
     for (int i = 0; i < P::E; i++) {
