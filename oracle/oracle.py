@@ -367,3 +367,27 @@ def pocs(F2, params, k2, n_med, want_dd=True):
     lib().or_pocs(_p(F2), r, ctypes.byref(params), ctypes.c_double(k2), ctypes.c_double(n_med), int(want_dd),
                   _p(out), _p(hist))
     return out, hist[:params.iterations]
+
+
+def bilinear(img, m2, n2):
+    """bilinear (cTDM/HilbertTransform.cu:2404-2435): (N1, M1) float32 image -> (N2, M2),
+    ratios (M1 - 1) / M2 and (N1 - 1) / N2, float32 arithmetic as written."""
+    a = np.asarray(img, np.float32)
+    n1, m1 = a.shape
+    xr = np.float32(m1 - 1) / np.float32(m2)
+    yr = np.float32(n1 - 1) / np.float32(n2)
+    j = np.arange(m2, dtype=np.float32)
+    i = np.arange(n2, dtype=np.float32)
+    xs = (xr * j).astype(np.float32)
+    ys = (yr * i).astype(np.float32)
+    x = xs.astype(np.int64)
+    y = ys.astype(np.int64)
+    xd = (xs - x.astype(np.float32)).astype(np.float32)[None, :]
+    yd = (ys - y.astype(np.float32)).astype(np.float32)[:, None]
+    A = a[y[:, None], x[None, :]]
+    B = a[y[:, None], x[None, :] + 1]
+    C = a[y[:, None] + 1, x[None, :]]
+    D = a[y[:, None] + 1, x[None, :] + 1]
+    one = np.float32(1)
+    out = A * (one - xd) * (one - yd) + B * xd * (one - yd) + C * yd * (one - xd) + D * (xd * yd)
+    return out.astype(np.float32)

@@ -196,3 +196,36 @@ def test_job_maps_algorithm_a_and_raw_files(ctx, oracle, tmp_path):
         np.testing.assert_array_equal(raw, m["phase"])
         raw = np.fromfile(os.path.join(ds["save_dir"], f"Amp{k:03d}_256x256.raw"), np.float32).reshape(256, 256)
         np.testing.assert_array_equal(raw, m["amp"])
+
+
+def test_job_resize_flag_0(ctx, oracle, tmp_path):
+    """ResizeFlag 0: the frame check runs on the whole map with 0.5 and 5 pi, and the
+    stacks are the bilinear resize N -> R of each map (Combine2Stack's first branch);
+    the volume equals BatchRecon on those stacks."""
+    from ctdm_gb300 import _lib, jobs
+    from ctdm_gb300 import dataset
+    ds = dataset.make_dataset(tmp_path, n=512, frames=4, seed=8, recon_flag=1, resize_flag=0, photons=1e5, na=0.3)
+    r = jobs.run_job(jobs.parse_job_file(ds["job_file"]))
+    maps = [jobs.read_phimap(os.path.join(ds["save_dir"], f"buffer{k:03d}.phimap")) for k in range(1, 5)]
+    want_status = [not oracle.check_frame(m["phase"], 0, 0.5, 5 * np.pi) for m in maps]
+    assert [m["status"] for m in maps] == want_status
+    assert (r.frames, r.rejected, r.n_holo, r.recon_size) == (4, 4 - sum(want_status), 512, 256)
+    keep = [m for m in maps if m["status"]]
+    if len(keep) < 2:
+        assert r.recon_frames == 0
+        return
+    assert r.recon_frames == len(keep)
+    ph = np.stack([oracle.bilinear(m["phase"], 256, 256) for m in keep]).astype(np.float32)
+    am = np.stack([oracle.bilinear(m["amp"], 256, 256) for m in keep]).astype(np.float32)
+    ax = np.array([m["angle_x"] for m in keep], np.float32)
+    ay = np.array([m["angle_y"] for m in keep], np.float32)
+    out = tmp_path / "ref"
+    out.mkdir()
+    lib = _lib.load()
+    lib.ctdm_set_recon_globals(256, OPTICS["n_med"], OPTICS["wavelength_nm"], OPTICS["camera_pixel_um"],
+                               OPTICS["mag"], 2, 0, os.fsencode(str(out)))
+    lib.BatchRecon(ph.ctypes.data, am.ctypes.data, ax.ctypes.data, ay.ctypes.data, len(ax))
+    assert _lib.last_error() == ""
+    got = jobs.read_rimap(os.path.join(ds["save_dir"], jobs.rimap_name(256)), 256)
+    want = jobs.read_rimap(os.path.join(str(out), jobs.rimap_name(256)), 256)
+    assert rmse(got, want) < RI_TOL
