@@ -21,6 +21,28 @@ namespace ctdm {
 
 using fftl::Plan;
 
+// Line plan of the three passes: 256 threads per CTA and at most 16 points per
+// thread, so that four CTAs fit on an SM.  The passes are latency-bound (a few
+// loads and a transform per line between barriers), and at 512 points moving from
+// 16 lines x 16 threads at 128 registers (2 CTAs per SM) to 8 lines x 32 threads
+// at 64 registers (4 CTAs) cut the three passes from 369 to 219 us on 121 maps
+// of 256 x 256.
+template <int L2>
+struct DctPlan : Plan<L2> {};
+template <>
+struct DctPlan<512> : fftl::PV<512, 2> {};
+template <>
+struct DctPlan<768> : fftl::PV<768, 1> {};
+template <>
+struct DctPlan<1024> : fftl::PlanT<1024, 4, 64, fftl::Radices<16, 16, 4>, fftl::Radices<4, 16, 16>> {};
+
+// Resident CTAs per SM the register allocation aims for.
+template <class P>
+__host__ __device__ constexpr int dct_min_ctas()
+{
+    return P::E <= 16 ? 1024 / P::THREADS : (P::E <= 24 ? 768 / P::THREADS : 512 / P::THREADS);
+}
+
 // NumericDerivative1 wrap: t - 2 pi sign(t) floor(|pi sign(t) + t| / 2 pi), which
 // the reference evaluates in double; it is exactly t when |t| < pi.  For a wrapped
 // difference (|t| < 4 pi, so the floor q is 0, 1 or 2) the float form
@@ -66,6 +88,17 @@ __device__ __forceinline__ float lap_at(const float *__restrict__ phi, int x, in
     return (c1 - c2) + (c3 - c4);
 }
 
+// lap_at on staged rows: r points at row y, rows y - 1 and y + 1 lie M before and after.
+__device__ __forceinline__ float lap_rows(const float *r, int x, int y, int M)
+{
+    const float c = r[x];
+    const float c1 = (x == M - 1) ? 0.f : wrap_grad(r[x + 1] - c);
+    const float c2 = (x > 0) ? wrap_grad(c - r[x - 1]) : 0.f;
+    const float c3 = (y == M - 1) ? 0.f : wrap_grad(r[x + M] - c);
+    const float c4 = (y > 0) ? wrap_grad(c - r[x - M]) : 0.f;
+    return (c1 - c2) + (c3 - c4);
+}
+
 // countFDCT (:202-216): X_k from the 2M-point transform Y of the mirrored line.
 __device__ __forceinline__ float dct_from_fft(float2 Y, int k, const float2 *__restrict__ dtw, float dT)
 {
@@ -94,25 +127,69 @@ __device__ __forceinline__ float2 idct_input(const float *X, int p, int M, const
 
 // Pass 1: rows.  phi: A x M x M; T: A x M x M (row DCT coefficients, [a][y][kx]).
 template <int L2>
-__global__ void __launch_bounds__(Plan<L2>::THREADS) dct_rows_kernel(const float *__restrict__ phi, float *T,
-                                                                    long nlines, int M, const float2 *__restrict__ dtw,
-                                                                    const float2 *__restrict__ tw)
+__global__ void __launch_bounds__(DctPlan<L2>::THREADS, dct_min_ctas<DctPlan<L2>>())
+    dct_rows_kernel(const float *__restrict__ phi, float *T, long nlines, int /* M = L2 / 2 */,
+                    const float2 *__restrict__ dtw, const float2 *__restrict__ tw)
 {
-    using P = Plan<L2>;
+    using P = DctPlan<L2>;
+    constexpr int M = L2 / 2;
     extern __shared__ float4 smem4[];
     float2 *buf = reinterpret_cast<float2 *>(smem4);
     const long line0 = (long)blockIdx.x * P::B;
-    for (int e = threadIdx.x; e < P::B * M; e += P::THREADS) {
-        const int b = e / M, x = e - b * M;
-        const long l = line0 + b;
-        float v = 0.f;
-        if (l < nlines) {
-            const long a = l / M;
-            const int y = (int)(l % M);
-            v = lap_at(phi + a * (long)M * M, x, y, M);
+    // map and row of the CTA's first line; a line b further on is y0 + b rows later
+    const long a0 = line0 / M;
+    const int y0 = (int)(line0 - a0 * M);
+    if constexpr (P::B <= M) {
+        // B divides M, so the CTA's lines are rows y0 .. y0 + B - 1 of one map: rows
+        // y0 - 1 .. y0 + B are staged in shared memory by independent coalesced loads
+        // (a thread's loads are all in flight together), and the Laplacian is taken
+        // from there.  The staging fits in the line buffer: (B + 2) M floats <= 4 B M.
+        constexpr int SR = P::B + 2, NS = (SR * M + P::THREADS - 1) / P::THREADS, PER = M / P::T;
+        float *S = reinterpret_cast<float *>(buf);
+        const float *map = phi + a0 * (long)M * M;
+        const bool live = line0 < nlines;
+#pragma unroll
+        for (int k = 0; k < NS; ++k) {
+            const int e = threadIdx.x + k * P::THREADS;
+            if (e < SR * M) {
+                const int y = y0 - 1 + e / M;
+                S[e] = (live && y >= 0 && y < M) ? __ldg(map + (long)y0 * M - M + e) : 0.f;
+            }
         }
-        buf[b * P::LP + x] = make_float2(v, 0.f);
-        buf[b * P::LP + (L2 - 1 - x)] = make_float2(v, 0.f);
+        __syncthreads();
+        float v[PER];
+#pragma unroll
+        for (int k = 0; k < PER; ++k) {
+            const int e = threadIdx.x + k * P::THREADS;
+            const int b = e / M, x = e - b * M;
+            v[k] = lap_rows(S + (b + 1) * M, x, y0 + b, M);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < PER; ++k) {
+            const int e = threadIdx.x + k * P::THREADS;
+            const int b = e / M, x = e - b * M;
+            buf[b * P::LP + x] = make_float2(v[k], 0.f);
+            buf[b * P::LP + (L2 - 1 - x)] = make_float2(v[k], 0.f);
+        }
+    } else {
+        // maps smaller than B lines: the CTA covers several maps
+        for (int e = threadIdx.x; e < P::B * M; e += P::THREADS) {
+            const int b = e / M, x = e - b * M;
+            const long l = line0 + b;
+            float v = 0.f;
+            if (l < nlines) {
+                int y = y0 + b;
+                long a = a0;
+                while (y >= M) {
+                    y -= M;
+                    a++;
+                }
+                v = lap_at(phi + a * (long)M * M, x, y, M);
+            }
+            buf[b * P::LP + x] = make_float2(v, 0.f);
+            buf[b * P::LP + (L2 - 1 - x)] = make_float2(v, 0.f);
+        }
     }
     __syncthreads();
     P::template run<false>(buf, tw);
@@ -124,19 +201,29 @@ __global__ void __launch_bounds__(Plan<L2>::THREADS) dct_rows_kernel(const float
     }
 }
 
+// Row stride of the column pass's coefficient staging: a warp holds min(B, 32) lines
+// at 32 / B consecutive positions each, so a stride of M (a multiple of 32 from M = 32
+// up) plus 32 / B puts all of them on distinct banks.
+template <int L2>
+__host__ __device__ constexpr int x_stride(int M)
+{
+    return M + (DctPlan<L2>::B >= 32 ? 1 : 32 / DctPlan<L2>::B);
+}
+
 // Pass 2: columns.  Line l = kx + M*a, element y at T[a*M*M + y*M + kx].
 template <int L2>
-__global__ void __launch_bounds__(Plan<L2>::THREADS) dct_cols_kernel(float *T, long nlines, int M, int mode,
-                                                                    const float2 *__restrict__ dtw,
-                                                                    const float *__restrict__ eig,
-                                                                    const float2 *__restrict__ tw)
+__global__ void __launch_bounds__(DctPlan<L2>::THREADS, dct_min_ctas<DctPlan<L2>>())
+    dct_cols_kernel(float *T, long nlines, int /* M = L2 / 2 */, int mode, const float2 *__restrict__ dtw,
+                    const float *__restrict__ eig, const float2 *__restrict__ tw)
 {
-    using P = Plan<L2>;
+    using P = DctPlan<L2>;
+    constexpr int M = L2 / 2;
     extern __shared__ float4 smem4[];
     float2 *buf = reinterpret_cast<float2 *>(smem4);
-    float *X = reinterpret_cast<float *>(buf + P::B * P::LP);   // B x M
+    float *X = reinterpret_cast<float *>(buf + P::B * P::LP);   // B rows of x_stride(M)
     const long line0 = (long)blockIdx.x * P::B;
     const int b = threadIdx.x % P::B, t = threadIdx.x / P::B;
+    float *Xb = X + b * x_stride<L2>(M);
     const long l = line0 + b;
     const bool ok = l < nlines;
     const int kx = ok ? (int)(l % M) : 0;
@@ -157,10 +244,10 @@ __global__ void __launch_bounds__(Plan<L2>::THREADS) dct_cols_kernel(float *T, l
         // the denominator is -(4 sin^2(2 pi i/(4M-1)) + 4 sin^2(2 pi j/(4M-1))), free of cancellation
         if (kx == 0 && ky == 0) v = 0.f;
         else v = v / (-(ex + __ldg(&eig[ky])));
-        X[b * M + ky] = v;
+        Xb[ky] = v;
     }
     __syncthreads();
-    for (int p = t; p < L2; p += P::T) buf[b * P::LP + p] = idct_input(X + b * M, p, M, dtw, dT, mode);
+    for (int p = t; p < L2; p += P::T) buf[b * P::LP + p] = idct_input(Xb, p, M, dtw, dT, mode);
     __syncthreads();
     P::template run<true>(buf, tw);
     if (!ok) return;
@@ -169,12 +256,12 @@ __global__ void __launch_bounds__(Plan<L2>::THREADS) dct_cols_kernel(float *T, l
 
 // Pass 3: rows inverse.  T: [a][y][kx] -> out [a][y][x].
 template <int L2>
-__global__ void __launch_bounds__(Plan<L2>::THREADS) dct_rows_inv_kernel(const float *__restrict__ T, float *out,
-                                                                        long nlines, int M, int mode,
-                                                                        const float2 *__restrict__ dtw,
-                                                                        const float2 *__restrict__ tw)
+__global__ void __launch_bounds__(DctPlan<L2>::THREADS, dct_min_ctas<DctPlan<L2>>())
+    dct_rows_inv_kernel(const float *__restrict__ T, float *out, long nlines, int /* M = L2 / 2 */, int mode,
+                        const float2 *__restrict__ dtw, const float2 *__restrict__ tw)
 {
-    using P = Plan<L2>;
+    using P = DctPlan<L2>;
+    constexpr int M = L2 / 2;
     extern __shared__ float4 smem4[];
     float2 *buf = reinterpret_cast<float2 *>(smem4);
     float *X = reinterpret_cast<float *>(buf + P::B * P::LP);
@@ -210,11 +297,11 @@ static cudaError_t set_smem2(K kernel, size_t smem)
 template <int L2>
 static cudaError_t dct_launch(const float *phi, float *out, float *T, int A, int M, int mode, cudaStream_t s)
 {
-    using P = Plan<L2>;
+    using P = DctPlan<L2>;
     const long nl = (long)A * M;
     const unsigned grid = (unsigned)((nl + P::B - 1) / P::B);
-    const size_t smem1 = fftl::smem_bytes<L2>();
-    const size_t smem2 = smem1 + sizeof(float) * P::B * M;
+    const size_t smem1 = fftl::plan_smem<P>();
+    const size_t smem2 = smem1 + sizeof(float) * P::B * x_stride<L2>(M);
     const float2 *dtw = dct_twiddles(M);
     const float2 *tw = twiddles(L2);
     if (!dtw || !tw || !dct_eigen(M)) return cudaErrorInitializationError;   // device tables not built
@@ -247,11 +334,11 @@ template <int L2>
 static cudaError_t dct_launch_explicit(const float *phi, float *out, float *T, int A, int M, int mode,
                                        const float2 *tw, const float2 *dtw, const float *eig, cudaStream_t s)
 {
-    using P = Plan<L2>;
+    using P = DctPlan<L2>;
     const long nl = (long)A * M;
     const unsigned grid = (unsigned)((nl + P::B - 1) / P::B);
-    const size_t smem1 = fftl::smem_bytes<L2>();
-    const size_t smem2 = smem1 + sizeof(float) * P::B * M;
+    const size_t smem1 = fftl::plan_smem<P>();
+    const size_t smem2 = smem1 + sizeof(float) * P::B * x_stride<L2>(M);
     cudaError_t e = set_smem2<L2>(dct_rows_kernel<L2>, smem1);
     if (e != cudaSuccess) return e;
     dct_rows_kernel<L2><<<grid, P::THREADS, smem1, s>>>(phi, T, nl, M, dtw, tw); note_launch();

@@ -121,7 +121,7 @@ def test_dct_unwrap_golden_input(ctx, dev, oracle, mode):
         assert rmse(out.cpu().numpy(), ref_dump) < 1e-3   # the reference's float denominator
 
 
-@pytest.mark.parametrize("m", [16, 64, 128, 384, 768])
+@pytest.mark.parametrize("m", [16, 32, 64, 128, 256, 384, 512, 768])
 def test_dct_unwrap_sizes(ctx, dev, oracle, m):
     import torch
     rng = np.random.default_rng(m)
