@@ -267,6 +267,11 @@ def set_loop_scheme(r, scheme, device=0):
     check(load().ctdm_set_loop_scheme(int(device), int(r), int(scheme)), "ctdm_set_loop_scheme")
 
 
+def set_fill_list_capacity(capacity):
+    """Shared-memory list entries of the Goldstein flood fill (0: the default)."""
+    check(load().ctdm_set_fill_list_capacity(int(capacity)), "ctdm_set_fill_list_capacity")
+
+
 def plans(r, device=0):
     """(variants (x, y, z), tuned) currently used for side r."""
     v = (ctypes.c_int * 3)()

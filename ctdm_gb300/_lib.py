@@ -121,6 +121,7 @@ _SIGS = {
     "ctdm_set_plans": (c_int, [c_int, c_int, P_int]),
     "ctdm_loop_scheme": (c_int, [c_int, c_int, P_int]),
     "ctdm_set_loop_scheme": (c_int, [c_int, c_int, c_int]),
+    "ctdm_set_fill_list_capacity": (c_int, [c_int]),
     "ctdm_set_recon_globals": (None, [c_int, c_double, c_double, c_double, c_double, c_int, c_int, ctypes.c_char_p]),
     "DCT_UWLS_Unwrapped": (None, [c_void_p, c_void_p, c_int, c_int]),
     "FastUnwrapping": (None, [c_void_p, c_void_p, c_int, c_int]),

@@ -743,8 +743,8 @@ static ctdm_status pipeline_core(ctdm_ctx *c, const ctdm_params *p, int A, int M
     }
 
     // Goldstein: when its phase does not feed the reconstruction it runs on the side
-    // stream (latency-bound, one CTA per map) beside the memory-bound passes, and the
-    // call's stream joins it at the end.
+    // stream (latency-bound, one CTA per map) beside the loop passes, and the call's
+    // stream joins it at the end.
     const bool run_gold = p->run_goldstein || p->unwrap_method == CTDM_METHOD_GOLDSTEIN;
     const bool gold_side = run_gold && p->unwrap_method != CTDM_METHOD_GOLDSTEIN;
     if (run_gold) {
@@ -763,10 +763,21 @@ static ctdm_status pipeline_core(ctdm_ctx *c, const ctdm_params *p, int A, int M
     const float *unwrapped =
         p->unwrap_method == CTDM_METHOD_GOLDSTEIN ? B<float>(c, B_GOLD) : B<float>(c, B_PHU);
     // Front end per chunk of angles (one chunk unless the holograms arrive in chunks):
-    // QPI, unwrapping, spectra.  Goldstein runs once over all maps after the last
-    // chunk's QPI (its kernels are latency-bound per map, so chunks would repeat that
-    // latency); when its phase feeds the reconstruction the spectra follow it.
+    // QPI, unwrapping, spectra.  Goldstein runs once over all maps (its kernels are
+    // latency-bound per map, so chunks would repeat that latency): after the last
+    // chunk's QPI when its phase feeds the reconstruction (the spectra follow it), else
+    // on the side stream after the Ewald mapping.
     const bool gold_feeds = p->unwrap_method == CTDM_METHOD_GOLDSTEIN;
+    auto goldstein_all = [&](cudaStream_t gs) -> ctdm_status {
+        const float *ph_all = B<float>(c, B_PHASE);
+        CK(goldstein_residues(ph_all, A, M, M, B<int8_t>(c, B_CHG), gs), "goldstein residues");
+        CK(goldstein_cuts(B<int8_t>(c, B_CHG), A, M, M, B<uint8_t>(c, B_CUT), B<int8_t>(c, B_GWORK), gs),
+           "goldstein cuts");
+        CK(goldstein_floodfill(B<uint8_t>(c, B_CUT), ph_all, A, M, M, B<float>(c, B_GOLD), B<uint8_t>(c, B_GSTATE),
+                               B<int>(c, B_GLIST), B<int>(c, B_GSTATUS), gs),
+           "goldstein flood fill");
+        return CTDM_OK;
+    };
     auto spectra = [&](int a0, int ac) -> ctdm_status {
         const long o = (long)a0 * mm;
         float2 *U = B<float2>(c, B_U) + (long)a0 * rr;
@@ -787,27 +798,9 @@ static ctdm_status pipeline_core(ctdm_ctx *c, const ctdm_params *p, int A, int M
             if (st != CTDM_OK) return st;
             tm.mark(S_QPI, s);
         }
-        if (run_gold && k == nchunks - 1) {
-            cudaStream_t gs = s;
-            if (gold_side) {
-                CK(cudaEventRecord(c->fork, s), "fork");
-                CK(cudaStreamWaitEvent(c->side, c->fork, 0), "fork wait");
-                gs = c->side;
-                tm.side_mark(gs);
-            }
-            const float *ph_all = B<float>(c, B_PHASE);
-            CK(goldstein_residues(ph_all, A, M, M, B<int8_t>(c, B_CHG), gs), "goldstein residues");
-            CK(goldstein_cuts(B<int8_t>(c, B_CHG), A, M, M, B<uint8_t>(c, B_CUT), B<int8_t>(c, B_GWORK), gs),
-               "goldstein cuts");
-            CK(goldstein_floodfill(B<uint8_t>(c, B_CUT), ph_all, A, M, M, B<float>(c, B_GOLD), B<uint8_t>(c, B_GSTATE),
-                                   B<int>(c, B_GLIST), B<int>(c, B_GSTATUS), gs),
-               "goldstein flood fill");
-            if (gold_side) {
-                tm.side_mark(gs);
-                CK(cudaEventRecord(c->join, gs), "join");
-            } else {
-                tm.mark(S_GOLD, s);
-            }
+        if (run_gold && !gold_side && k == nchunks - 1) {
+            if ((st = goldstein_all(s)) != CTDM_OK) return st;
+            tm.mark(S_GOLD, s);
         }
         if (gold_feeds) continue;
         if (p->unwrap_method == CTDM_METHOD_DCT) {
@@ -844,6 +837,16 @@ static ctdm_status pipeline_core(ctdm_ctx *c, const ctdm_params *p, int A, int M
     ea.mask = mask_mode ? B<uint8_t>(c, B_MASK) : nullptr;
     CK(launch_ewald(ea, s), "ewald mapping");
     tm.mark(S_EWALD, s);
+    if (gold_side) {
+        // forked after the mapping, whose CTAs lose room on an SM to a resident fill,
+        // so that it runs beside the loop passes
+        CK(cudaEventRecord(c->fork, s), "fork");
+        CK(cudaStreamWaitEvent(c->side, c->fork, 0), "fork wait");
+        tm.side_mark(c->side);
+        if ((st = goldstein_all(c->side)) != CTDM_OK) return st;
+        tm.side_mark(c->side);
+        CK(cudaEventRecord(c->join, c->side), "join");
+    }
     st = do_positivity(c, R, p->iterations, p->check_mode, k * k, p->n_med, B<float2>(c, B_F2),
                        mask_mode ? B<uint8_t>(c, B_MASK) : nullptr, B<float2>(c, B_G),
                        reinterpret_cast<float2 *>(d_ri), s);

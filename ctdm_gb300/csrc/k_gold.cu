@@ -23,6 +23,7 @@
 // from the visiting order.  One CTA per map, state bits in shared memory.
 #include <cmath>
 
+#include "api_internal.h"
 #include "kernels_front.cuh"
 
 namespace ctdm {
@@ -124,17 +125,44 @@ __device__ __forceinline__ void seq_cell(unsigned s, unsigned m1, unsigned m2, u
     nn = n1 + s;
 }
 
+// Residues of a map in index order, gathered before any cut is placed: lanes load
+// CUTS_BATCH bytes each per step, all independent (the charges are mostly zero, and
+// one dependent load per 32 pixels made the scan most of the kernel's time).  Pairing
+// only clears charges, so a gathered residue that is already paired is skipped.
+constexpr int CUTS_BATCH = 32, CUTS_LIST = 2048;
+
 __global__ void __launch_bounds__(32) cuts_kernel(const int8_t *__restrict__ charges, int W, int H, uint8_t *cuts,
                                                   int8_t *work)
 {
+    __shared__ unsigned s_res[CUTS_LIST];
     const int a = blockIdx.x, lane = threadIdx.x;
     const long n = (long)W * H;
     volatile int8_t *masked = work + a * n;
     volatile uint8_t *cut = cuts + a * n;
-    const int8_t *q = charges + a * n;
-    for (long p = lane; p < n; p += 32) {
-        masked[p] = q[p];
-        cut[p] = 0;
+    const int8_t *__restrict__ q = charges + a * n;
+    int nres = 0;
+    for (long base = 0; base < n; base += 32 * CUTS_BATCH) {
+        int v[CUTS_BATCH];
+#pragma unroll
+        for (int k = 0; k < CUTS_BATCH; k++) {
+            const long pl = base + 32 * k + lane;
+            v[k] = pl < n ? __ldg(q + pl) : 0;
+        }
+#pragma unroll
+        for (int k = 0; k < CUTS_BATCH; k++) {
+            const long pl = base + 32 * k + lane;
+            if (pl < n) {
+                masked[pl] = (int8_t)v[k];
+                cut[pl] = 0;
+            }
+            unsigned pend = __ballot_sync(0xffffffffu, v[k] != 0);
+            while (pend) {
+                const int l = __ffs(pend) - 1;
+                pend &= pend - 1;
+                if (lane == 0 && nres < CUTS_LIST) s_res[nres] = (unsigned)(base + 32 * k + l);
+                nres++;
+            }
+        }
     }
     __syncwarp();
     int maxBox = 901;
@@ -144,10 +172,20 @@ __global__ void __launch_bounds__(32) cuts_kernel(const int8_t *__restrict__ cha
     const unsigned hr = (unsigned)__float2int_rn(__fmul_rn((float)W, 0.5f));
     if (hr < maxR) maxR = hr;
     const unsigned uW = (unsigned)W, uH = (unsigned)H;
-    for (long base = 0; base < n; base += 32) {
-        const long pl = base + lane;
-        const int v = pl < n ? masked[pl] : 0;
-        unsigned pend = __ballot_sync(0xffffffffu, v != 0);
+    // more residues than the list holds: walk the map in the same order instead
+    const bool listed = nres <= CUTS_LIST;
+    const long nsteps = listed ? (long)nres : (n + 31) / 32;
+    for (long it = 0; it < nsteps; it++) {
+        long base;
+        unsigned pend;
+        if (listed) {
+            base = (long)s_res[it];
+            pend = 1u;
+        } else {
+            base = it * 32;
+            const long pl = base + lane;
+            pend = __ballot_sync(0xffffffffu, (pl < n ? masked[pl] : 0) != 0);
+        }
         while (pend) {
             const int l = __ffs(pend) - 1;
             pend &= pend - 1;
@@ -287,13 +325,20 @@ __device__ __forceinline__ float unwrap_from(float ref, float ph)
     return __fadd_rn(ref, dp);
 }
 
+// Lists of one fill: cur / nxt / prev hold pixel indices, ref and nv are indexed by
+// the position in cur.  cap is their capacity; a longer list is an overflow.
 struct FFLists {
     int *cur, *nxt, *prev, *ref;
     float *nv;
+    int cap;
 };
 
 // One sweep over the list (use_cuts: main loop; else the final cut-pixel fill,
-// which ignores cuts and makes no marks).  Marks append to lists.nxt.
+// which ignores cuts and makes no marks).  Marks append to lists.nxt (past cap they
+// are counted, not stored).  Values reach o in two steps: those whose reference was
+// unwrapped before the sweep are computed from the old o, then published together
+// after a barrier (so every such read sees the old value); the rest are computed in
+// dependency rounds from values already published in o.
 __device__ void sweep(uint8_t *st, const FFLists &ls, int L, int *nnext, const float *ph, float *o, int W, int H,
                       bool use_cuts)
 {
@@ -362,9 +407,14 @@ __device__ void sweep(uint8_t *st, const FFLists &ls, int L, int *nnext, const f
         const unsigned sn = st[nb];
         const bool dep = (sn & F_LIST) && nb < p && (sn & F_CAND);
         if (!dep) {
-            ls.nv[p] = unwrap_from(o[nb], ph[p]);
+            ls.nv[e] = unwrap_from(o[nb], ph[p]);
             st[p] = (uint8_t)(s | F_READY);
         }
+    }
+    __syncthreads();
+    for (int e = t; e < L; e += FF_THREADS) {
+        const int p = list[e];
+        if ((st[p] & (F_CAND | F_READY)) == (F_CAND | F_READY)) o[p] = ls.nv[e];
     }
     __syncthreads();
     // dependency rounds: a value computed in a round is published (F_READY) only
@@ -378,7 +428,7 @@ __device__ void sweep(uint8_t *st, const FFLists &ls, int L, int *nnext, const f
             if (!(s & F_CAND) || (s & F_READY)) continue;
             const int nb = ls.ref[e];
             if (st[nb] & F_READY) {
-                ls.nv[p] = unwrap_from(ls.nv[nb], ph[p]);
+                o[p] = unwrap_from(o[nb], ph[p]);
                 st[p] = (uint8_t)(s | F_PREV);
             } else {
                 pending = true;
@@ -405,7 +455,10 @@ __device__ void sweep(uint8_t *st, const FFLists &ls, int L, int *nnext, const f
                 if (sn & F_CUT) continue;
                 if (ub_at_visit(st, nb, p)) continue;
                 if (!(sn & F_LIST) || nb < p) {
-                    if (!(byte_or(st + nb, F_MARK) & F_MARK)) ls.nxt[atomicAdd(nnext, 1)] = nb;
+                    if (!(byte_or(st + nb, F_MARK) & F_MARK)) {
+                        const int q = atomicAdd(nnext, 1);
+                        if (q < ls.cap) ls.nxt[q] = nb;
+                    }
                 }
             }
         }
@@ -414,32 +467,174 @@ __device__ void sweep(uint8_t *st, const FFLists &ls, int L, int *nnext, const f
     for (int e = t; e < L; e += FF_THREADS) {
         const int p = list[e];
         const unsigned s = st[p];
-        if (s & F_CAND) o[p] = ls.nv[p];
         st[p] = (uint8_t)((s & (F_CUT | F_MARK)) | ((s & F_NEW) ? F_UB : 0u) | F_PREV);
     }
     __syncthreads();
 }
 
-template <bool SMEM>
-__global__ void __launch_bounds__(FF_THREADS) floodfill_kernel(const uint8_t *__restrict__ cuts,
-                                                              const float *__restrict__ phi, int W, int H, float *out,
-                                                              uint8_t *gstate, int *lists, int *status)
+// The sweep for lists of at most FF_THREADS pixels, one per thread, with the pixel's
+// index, state and neighbours in registers.  It also does the list's conversion
+// (MARK -> LIST) and clears F_PREV of the previous list, and returns whether every
+// pixel of the list was in the previous one.  Its phases, each ended by a barrier:
+//   1. conversion, candidates (from UB and CUT, which no phase of the sweep changes),
+//      loads of ph[p] and of the neighbours' old values in o;
+//   2. F_PREV cleared on the previous list's pixels outside this list (the owners
+//      clear their own), and the fixed point over left / upper neighbours;
+//   3. reference neighbour; a value whose reference is not a pixel of this sweep
+//      computed from the loaded old value and stored in o at once (every read of an
+//      old value was issued before barrier 1);
+//   4. dependency rounds, only when some pixel waits on another of this sweep;
+//   5. adjoin marks (atomics only); 6. the final states.
+// Plain stores to st touch only the owner's pixel except in phase 2, where the
+// stores go to pixels outside the list, so no byte store races an atomic or another
+// store to the same byte.
+__device__ bool sweep_owned(uint8_t *st, const FFLists &ls, int L, int Lprev, int *nnext, const float *ph, float *o,
+                            int W, int H)
 {
-    extern __shared__ uint8_t sstate[];
-    __shared__ int s_ok, s_nnext;
-    const int a = blockIdx.x, t = threadIdx.x;
+    const int t = threadIdx.x;
+    const bool own = t < L;
+    int p = 0;
+    unsigned s = 0;
+    int nbk[4] = {0, 0, 0, 0};
+    bool okk[4] = {false, false, false, false};
+    float onb[4] = {0.f, 0.f, 0.f, 0.f};
+    float phv = 0.f;
+    bool all_prev = true;
+    if (own) {
+        p = ls.cur[t];
+#pragma unroll
+        for (int k = 0; k < 4; k++) okk[k] = neighbour(p, k, W, H, nbk[k]);
+        phv = ph[p];
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            if (okk[k]) onb[k] = o[nbk[k]];
+        s = st[p];
+        all_prev = (s & F_PREV) != 0;
+        s = (s & ~(F_MARK | F_PREV)) | F_LIST;
+        bool cand = false;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            if (!okk[k]) continue;
+            const unsigned sn = st[nbk[k]];
+            if (sn & F_CUT) continue;
+            if (sn & F_UB) cand = true;
+        }
+        if (cand) s |= F_CAND | F_NEW;
+        if (s & F_UB) s |= F_NEW;
+        st[p] = (uint8_t)s;
+    }
+    const bool same = __syncthreads_and(all_prev);
+    for (int e = t; e < Lprev; e += FF_THREADS) {
+        const int q = ls.prev[e];
+        const unsigned r = st[q];
+        if (!(r & F_LIST)) st[q] = (uint8_t)(r & ~F_PREV);
+    }
+    for (int guard = 0; guard <= L; guard++) {
+        bool changed = false;
+        if (own && !(s & F_CAND)) {
+            bool cand = false;
+#pragma unroll
+            for (int k = 1; k < 4; k += 2) {
+                if (!okk[k]) continue;
+                const unsigned sn = st[nbk[k]];
+                if (sn & F_CUT) continue;
+                if ((sn & F_LIST) && (sn & F_NEW)) cand = true;
+            }
+            if (cand) {
+                s |= F_CAND | F_NEW;
+                st[p] = (uint8_t)s;
+                changed = true;
+            }
+        }
+        if (!__syncthreads_or(changed)) break;
+    }
+    int kref = -1;
+    bool wait_dep = false;
+    if (own && (s & F_CAND)) {
+        unsigned sref = 0;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            if (kref >= 0 || !okk[k]) continue;
+            const unsigned sn = st[nbk[k]];
+            if (sn & F_CUT) continue;
+            const bool ub = ((sn & F_LIST) && nbk[k] < p) ? (sn & F_NEW) != 0 : (sn & F_UB) != 0;
+            if (ub) {
+                kref = k;
+                sref = sn;
+            }
+        }
+        // a candidate always has a reference: an unwrapped neighbour made it one
+        if (kref >= 0) {
+            wait_dep = (sref & F_LIST) && nbk[kref] < p && (sref & F_CAND);
+            if (!wait_dep) {
+                o[p] = unwrap_from(onb[kref], phv);
+                s |= F_READY;
+                st[p] = (uint8_t)s;
+            }
+        }
+    }
+    if (__syncthreads_or(wait_dep)) {
+        for (int guard = 0; guard <= L; guard++) {
+            bool done_now = false;
+            if (wait_dep) {
+                const int nb = nbk[kref];
+                if (st[nb] & F_READY) {
+                    o[p] = unwrap_from(o[nb], phv);
+                    done_now = true;
+                }
+            }
+            __syncthreads();
+            if (done_now) {
+                s |= F_READY;
+                st[p] = (uint8_t)s;
+                wait_dep = false;
+            }
+            if (!__syncthreads_or(wait_dep)) break;
+        }
+    }
+    if (own) {
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            if (!okk[k]) continue;
+            const int nb = nbk[k];
+            const unsigned sn = st[nb];
+            if (sn & F_CUT) continue;
+            const bool ub = ((sn & F_LIST) && nb < p) ? (sn & F_NEW) != 0 : (sn & F_UB) != 0;
+            if (ub) continue;
+            if (!(sn & F_LIST) || nb < p) {
+                if (!(byte_or(st + nb, F_MARK) & F_MARK)) {
+                    const int q = atomicAdd(nnext, 1);
+                    if (q < ls.cap) ls.nxt[q] = nb;
+                }
+            }
+        }
+    }
+    __syncthreads();
+    if (own) {
+        const unsigned r = st[p];
+        st[p] = (uint8_t)((r & (F_CUT | F_MARK)) | ((r & F_NEW) ? F_UB : 0u) | F_PREV);
+    }
+    __syncthreads();
+    return same;
+}
+
+// Shared-memory lists per fill (each of cur, nxt, prev, ref, nv): a sweep's list is
+// the front of the fill, 170 pixels on average and a few hundred at most on 256 x 256
+// maps; a fill whose list outgrows the capacity starts over on the global lists.  The
+// fill runs beside the reconstruction's loop passes, which lose resident CTAs to a
+// larger footprint: 3072 entries (124 KB with the states) slowed the loop by 0.5 ms.
+constexpr int FF_SMEM_MAX = 3072, FF_SMEM_CAP = 1024;
+static int g_fill_cap = FF_SMEM_CAP;   // set by ctdm_set_fill_list_capacity
+
+// The fill of one map (FloodFill, cTDM/PhaseUnwrapping.cu).  Returns the status (0
+// done, 1 sweep limit, 2 no seed) or -1 when a list outgrew ls.cap.
+// s_cnt[2]: list lengths; the list of sweep j is counted in s_cnt[j & 1] while sweep j
+// counts the next one in s_cnt[(j + 1) & 1].
+__device__ int fill_map(uint8_t *st, const uint8_t *cut, const float *ph, float *o, int W, int H, FFLists ls,
+                        int *s_ok, int *s_cnt)
+{
+    const int t = threadIdx.x;
     const long n = (long)W * H;
-    uint8_t *st = SMEM ? sstate : gstate + a * n;
-    const uint8_t *cut = cuts + a * n;
-    const float *ph = phi + a * n;
-    float *o = out + a * n;
-    int *base = lists + a * 5 * n;
-    FFLists ls;
-    ls.cur = base;
-    ls.nxt = base + n;
-    ls.prev = base + 2 * n;
-    ls.ref = base + 3 * n;
-    ls.nv = reinterpret_cast<float *>(base + 4 * n);
     int nbc_local = 0;
     for (long p = t; p < n; p += FF_THREADS) {
         st[p] = cut[p] ? (uint8_t)F_CUT : (uint8_t)0;
@@ -472,53 +667,58 @@ __global__ void __launch_bounds__(FF_THREADS) floodfill_kernel(const uint8_t *__
             st[seed] |= F_UB;
             o[seed] = ph[seed];
         }
-        s_ok = ok;
-        s_nnext = cnt;
+        *s_ok = ok;
+        s_cnt[0] = cnt;
+        s_cnt[1] = 0;
     }
     __syncthreads();
-    if (!s_ok) {
-        if (t == 0) status[a] = 2;
-        return;
-    }
-    int L1 = 0, Lprev = 0, countLimit = 0, stat = 0;
+    if (!*s_ok) return 2;
+    int L1 = 0, Lprev = 0, countLimit = 0, stat = 0, j = 0;
     bool abort_fill = false;
     for (int outer = 0; outer < 4; outer++) {
         __syncthreads();
-        if (s_nnext == 0) break;
+        if (s_cnt[j & 1] == 0) break;
         if (countLimit >= 2) { stat = 2; break; }
         int term = 0;
         while (countLimit < 2) {
             if (++term > 5000) { stat = 1; abort_fill = true; break; }
-            // the marked pixels become this sweep's list
+            // the marked pixels become this sweep's list (every sweep ends with a barrier,
+            // after which its count is final and the other counter unread)
             int *tmp = ls.prev;
             ls.prev = ls.cur;
             ls.cur = ls.nxt;
             ls.nxt = tmp;
-            __syncthreads();
-            const int L2 = s_nnext;
-            __syncthreads();
-            if (t == 0) s_nnext = 0;
-            bool all_prev = true;
-            for (int e = t; e < L2; e += FF_THREADS) {
-                const int p = ls.cur[e];
-                const unsigned s = st[p];
-                all_prev &= (s & F_PREV) != 0;
-                st[p] = (uint8_t)((s & ~F_MARK) | F_LIST);
+            const int L2 = s_cnt[j & 1];
+            if (L2 > ls.cap) return -1;
+            int *nnext = &s_cnt[(j + 1) & 1];
+            if (t == 0) *nnext = 0;
+            bool same;
+            if (L2 <= FF_THREADS) {
+                same = sweep_owned(st, ls, L2, Lprev, nnext, ph, o, W, H);
+            } else {
+                bool all_prev = true;
+                for (int e = t; e < L2; e += FF_THREADS) {
+                    const int p = ls.cur[e];
+                    const unsigned s = st[p];
+                    all_prev &= (s & F_PREV) != 0;
+                    st[p] = (uint8_t)((s & ~F_MARK) | F_LIST);
+                }
+                same = __syncthreads_and(all_prev);
+                for (int e = t; e < Lprev; e += FF_THREADS) {
+                    const int p = ls.prev[e];
+                    st[p] = (uint8_t)(st[p] & ~F_PREV);
+                }
+                __syncthreads();
+                sweep(st, ls, L2, nnext, ph, o, W, H, true);
             }
-            const bool same = __syncthreads_and(all_prev);
             if (L1 == L2) {
                 if (same) countLimit++;
             } else {
                 countLimit = 0;
             }
-            for (int e = t; e < Lprev; e += FF_THREADS) {
-                const int p = ls.prev[e];
-                st[p] = (uint8_t)(st[p] & ~F_PREV);
-            }
-            __syncthreads();
-            sweep(st, ls, L2, &s_nnext, ph, o, W, H, true);
             L1 = L2;
             Lprev = L2;
+            j++;
         }
         if (abort_fill) break;
     }
@@ -530,8 +730,9 @@ __global__ void __launch_bounds__(FF_THREADS) floodfill_kernel(const uint8_t *__
             const int p = ls.cur[e];
             st[p] = (uint8_t)(st[p] & ~F_PREV);
         }
+        int *s_nnext = &s_cnt[0];
         __syncthreads();
-        if (t == 0) s_nnext = 0;
+        if (t == 0) *s_nnext = 0;
         __syncthreads();
         for (long p = t; p < n; p += FF_THREADS) {
             const unsigned s = st[p];
@@ -539,10 +740,14 @@ __global__ void __launch_bounds__(FF_THREADS) floodfill_kernel(const uint8_t *__
             bool add = (s & F_MARK) != 0;
             if (!add && (s & F_CUT) && rr >= 1 && rr <= W - 2 && cc >= 1 && cc <= H - 2)
                 add = !(st[p + 1] & F_CUT) || !(st[p - 1] & F_CUT) || !(st[p - W] & F_CUT) || !(st[p + W] & F_CUT);
-            if (add) ls.nxt[atomicAdd(&s_nnext, 1)] = (int)p;
+            if (add) {
+                const int q = atomicAdd(s_nnext, 1);
+                if (q < ls.cap) ls.nxt[q] = (int)p;
+            }
         }
         __syncthreads();
-        const int L2 = s_nnext;
+        const int L2 = *s_nnext;
+        if (L2 > ls.cap) return -1;
         for (int e = t; e < L2; e += FF_THREADS) {
             const int p = ls.nxt[e];
             st[p] = (uint8_t)((st[p] & ~F_MARK) | F_LIST);
@@ -551,9 +756,52 @@ __global__ void __launch_bounds__(FF_THREADS) floodfill_kernel(const uint8_t *__
         ls.cur = ls.nxt;
         ls.nxt = tmp;
         __syncthreads();
-        sweep(st, ls, L2, &s_nnext, ph, o, W, H, false);
+        sweep(st, ls, L2, s_nnext, ph, o, W, H, false);
     }
-    if (t == 0) status[a] = stat;
+    return stat;
+}
+
+// One CTA per map.  SMEM: the pixel states (n bytes) and the lists live in shared
+// memory, the lists with capacity min(n, FF_SMEM_CAP) and the global ones (5 n ints per
+// map) as the fallback; otherwise states and lists are global.
+template <bool SMEM>
+__global__ void __launch_bounds__(FF_THREADS) floodfill_kernel(const uint8_t *__restrict__ cuts,
+                                                              const float *__restrict__ phi, int W, int H, float *out,
+                                                              uint8_t *gstate, int *lists, int *status,
+                                                              int smem_cap)
+{
+    extern __shared__ __align__(16) uint8_t sstate[];
+    __shared__ int s_ok, s_cnt[2];
+    const int a = blockIdx.x;
+    const long n = (long)W * H;
+    uint8_t *st = SMEM ? sstate : gstate + a * n;
+    const uint8_t *cut = cuts + a * n;
+    const float *ph = phi + a * n;
+    float *o = out + a * n;
+    int *base = lists + a * 5 * n;
+    FFLists gl;
+    gl.cur = base;
+    gl.nxt = base + n;
+    gl.prev = base + 2 * n;
+    gl.ref = base + 3 * n;
+    gl.nv = reinterpret_cast<float *>(base + 4 * n);
+    gl.cap = (int)n;
+    int stat = -1;
+    if constexpr (SMEM) {
+        const int cap = n < smem_cap ? (int)n : smem_cap;
+        int *sl = reinterpret_cast<int *>(sstate + ((n + 15) & ~15L));
+        FFLists sm;
+        sm.cur = sl;
+        sm.nxt = sl + cap;
+        sm.prev = sl + 2 * cap;
+        sm.ref = sl + 3 * cap;
+        sm.nv = reinterpret_cast<float *>(sl + 4 * cap);
+        sm.cap = cap;
+        stat = fill_map(st, cut, ph, o, W, H, sm, &s_ok, s_cnt);
+        __syncthreads();
+    }
+    if (stat < 0) stat = fill_map(st, cut, ph, o, W, H, gl, &s_ok, s_cnt);
+    if (threadIdx.x == 0) status[a] = stat;
 }
 
 cudaError_t goldstein_floodfill(const uint8_t *cuts, const float *phi, int A, int W, int H, float *out, uint8_t *state,
@@ -561,15 +809,26 @@ cudaError_t goldstein_floodfill(const uint8_t *cuts, const float *phi, int A, in
 {
     const long n = (long)W * H;
     if (n <= 96 * 1024) {
-        const size_t smem = (size_t)((n + 3) & ~3L);
+        const int cap = n < g_fill_cap ? (int)n : g_fill_cap;
+        const size_t smem = (size_t)(((n + 15) & ~15L) + 5 * sizeof(int) * (size_t)cap);
         cudaError_t e = cudaFuncSetAttribute(floodfill_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
         if (e != cudaSuccess) return e;
-        floodfill_kernel<true><<<A, FF_THREADS, smem, s>>>(cuts, phi, W, H, out, state, lists, status); note_launch();
+        floodfill_kernel<true><<<A, FF_THREADS, smem, s>>>(cuts, phi, W, H, out, state, lists, status, cap);
+        note_launch();
     } else {
-        floodfill_kernel<false><<<A, FF_THREADS, 0, s>>>(cuts, phi, W, H, out, state, lists, status); note_launch();
+        floodfill_kernel<false><<<A, FF_THREADS, 0, s>>>(cuts, phi, W, H, out, state, lists, status, 0);
+        note_launch();
     }
     return cudaGetLastError();
 }
 
 }  // namespace ctdm
+
+extern "C" ctdm_status ctdm_set_fill_list_capacity(int capacity)
+{
+    if (capacity != 0 && (capacity < 16 || capacity > ctdm::FF_SMEM_MAX))
+        return ctdm::fail_invalid("ctdm_set_fill_list_capacity: capacity outside 16..3072");
+    ctdm::g_fill_cap = capacity == 0 ? ctdm::FF_SMEM_CAP : capacity;
+    return CTDM_OK;
+}

@@ -214,6 +214,10 @@ CTDM_API ctdm_status ctdm_goldstein(ctdm_ctx *ctx, int A, int W, int H, const fl
 /* Flood fill alone with caller-provided branch cuts (0/1 per pixel). */
 CTDM_API ctdm_status ctdm_goldstein_fill(ctdm_ctx *ctx, int A, int W, int H, const uint8_t *d_cuts, const float *d_phi,
                                          float *d_out, int *h_status, void *stream);
+/* Entries per list (16..3072; 0: the default 1024) that the flood fill of maps of up
+ * to 96 Ki pixels keeps in shared memory; a fill whose list outgrows them starts over
+ * on global lists, with the same result.  Applies to later launches in the process. */
+CTDM_API ctdm_status ctdm_set_fill_list_capacity(int capacity);
 /* Resize M -> N, centre crop R, median + checkMaps, u = log A + i phi (transposed,
  * quadrant-swapped), forward FFT2: d_U (A*R*R complex). */
 CTDM_API ctdm_status ctdm_prepare_spectra(ctdm_ctx *ctx, int A, int M, int N, int R, const float *d_phase,

@@ -57,6 +57,27 @@ def test_goldstein_global_state_path(ctx, dev, oracle):
     assert st[0] == ost and np.sqrt(np.mean((o[0] - oo) ** 2)) < PHASE_TOL
 
 
+@pytest.mark.parametrize("cap", [16, 200])
+def test_goldstein_list_overflow_restart(ctx, dev, oracle, cap):
+    """A fill whose list outgrows the shared-memory capacity starts over on the global
+    lists: the same result, bit for bit, as with room to spare."""
+    import ctdm_gb300 as C
+    maps = np.stack([noisy_phase(256, s, 0.6) for s in range(2)])
+    ref = run_gpu(ctx, dev, maps)
+    try:
+        C.set_fill_list_capacity(cap)
+        got = run_gpu(ctx, dev, maps)
+    finally:
+        C.set_fill_list_capacity(0)
+    assert np.array_equal(got[2], ref[2]) and np.array_equal(got[3], ref[3])
+    oo, _, ost = oracle.goldstein_floodfill(oracle.goldstein_cuts(oracle.goldstein_residues(maps[0])), maps[0])
+    assert ref[3][0] == ost and np.sqrt(np.mean((ref[2][0] - oo) ** 2)) < PHASE_TOL
+    with pytest.raises(Exception):
+        C.set_fill_list_capacity(8)
+    with pytest.raises(Exception):
+        C.set_fill_list_capacity(4096)
+
+
 def test_goldstein_enclosed_regions(ctx, dev, oracle):
     """Planted cut pixels enclose regions the fill cannot reach; status, reached set
     and values still match the serial specification."""
