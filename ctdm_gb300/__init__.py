@@ -102,6 +102,29 @@ class Context:
                                        _ptr(angx), _ptr(angy), _ptr(out)), fn[0])
         return out
 
+    def submit(self, params, holo, bg, angx, angy, out):
+        """ctdm_submit: enqueue a host-buffer reconstruction into `out` and return.  The
+        arrays (numpy, or pinned torch CPU tensors for overlapped copies) must stay alive
+        and `out` unread until wait()."""
+        def ptr_dtype(a):
+            if hasattr(a, "data_ptr"):
+                return a.data_ptr(), {"torch.uint16": 2, "torch.uint8": 1, "torch.float32": 4}[str(a.dtype)]
+            a = np.asarray(a)
+            bpc = {np.dtype(np.uint16): 2, np.dtype(np.uint8): 1, np.dtype(np.float32): 4}[a.dtype]
+            assert a.flags.c_contiguous
+            return a.ctypes.data, bpc
+        hp, bpc = ptr_dtype(holo)
+        bp, bpc_bg = ptr_dtype(bg)
+        op = out.data_ptr() if hasattr(out, "data_ptr") else np.asarray(out).ctypes.data
+        if bpc != bpc_bg:
+            raise ValueError("holograms and background must have the same type")
+        angx, angy = _f32(angx), _f32(angy)
+        check(self.lib.ctdm_submit(self.handle, ctypes.byref(params), len(angx), hp, bp, bpc, _ptr(angx), _ptr(angy),
+                                   op), "ctdm_submit")
+
+    def wait(self):
+        check(self.lib.ctdm_wait(self.handle), "ctdm_wait")
+
     def carrier(self):
         c = (ctypes.c_int * 3)()
         check(self.lib.ctdm_ctx_carrier(self.handle, c), "ctdm_ctx_carrier")

@@ -79,6 +79,9 @@ _SIGS = {
                                      c_void_p, c_void_p]),
     "ctdm_reconstruct_u8": (c_int, [c_void_p, ctypes.POINTER(Params), c_int, c_void_p, c_void_p, c_void_p,
                                     c_void_p, c_void_p]),
+    "ctdm_submit": (c_int, [c_void_p, ctypes.POINTER(Params), c_int, c_void_p, c_void_p, c_int, c_void_p, c_void_p,
+                            c_void_p]),
+    "ctdm_wait": (c_int, [c_void_p]),
     "ctdm_qpi": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_int, P_int, c_void_p, c_void_p,
                          c_void_p]),
     "ctdm_qpi_b": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_int, P_int, c_void_p, c_void_p, c_void_p]),

@@ -255,6 +255,7 @@ struct ctdm_ctx {
     struct Pinned {
         AngleGeom geom[512];
         int carrier[4];
+        int derr;
     } *pin = nullptr;
     cudaEvent_t geom_done = nullptr, carrier_done = nullptr;
     bool carrier_pending = false;
@@ -262,6 +263,12 @@ struct ctdm_ctx {
     static const int kChunks = 16;
     cudaStream_t copy = nullptr;
     cudaEvent_t ready[kChunks + 1] = {};
+    // host-buffer calls in flight (ctdm_submit): the input buffers are free again once
+    // a call's front end has read them (inputs_free), the volume is downloaded on its own
+    // stream after vol_ready and may be overwritten after vol_free
+    cudaStream_t d2h = nullptr;
+    cudaEvent_t inputs_free = nullptr, vol_ready = nullptr, vol_free = nullptr;
+    int in_flight = 0;
     // device status word (bounded device-side waits record a code here)
     int *d_err = nullptr;
 };
@@ -272,6 +279,8 @@ struct ctdm_ctx {
 struct ChunkFeed {
     const cudaEvent_t *ready;
     int per;
+    cudaEvent_t inputs_free;   // recorded once the front end has read the inputs
+    cudaEvent_t out_free;      // the output volume may be written after it
 };
 
 static cudaError_t ensure(ctdm_ctx *c, int id, size_t bytes)
@@ -322,6 +331,10 @@ extern "C" ctdm_status ctdm_ctx_create(int device, ctdm_ctx **out)
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->copy, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->d2h, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->inputs_free, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->vol_ready, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->vol_free, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMallocHost(&c->pin, sizeof(ctdm_ctx::Pinned));
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->geom_done, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->carrier_done, cudaEventDisableTiming);
@@ -342,6 +355,10 @@ extern "C" void ctdm_ctx_destroy(ctdm_ctx *c)
 {
     if (!c) return;
     cudaSetDevice(c->device);
+    // calls still in flight (ctdm_submit without ctdm_wait) finish before the buffers go
+    for (cudaStream_t st : {c->copy, c->d2h, c->side})
+        if (st) cudaStreamSynchronize(st);
+    if (c->in_flight) cudaStreamSynchronize(0);
     for (int i = 0; i < NBUF; i++)
         if (c->buf[i]) cudaFree(c->buf[i]);
     for (int i = 0; i < StageTimer::kMax; i++)
@@ -350,8 +367,9 @@ extern "C" void ctdm_ctx_destroy(ctdm_ctx *c)
         if (c->timer.side[i]) cudaEventDestroy(c->timer.side[i]);
     if (c->side) cudaStreamDestroy(c->side);
     if (c->copy) cudaStreamDestroy(c->copy);
+    if (c->d2h) cudaStreamDestroy(c->d2h);
     if (c->pin) cudaFreeHost(c->pin);
-    for (cudaEvent_t e : {c->geom_done, c->carrier_done})
+    for (cudaEvent_t e : {c->geom_done, c->carrier_done, c->inputs_free, c->vol_ready, c->vol_free})
         if (e) cudaEventDestroy(e);
     for (cudaEvent_t e : c->ready)
         if (e) cudaEventDestroy(e);
@@ -817,6 +835,7 @@ static ctdm_status pipeline_core(ctdm_ctx *c, const ctdm_params *p, int A, int M
         if ((st = spectra(a0, ac)) != CTDM_OK) return st;
     }
     if (gold_feeds && (st = spectra(0, A)) != CTDM_OK) return st;
+    if (feed && feed->inputs_free) CK(cudaEventRecord(feed->inputs_free, s), "inputs read");
 
     const double fm0 = p->n_med / p->wavelength;
     const double df = 1.0 / (R * p->dx);
@@ -847,6 +866,8 @@ static ctdm_status pipeline_core(ctdm_ctx *c, const ctdm_params *p, int A, int M
         tm.side_mark(c->side);
         CK(cudaEventRecord(c->join, c->side), "join");
     }
+    // the final pass writes the output volume: the previous call's download of it first
+    if (feed && feed->out_free) CK(cudaStreamWaitEvent(s, feed->out_free, 0), "wait for the volume download");
     st = do_positivity(c, R, p->iterations, p->check_mode, k * k, p->n_med, B<float2>(c, B_F2),
                        mask_mode ? B<uint8_t>(c, B_MASK) : nullptr, B<float2>(c, B_G),
                        reinterpret_cast<float2 *>(d_ri), s);
@@ -916,10 +937,19 @@ int max_angles() { return kMaxAngles; }
 
 // Host-buffer reconstruction.  bpc: bytes per hologram value, 4 (float) or 1 / 2 (integer
 // camera counts, uploaded as they are and widened to float on the copy stream).
-static ctdm_status reconstruct_host(ctdm_ctx *c, const ctdm_params *p, int A, const void *h_holo, const void *h_bg,
-                                    int bpc, const float *h_angx, const float *h_angy, ctdm_cfloat *h_ri)
+// Host-buffer call, enqueued only: the backgrounds, then the holograms in chunks of
+// angles go up on the copy stream (the front end of a chunk runs while the later chunks
+// are in flight), the pipeline runs on the legacy default stream and the volume comes
+// back on the download stream.  Consecutive calls overlap: a call's uploads wait only
+// until the previous call's front end has read the input buffers (so they run beside
+// its loop), and its final pass waits for the previous call's download (which runs
+// beside this call's front end).  With pageable host buffers the copies are staged by
+// the driver and the overlap is lost, the result is the same.
+static ctdm_status submit_host(ctdm_ctx *c, const ctdm_params *p, int A, const void *h_holo, const void *h_bg, int bpc,
+                               const float *h_angx, const float *h_angy, ctdm_cfloat *h_ri)
 {
     if (!c || !p || !h_holo || !h_bg || !h_ri) return invalid("ctdm_reconstruct: NULL argument");
+    if (bpc != 1 && bpc != 2 && bpc != 4) return invalid("ctdm_submit: bytes per count must be 1, 2 or 4");
     int M;
     ctdm_status st = validate(p, A, M);
     if (st != CTDM_OK) return st;
@@ -934,9 +964,6 @@ static ctdm_status reconstruct_host(ctdm_ctx *c, const ctdm_params *p, int A, co
         CK(ensure(c, B_STAGE, (size_t)bpc * A * nn), "alloc hologram staging");
         CK(ensure(c, B_STAGEBG, (size_t)bpc * nbg * nn), "alloc background staging");
     }
-    // the backgrounds first, then the holograms in chunks of angles on the copy stream:
-    // the front end of a chunk (QPI, unwrapping, spectra) runs while the later chunks are
-    // still in flight over the host link
     auto upload = [&](void *dst_stage, float *dst, const void *src, long count) -> cudaError_t {
         if (!counts) return cudaMemcpyAsync(dst, src, sizeof(float) * count, cudaMemcpyHostToDevice, c->copy);
         cudaError_t e = cudaMemcpyAsync(dst_stage, src, (size_t)bpc * count, cudaMemcpyHostToDevice, c->copy);
@@ -947,8 +974,9 @@ static ctdm_status reconstruct_host(ctdm_ctx *c, const ctdm_params *p, int A, co
     // 2.5x slower front ends); the first chunk's upload is the one not overlapped
     const int per = std::max(32, (A + ctdm_ctx::kChunks - 1) / ctdm_ctx::kChunks);
     const int nchunks = (A + per - 1) / per;
-    CK(cudaEventRecord(c->ready[ctdm_ctx::kChunks], s), "copy start");
-    CK(cudaStreamWaitEvent(c->copy, c->ready[ctdm_ctx::kChunks], 0), "copy start");
+    // the staging and input buffers: free once every earlier call's front end has read
+    // them (a device-buffer or stage call in between ran on the default stream too)
+    CK(cudaStreamWaitEvent(c->copy, c->inputs_free, 0), "copy start");
     CK(upload(c->buf[B_STAGEBG], B<float>(c, B_BG), h_bg, nbg * nn), "upload background");
     CK(cudaEventRecord(c->ready[ctdm_ctx::kChunks], c->copy), "background uploaded");
     const char *hsrc = static_cast<const char *>(h_holo);
@@ -961,21 +989,58 @@ static ctdm_status reconstruct_host(ctdm_ctx *c, const ctdm_params *p, int A, co
         CK(cudaEventRecord(c->ready[k], c->copy), "holograms uploaded");
     }
     CK(cudaStreamWaitEvent(s, c->ready[ctdm_ctx::kChunks], 0), "wait for the background");
-    const ChunkFeed feed = {c->ready, per};
+    const ChunkFeed feed = {c->ready, per, c->inputs_free, c->vol_free};
     st = reconstruct_core(c, p, A, M, B<float>(c, B_HOLO), B<float>(c, B_BG), h_angx, h_angy, B<ctdm_cfloat>(c, B_RI),
                           s, &feed);
     if (st != CTDM_OK) return st;
-    CK(cudaMemcpyAsync(h_ri, c->buf[B_RI], sizeof(float2) * r3, cudaMemcpyDeviceToHost, s), "download volume");
-    int derr = 0;
-    CK(cudaMemcpyAsync(&derr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, s), "device status");
-    CK(cudaStreamSynchronize(s), "synchronise");
+    CK(cudaEventRecord(c->vol_ready, s), "volume ready");
+    CK(cudaStreamWaitEvent(c->d2h, c->vol_ready, 0), "volume ready");
+    CK(cudaMemcpyAsync(h_ri, c->buf[B_RI], sizeof(float2) * r3, cudaMemcpyDeviceToHost, c->d2h), "download volume");
+    CK(cudaMemcpyAsync(&c->pin->derr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->d2h), "device status");
+    CK(cudaEventRecord(c->vol_free, c->d2h), "volume downloaded");
+    c->in_flight++;
+    g_err.clear();
+    return CTDM_OK;
+}
+
+// Waits for every submitted call; reports a bounded device-side wait that ran out in
+// any of them.
+static ctdm_status wait_host(ctdm_ctx *c)
+{
+    if (!c) return invalid("ctdm_wait: NULL context");
+    CK(cudaSetDevice(c->device), "cudaSetDevice");
+    if (c->in_flight == 0) return CTDM_OK;
+    CK(cudaStreamSynchronize(c->d2h), "synchronise");
+    CK(cudaStreamSynchronize(0), "synchronise");
+    c->in_flight = 0;
+    const int derr = c->pin->derr;
     if (derr != 0) {
+        c->pin->derr = 0;
         cudaMemset(c->d_err, 0, sizeof(int));
         g_err = "a bounded device-side wait ran out (code " + std::to_string(derr) + ")";
         return CTDM_ERR_TIMEOUT;
     }
     g_err.clear();
     return CTDM_OK;
+}
+
+static ctdm_status reconstruct_host(ctdm_ctx *c, const ctdm_params *p, int A, const void *h_holo, const void *h_bg,
+                                    int bpc, const float *h_angx, const float *h_angy, ctdm_cfloat *h_ri)
+{
+    ctdm_status st = submit_host(c, p, A, h_holo, h_bg, bpc, h_angx, h_angy, h_ri);
+    if (st != CTDM_OK) return st;
+    return wait_host(c);
+}
+
+extern "C" ctdm_status ctdm_submit(ctdm_ctx *c, const ctdm_params *p, int A, const void *h_holo, const void *h_bg,
+                                   int bytes_per_count, const float *h_angx, const float *h_angy, ctdm_cfloat *h_ri)
+{
+    return submit_host(c, p, A, h_holo, h_bg, bytes_per_count, h_angx, h_angy, h_ri);
+}
+
+extern "C" ctdm_status ctdm_wait(ctdm_ctx *c)
+{
+    return wait_host(c);
 }
 
 extern "C" ctdm_status ctdm_reconstruct(ctdm_ctx *c, const ctdm_params *p, int A, const float *h_holo,
@@ -1381,6 +1446,7 @@ extern "C" void extractQPI_AlgorithmB(float *SP, float *BG, ctdm_cfloat *cuSP_FF
     }
     const int N = Nx, M = N / 4;
     const long nn = (long)N * N;
+    if (wait_host(c) != CTDM_OK) return;   // host-buffer calls in flight still own B_HOLO / B_BG
     if (ensure(c, B_HOLO, sizeof(float) * nn) != cudaSuccess || ensure(c, B_BG, sizeof(float) * nn) != cudaSuccess ||
         ensure(c, B_T1, sizeof(float2) * M * M) != cudaSuccess || ensure(c, B_QMAG, sizeof(float) * M * N) != cudaSuccess ||
         ensure(c, B_CARRIER, sizeof(int) * 3) != cudaSuccess) {

@@ -124,7 +124,7 @@ CTDM_API unsigned long long ctdm_launch_count(void);
 CTDM_API ctdm_status ctdm_reconstruct_device(ctdm_ctx *ctx, const ctdm_params *p, int n_angles, const float *d_holo,
                                     const float *d_bg, const float *h_angx, const float *h_angy,
                                     ctdm_cfloat *d_ri, void *stream);
-/* Same with host buffers: copies in, reconstructs, copies the volume out, syncs.  The
+/* Same with host buffers: copies in, reconstructs, copies the volume out, waits.  The
  * holograms go over the host link in chunks of angles while the front end of the
  * earlier chunks runs; pinned host memory lets the copies overlap. */
 CTDM_API ctdm_status ctdm_reconstruct(ctdm_ctx *ctx, const ctdm_params *p, int n_angles, const float *h_holo,
@@ -138,6 +138,19 @@ CTDM_API ctdm_status ctdm_reconstruct_u16(ctdm_ctx *ctx, const ctdm_params *p, i
 CTDM_API ctdm_status ctdm_reconstruct_u8(ctdm_ctx *ctx, const ctdm_params *p, int n_angles, const uint8_t *h_holo,
                                          const uint8_t *h_bg, const float *h_angx, const float *h_angy,
                                          ctdm_cfloat *h_ri);
+/* The host-buffer call without the wait, for a stream of tomograms (no reference
+ * counterpart): enqueues the reconstruction and returns.  bytes_per_count: 4 (float),
+ * 2 (uint16) or 1 (uint8) per hologram pixel.  The host buffers must stay valid, and
+ * h_ri unread, until ctdm_wait returns.  Calls in flight overlap: a call's uploads run
+ * beside the previous call's loop once that call's front end has read the inputs, and
+ * its volume download beside the next call's front end; with pageable buffers the copies
+ * do not overlap, the results are the same.  ctdm_reconstruct* is ctdm_submit + ctdm_wait. */
+CTDM_API ctdm_status ctdm_submit(ctdm_ctx *ctx, const ctdm_params *p, int n_angles, const void *h_holo,
+                                 const void *h_bg, int bytes_per_count, const float *h_angx, const float *h_angy,
+                                 ctdm_cfloat *h_ri);
+/* Waits for every call submitted on ctx; CTDM_ERR_TIMEOUT when a bounded device-side
+ * wait ran out in any of them. */
+CTDM_API ctdm_status ctdm_wait(ctdm_ctx *ctx);
 
 /* --- batched reconstruction (no reference counterpart) ----------------------------
  * Many independent tomograms, each with its own sizes and angle count, scheduled over

@@ -42,3 +42,35 @@ def test_integer_counts_equal_float_path(ctx, dev, kind):
     want = ctx.reconstruct(p, holo.astype(np.float32), bg.astype(np.float32), acq.ang_x, acq.ang_y)
     got = ctx.reconstruct(p, holo, bg, acq.ang_x, acq.ang_y)
     assert np.array_equal(got, want)
+
+
+def test_submitted_calls_overlap_and_match(ctx, dev):
+    """ctdm_submit: three different tomograms in flight at once (pinned buffers, so each
+    call's uploads run beside the previous call's loop and its download beside the next
+    call's front end) give the synchronous call's volumes bit for bit, in any order and
+    with pageable buffers too."""
+    import torch
+    import ctdm_gb300 as C
+    from ctdm_gb300 import phantom
+    acqs = [phantom.acquisition(128, 64, 70, seed=31 + k, pixel=0.2e-6, photons=1e4) for k in range(3)]
+    ps = [C.params_for(a, 3, run_goldstein=k % 2) for k, a in enumerate(acqs)]
+    r = acqs[0].r_vol
+    want = [ctx.reconstruct(p, a.holograms.astype(np.uint16), a.background.astype(np.uint16), a.ang_x, a.ang_y)
+            for p, a in zip(ps, acqs)]
+    pinned = [(torch.from_numpy(a.holograms.astype(np.uint16)).pin_memory(),
+               torch.from_numpy(a.background.astype(np.uint16)).pin_memory()) for a in acqs]
+    for order in ([0, 1, 2], [2, 0, 1, 0]):
+        outs = [torch.empty((r, r, r), dtype=torch.complex64).pin_memory() for _ in order]
+        for o, k in zip(outs, order):
+            ctx.submit(ps[k], pinned[k][0], pinned[k][1], acqs[k].ang_x, acqs[k].ang_y, o)
+        ctx.wait()
+        for o, k in zip(outs, order):
+            assert np.array_equal(o.numpy(), want[k]), (order, k)
+    outs = [np.empty((r, r, r), np.complex64) for _ in range(2)]
+    hs = [(a.holograms.astype(np.uint16), a.background.astype(np.uint16)) for a in acqs[:2]]
+    for k in range(2):
+        ctx.submit(ps[k], hs[k][0], hs[k][1], acqs[k].ang_x, acqs[k].ang_y, outs[k])
+    ctx.wait()
+    for k in range(2):
+        assert np.array_equal(outs[k], want[k])
+    ctx.wait()   # nothing in flight: returns at once
