@@ -67,18 +67,11 @@ cudaError_t loop_pass_variant(int kind, int variant, const LoopArgs &a, int flag
 
 static PlanChoice choice_of(int R);
 
-int loop_ztile(int R)
+// Lines per packed z-pass tile of variant v at side R (0: that plan reads F2 densely).
+static int ztile_of(int R, int v)
 {
     const char *env = std::getenv("CTDM_PACKED_Z");
     if (env && std::strcmp(env, "0") == 0) return 0;
-    int v = 0;
-    {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        std::lock_guard<std::mutex> lk(g_tune_mu);
-        auto it = g_choice.find({dev, R});
-        if (it != g_choice.end()) v = it->second.v[2];
-    }
     switch (R) {
     case 32: return loop_ztile_32(v);
     case 64: return loop_ztile_64(v);
@@ -89,6 +82,19 @@ int loop_ztile(int R)
     case 768: return loop_ztile_768(v);
     default: return 0;
     }
+}
+
+int loop_ztile(int R)
+{
+    int v = 0;
+    {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_choice.find({dev, R});
+        if (it != g_choice.end()) v = it->second.v[2];
+    }
+    return ztile_of(R, v);
 }
 
 static PlanChoice choice_of(int R)
@@ -197,7 +203,23 @@ cudaError_t autotune_loop(int R, int check_mode, int *chosen, double *ms_out, in
     if (e == cudaSuccess) e = cudaMalloc(&F2, sizeof(float2) * r3);
     if (e == cudaSuccess && check_mode) e = cudaMalloc(&mask, r3);
     if (e == cudaSuccess) e = cudaMalloc(&err, sizeof(int));
+    // packed z passes are timed as the loop runs them, on empty tiles (no measured
+    // samples: the same transforms, loads and stores, none of the few value loads)
+    int tbmin = 0;
+    for (int v = 0; v < nv; v++) {
+        const int tb = ztile_of(R, v);
+        if (tb > 0 && (tbmin == 0 || tb < tbmin)) tbmin = tb;
+    }
+    uint32_t *tmask = nullptr;
+    int *tcount = nullptr, *tprefix = nullptr;
+    const size_t tiles = tbmin ? (size_t)R * R / tbmin : 0;
+    if (e == cudaSuccess && tiles) e = cudaMalloc(&tmask, sizeof(uint32_t) * tiles * R);
+    if (e == cudaSuccess && tiles) e = cudaMalloc(&tcount, sizeof(int) * tiles);
+    if (e == cudaSuccess && tiles) e = cudaMalloc(&tprefix, sizeof(int) * tiles * R);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    if (e == cudaSuccess && tiles) e = cudaMemsetAsync(tmask, 0, sizeof(uint32_t) * tiles * R, s);
+    if (e == cudaSuccess && tiles) e = cudaMemsetAsync(tcount, 0, sizeof(int) * tiles, s);
+    if (e == cudaSuccess && tiles) e = cudaMemsetAsync(tprefix, 0, sizeof(int) * tiles * R, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(G, 0, sizeof(float2) * r3, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(F2, 0, sizeof(float2) * r3, s);
     if (e == cudaSuccess && mask) e = cudaMemsetAsync(mask, 0, r3, s);
@@ -218,12 +240,22 @@ cudaError_t autotune_loop(int R, int check_mode, int *chosen, double *ms_out, in
         a.s1 = (float)(-1.0 / ((double)r3 * k2));
         a.s2 = (float)(-k2 / (nm * nm));
         a.err = err;
+        a.tmask = tmask;
+        a.tcount = tcount;
+        a.tprefix = tprefix;
+        a.tvals = G;   // never read: every tile is empty
+        // the z pass of variant v as the loop would run it
+        auto zargs = [&](int v) {
+            LoopArgs z = a;
+            z.packed = tiles && ztile_of(R, v) > 0 ? 1 : 0;
+            return z;
+        };
         const int kinds[3] = {LOOP_X, LOOP_Y_FWD, LOOP_Z};
         for (int p = 0; p < 3 && e == cudaSuccess; p++) {
             double best = 1e30;
             for (int v = 0; v < nv && e == cudaSuccess; v++) {
                 double ms = 0;
-                e = time_variant(kinds[p], v, a, check_mode, s, 5, ms);
+                e = time_variant(kinds[p], v, kinds[p] == LOOP_Z ? zargs(v) : a, check_mode, s, 5, ms);
                 if (ms_out && p * 3 + v < n_ms) ms_out[p * 3 + v] = ms;
                 if (e == cudaSuccess && ms < best) {
                     best = ms;
@@ -244,11 +276,11 @@ cudaError_t autotune_loop(int R, int check_mode, int *chosen, double *ms_out, in
                     if (sc == 0) {
                         e = loop_pass_variant(LOOP_X, pc.v[0], a, 0, s);
                         if (e == cudaSuccess) e = loop_pass_variant(LOOP_Y_FWD, pc.v[1], a, 0, s);
-                        if (e == cudaSuccess) e = loop_pass_variant(LOOP_Z, pc.v[2], a, check_mode, s);
+                        if (e == cudaSuccess) e = loop_pass_variant(LOOP_Z, pc.v[2], zargs(pc.v[2]), check_mode, s);
                         if (e == cudaSuccess) e = loop_pass_variant(LOOP_Y_INV, pc.v[1], a, 0, s);
                     } else {
                         e = plane_variant(a, false, sc, s);
-                        if (e == cudaSuccess) e = loop_pass_variant(LOOP_Z, pc.v[2], a, check_mode, s);
+                        if (e == cudaSuccess) e = loop_pass_variant(LOOP_Z, pc.v[2], zargs(pc.v[2]), check_mode, s);
                     }
                     cudaEventRecord(e1, s);
                     if (e == cudaSuccess) e = cudaEventSynchronize(e1);
@@ -272,6 +304,9 @@ cudaError_t autotune_loop(int R, int check_mode, int *chosen, double *ms_out, in
     cudaFree(F2);
     cudaFree(mask);
     cudaFree(err);
+    cudaFree(tmask);
+    cudaFree(tcount);
+    cudaFree(tprefix);
     if (e != cudaSuccess) return e;
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
