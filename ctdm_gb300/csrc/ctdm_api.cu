@@ -281,6 +281,8 @@ struct ChunkFeed {
     int per;
     cudaEvent_t inputs_free;   // recorded once the front end has read the inputs
     cudaEvent_t out_free;      // the output volume may be written after it
+    const void *counts;        // QPI Algorithm A reads the holograms from here when set:
+    int bpc;                   // camera counts of bpc bytes, as uploaded
 };
 
 static cudaError_t ensure(ctdm_ctx *c, int id, size_t bytes)
@@ -548,7 +550,8 @@ static ctdm_status qpi_setup(ctdm_ctx *c, int N, int M, int A, const float *bg, 
     CK(ensure(c, B_BGF, sizeof(float2) * nbg * mm), "alloc BG field");
     for (long a0 = 0; a0 < nbg; a0 += chunk) {
         const int ac = (int)std::min<long>(chunk, nbg - a0);
-        CK(qpi_forward_window(bg + a0 * nn, ac, N, M, car, B<float2>(c, B_T1), B<float2>(c, B_S), s), "qpi bg fwd");
+        CK(qpi_forward_window(bg + a0 * nn, 4, ac, N, M, car, B<float2>(c, B_T1), B<float2>(c, B_S), s),
+           "qpi bg fwd");
         CK(qpi_inverse_window(B<float2>(c, B_S), ac, M, B<float2>(c, B_BGF) + a0 * mm, nullptr, 0, nullptr, nullptr,
                               s),
            "qpi bg inv");
@@ -558,7 +561,8 @@ static ctdm_status qpi_setup(ctdm_ctx *c, int N, int M, int A, const float *bg, 
 
 // Second part: phase and amplitude of angles [first, first + count) (holo: the whole
 // stack; the background fields of qpi_setup).
-static ctdm_status qpi_angles(ctdm_ctx *c, int N, int M, int A, int first, int count, const float *holo,
+// holo: the stack, bpc bytes per pixel (4 float, 2 / 1 camera counts)
+static ctdm_status qpi_angles(ctdm_ctx *c, int N, int M, int A, int first, int count, const void *holo, int bpc,
                               int bg_per_angle, float *phase, float *amp, cudaStream_t s)
 {
     const long chunk = qpi_chunk(N, M, A);
@@ -566,7 +570,9 @@ static ctdm_status qpi_angles(ctdm_ctx *c, int N, int M, int A, int first, int c
     const int *car = B<int>(c, B_CARRIER);
     for (long a0 = first; a0 < first + count; a0 += chunk) {
         const int ac = (int)std::min<long>(chunk, first + count - a0);
-        CK(qpi_forward_window(holo + a0 * nn, ac, N, M, car, B<float2>(c, B_T1), B<float2>(c, B_S), s), "qpi fwd");
+        CK(qpi_forward_window(static_cast<const char *>(holo) + (size_t)bpc * a0 * nn, bpc, ac, N, M, car,
+                              B<float2>(c, B_T1), B<float2>(c, B_S), s),
+           "qpi fwd");
         const float2 *bgf = B<float2>(c, B_BGF) + (bg_per_angle ? a0 * mm : 0);
         CK(qpi_inverse_window(B<float2>(c, B_S), ac, M, nullptr, bgf, bg_per_angle ? mm : 0, phase + a0 * mm,
                               amp + a0 * mm, s),
@@ -580,7 +586,7 @@ static ctdm_status do_qpi(ctdm_ctx *c, int N, int M, int A, const float *holo, c
 {
     ctdm_status st = qpi_setup(c, N, M, A, bg, bg_per_angle, carrier_in, s);
     if (st != CTDM_OK) return st;
-    return qpi_angles(c, N, M, A, 0, A, holo, bg_per_angle, phase, amp, s);
+    return qpi_angles(c, N, M, A, 0, A, holo, 4, bg_per_angle, phase, amp, s);
 }
 
 static ctdm_status do_positivity(ctdm_ctx *c, int R, int iters, int check_mode, double k2, double n_med,
@@ -811,7 +817,9 @@ static ctdm_status pipeline_core(ctdm_ctx *c, const ctdm_params *p, int A, int M
         float *phase = B<float>(c, B_PHASE) + o;
         if (!alg_b) {
             if (feed) CK(cudaStreamWaitEvent(s, feed->ready[k], 0), "wait for holograms");
-            st = qpi_angles(c, N, M, A, a0, ac, d_holo, p->bg_per_angle, B<float>(c, B_PHASE), B<float>(c, B_AMP),
+            const bool cnt = feed && feed->counts;
+            st = qpi_angles(c, N, M, A, a0, ac, cnt ? feed->counts : d_holo, cnt ? feed->bpc : 4, p->bg_per_angle,
+                            B<float>(c, B_PHASE), B<float>(c, B_AMP),
                             s);
             if (st != CTDM_OK) return st;
             tm.mark(S_QPI, s);
@@ -956,18 +964,21 @@ static ctdm_status submit_host(ctdm_ctx *c, const ctdm_params *p, int A, const v
     CK(cudaSetDevice(c->device), "cudaSetDevice");
     const long nn = (long)p->n_holo * p->n_holo, r3 = (long)p->r_vol * p->r_vol * p->r_vol;
     const int nbg = p->bg_per_angle ? A : 1;
-    CK(ensure(c, B_HOLO, sizeof(float) * A * nn), "alloc holograms");
+    const bool counts = bpc != 4;
+    // QPI Algorithm A reads camera counts as they were uploaded; Algorithm B and the
+    // background path take floats, widened on the copy stream
+    const bool direct = counts && p->qpi_method == CTDM_QPI_A;
+    if (!direct) CK(ensure(c, B_HOLO, sizeof(float) * A * nn), "alloc holograms");
     CK(ensure(c, B_BG, sizeof(float) * nbg * nn), "alloc background");
     CK(ensure(c, B_RI, sizeof(float2) * r3), "alloc volume");
-    const bool counts = bpc != 4;
     if (counts) {
         CK(ensure(c, B_STAGE, (size_t)bpc * A * nn), "alloc hologram staging");
         CK(ensure(c, B_STAGEBG, (size_t)bpc * nbg * nn), "alloc background staging");
     }
-    auto upload = [&](void *dst_stage, float *dst, const void *src, long count) -> cudaError_t {
+    auto upload = [&](void *dst_stage, float *dst, const void *src, long count, bool widen) -> cudaError_t {
         if (!counts) return cudaMemcpyAsync(dst, src, sizeof(float) * count, cudaMemcpyHostToDevice, c->copy);
         cudaError_t e = cudaMemcpyAsync(dst_stage, src, (size_t)bpc * count, cudaMemcpyHostToDevice, c->copy);
-        return e == cudaSuccess ? widen_counts(dst_stage, bpc, count, dst, c->copy) : e;
+        return e == cudaSuccess && widen ? widen_counts(dst_stage, bpc, count, dst, c->copy) : e;
     };
     cudaStream_t s = 0;
     // chunks of at least 32 angles keep each stage's grid full (8-angle chunks measured
@@ -977,19 +988,19 @@ static ctdm_status submit_host(ctdm_ctx *c, const ctdm_params *p, int A, const v
     // the staging and input buffers: free once every earlier call's front end has read
     // them (a device-buffer or stage call in between ran on the default stream too)
     CK(cudaStreamWaitEvent(c->copy, c->inputs_free, 0), "copy start");
-    CK(upload(c->buf[B_STAGEBG], B<float>(c, B_BG), h_bg, nbg * nn), "upload background");
+    CK(upload(c->buf[B_STAGEBG], B<float>(c, B_BG), h_bg, nbg * nn, true), "upload background");
     CK(cudaEventRecord(c->ready[ctdm_ctx::kChunks], c->copy), "background uploaded");
     const char *hsrc = static_cast<const char *>(h_holo);
     char *stage = static_cast<char *>(c->buf[B_STAGE]);
     for (int k = 0; k < nchunks; k++) {
         const long a0 = (long)k * per, ac = std::min<long>(per, A - a0);
-        CK(upload(counts ? stage + (size_t)bpc * a0 * nn : nullptr, B<float>(c, B_HOLO) + a0 * nn,
-                  hsrc + (size_t)bpc * a0 * nn, ac * nn),
+        CK(upload(counts ? stage + (size_t)bpc * a0 * nn : nullptr, direct ? nullptr : B<float>(c, B_HOLO) + a0 * nn,
+                  hsrc + (size_t)bpc * a0 * nn, ac * nn, !direct),
            "upload holograms");
         CK(cudaEventRecord(c->ready[k], c->copy), "holograms uploaded");
     }
     CK(cudaStreamWaitEvent(s, c->ready[ctdm_ctx::kChunks], 0), "wait for the background");
-    const ChunkFeed feed = {c->ready, per, c->inputs_free, c->vol_free};
+    const ChunkFeed feed = {c->ready, per, c->inputs_free, c->vol_free, direct ? c->buf[B_STAGE] : nullptr, bpc};
     st = reconstruct_core(c, p, A, M, B<float>(c, B_HOLO), B<float>(c, B_BG), h_angx, h_angy, B<ctdm_cfloat>(c, B_RI),
                           s, &feed);
     if (st != CTDM_OK) return st;

@@ -99,8 +99,10 @@ template <> struct QRows<512> : fftl::PlanT<512, 8, 32, fftl::Radices<8, 8, 8>, 
 template <> struct QRows<1024> : fftl::PlanT<1024, 4, 64, fftl::Radices<16, 16, 4>, fftl::Radices<4, 16, 16>> {};
 template <> struct QRows<2048> : fftl::PlanT<2048, 2, 128, fftl::Radices<16, 16, 8>, fftl::Radices<8, 16, 16>> {};
 
-template <int N>
-__global__ void __launch_bounds__(QRows<N>::THREADS) qpi_rows_kernel(const float *__restrict__ holo, float2 *T1,
+// Holograms arrive as float or as 16- / 8-bit camera counts (read as they are and
+// converted on load, exact: every count is an integer below 2^24).
+template <int N, class T>
+__global__ void __launch_bounds__(QRows<N>::THREADS) qpi_rows_kernel(const T *__restrict__ holo, float2 *T1,
                                                                     const int *__restrict__ carrier, long npairs,
                                                                     int M, const float2 *__restrict__ tw)
 {
@@ -111,12 +113,12 @@ __global__ void __launch_bounds__(QRows<N>::THREADS) qpi_rows_kernel(const float
     const int t = threadIdx.x % P::T, b = threadIdx.x / P::T;
     const long q = (long)blockIdx.x * P::B + b;   // pair q covers rows 2q, 2q+1 of the stack
     const bool ok = q < npairs;
-    const float *r0 = holo + (ok ? 2 * q : 0) * N;
+    const T *r0 = holo + (ok ? 2 * q : 0) * N;
     float2 v[P::E];
 #pragma unroll
     for (int i = 0; i < P::E; i++) {
         const int p = fftl::slot_pos<N, P::T, P::F0>(i, t);
-        v[i] = ok ? make_float2(__ldcs(&r0[p]), __ldcs(&r0[N + p])) : make_float2(0.f, 0.f);
+        v[i] = ok ? make_float2((float)__ldcs(&r0[p]), (float)__ldcs(&r0[N + p])) : make_float2(0.f, 0.f);
     }
     P::template seq_row<false>(buf, v, tw);
     float2 *line = buf + b * Y::LINE;
@@ -234,19 +236,28 @@ __global__ void __launch_bounds__(Plan<M>::THREADS) qpi_final_kernel(const float
     }
 }
 
-template <int N>
-static cudaError_t qpi_fwd_launch(const float *holo, int A, int M, const int *carrier, float2 *T1, float2 *S,
-                                  cudaStream_t s)
+template <int N, class T>
+static cudaError_t qpi_rows_launch(const T *holo, long npairs, int M, const int *carrier, float2 *T1, cudaStream_t s)
 {
     using PR = QRows<N>;
     const size_t smem_r = fftl::plan_smem_row<PR>();
-    const long npairs = (long)A * N / 2;
-    cudaError_t e = set_smem<N>(qpi_rows_kernel<N>, smem_r);
+    cudaError_t e = set_smem<N>(qpi_rows_kernel<N, T>, smem_r);
     if (e != cudaSuccess) return e;
-    qpi_rows_kernel<N><<<(unsigned)((npairs + PR::B - 1) / PR::B), PR::THREADS, smem_r, s>>>(holo, T1, carrier, npairs,
-                                                                                           M, twiddles(N));
+    qpi_rows_kernel<N, T><<<(unsigned)((npairs + PR::B - 1) / PR::B), PR::THREADS, smem_r, s>>>(holo, T1, carrier,
+                                                                                              npairs, M, twiddles(N));
     note_launch();
-    e = cudaGetLastError();
+    return cudaGetLastError();
+}
+
+template <int N>
+static cudaError_t qpi_fwd_launch(const void *holo, int bpc, int A, int M, const int *carrier, float2 *T1, float2 *S,
+                                  cudaStream_t s)
+{
+    const long npairs = (long)A * N / 2;
+    cudaError_t e;
+    if (bpc == 2) e = qpi_rows_launch<N>(static_cast<const uint16_t *>(holo), npairs, M, carrier, T1, s);
+    else if (bpc == 1) e = qpi_rows_launch<N>(static_cast<const uint8_t *>(holo), npairs, M, carrier, T1, s);
+    else e = qpi_rows_launch<N>(static_cast<const float *>(holo), npairs, M, carrier, T1, s);
     if (e != cudaSuccess) return e;
     using PC = QCols<N>;
     const long nl = (long)A * M;
@@ -274,10 +285,10 @@ static cudaError_t qpi_inv_launch(float2 *S, int A, float2 *field_out, const flo
     return cudaGetLastError();
 }
 
-cudaError_t qpi_forward_window(const float *holo, int A, int N, int M, const int *carrier, float2 *T1, float2 *S,
-                               cudaStream_t s)
+cudaError_t qpi_forward_window(const void *holo, int bpc, int A, int N, int M, const int *carrier, float2 *T1,
+                               float2 *S, cudaStream_t s)
 {
-    CTDM_DISPATCH_L(N, qpi_fwd_launch, holo, A, M, carrier, T1, S, s)
+    CTDM_DISPATCH_L(N, qpi_fwd_launch, holo, bpc, A, M, carrier, T1, S, s)
 }
 
 cudaError_t qpi_inverse_window(float2 *S, int A, int M, float2 *field_out, const float2 *bgf, long bg_stride,

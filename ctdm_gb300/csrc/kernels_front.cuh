@@ -11,8 +11,9 @@ cudaError_t qpi_find_carrier(const float *bg, int N, float2 *scratch, unsigned l
                              cudaStream_t s);
 // Pruned forward transform of A holograms into their M x M window spectra S
 // (ifftshifted, masked).  T1: A*N*M complex scratch.
-cudaError_t qpi_forward_window(const float *holo, int A, int N, int M, const int *carrier, float2 *T1, float2 *S,
-                               cudaStream_t s);
+// holo: A holograms of N x N pixels, bpc bytes each (4 float, 2 uint16, 1 uint8 counts)
+cudaError_t qpi_forward_window(const void *holo, int bpc, int A, int N, int M, const int *carrier, float2 *T1,
+                               float2 *S, cudaStream_t s);
 // Inverse M x M transform of S (destroyed) and the epilogue: field_out != NULL
 // stores the complex field, otherwise phase/amp against bgf[a * bg_stride].
 cudaError_t qpi_inverse_window(float2 *S, int A, int M, float2 *field_out, const float2 *bgf, long bg_stride,
