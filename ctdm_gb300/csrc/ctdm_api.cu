@@ -197,7 +197,7 @@ const float *dct_eigen(int M)
 enum BufId {
     B_PHASE, B_AMP, B_PHU, B_CHG, B_CUT, B_GOLD, B_U, B_F2, B_COUNTS, B_G, B_T1, B_S, B_BGF, B_DCT, B_MASK, B_GEOM,
     B_CARRIER, B_KEY, B_SCRATCH, B_HOLO, B_BG, B_RI, B_GSTATE, B_GLIST, B_GSTATUS, B_FASTW, B_FASTIN, B_TMP, B_GWORK,
-    B_TMASK, B_TCOUNT, B_TVALS, B_QMAG, B_FIT, B_PV, B_PG, B_PV2, B_PG2, B_PVP, B_PPART, B_PCTL, B_PHIST, B_STAGE, B_STAGEBG, B_TPRE, NBUF
+    B_TMASK, B_TCOUNT, B_TVALS, B_QMAG, B_FIT, B_PV, B_PG, B_PV2, B_PG2, B_PVP, B_PPART, B_PCTL, B_PHIST, B_STAGE, B_STAGEBG, B_TPRE, B_RI2, NBUF
 };
 
 // Stage boundaries recorded with CUDA events when timing is enabled.
@@ -264,11 +264,20 @@ struct ctdm_ctx {
     cudaStream_t copy = nullptr;
     cudaEvent_t ready[kChunks + 1] = {};
     // host-buffer calls in flight (ctdm_submit): the input buffers are free again once
-    // a call's front end has read them (inputs_free), the volume is downloaded on its own
-    // stream after vol_ready and may be overwritten after vol_free
+    // a call's front end has read them (inputs_free).  Consecutive calls write their
+    // volumes into alternating buffers (slot 0: B_RI, 1: B_RI2); a call's volume is
+    // downloaded on its own stream once the next call's front end is done (front_done),
+    // so that the download runs beside that call's loop rather than its front end, and
+    // a slot is written again after vol_free[slot].
     cudaStream_t d2h = nullptr;
-    cudaEvent_t inputs_free = nullptr, vol_ready = nullptr, vol_free = nullptr;
-    int in_flight = 0;
+    cudaEvent_t inputs_free = nullptr, front_done = nullptr, vol_ready[2] = {}, vol_free[2] = {};
+    struct Download {
+        ctdm_cfloat *host = nullptr;
+        size_t bytes = 0;
+        int slot = 0;
+        bool pending = false;
+    } dl;
+    int slot = 0, in_flight = 0;
     // device status word (bounded device-side waits record a code here)
     int *d_err = nullptr;
 };
@@ -281,6 +290,7 @@ struct ChunkFeed {
     int per;
     cudaEvent_t inputs_free;   // recorded once the front end has read the inputs
     cudaEvent_t out_free;      // the output volume may be written after it
+    cudaEvent_t front_done;    // recorded after the Ewald mapping
     const void *counts;        // QPI Algorithm A reads the holograms from here when set:
     int bpc;                   // camera counts of bpc bytes, as uploaded
 };
@@ -335,8 +345,11 @@ extern "C" ctdm_status ctdm_ctx_create(int device, ctdm_ctx **out)
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->copy, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->d2h, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->inputs_free, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->vol_ready, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->vol_free, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->front_done, cudaEventDisableTiming);
+    for (int k = 0; k < 2 && e == cudaSuccess; k++) {
+        e = cudaEventCreateWithFlags(&c->vol_ready[k], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->vol_free[k], cudaEventDisableTiming);
+    }
     if (e == cudaSuccess) e = cudaMallocHost(&c->pin, sizeof(ctdm_ctx::Pinned));
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->geom_done, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->carrier_done, cudaEventDisableTiming);
@@ -371,7 +384,8 @@ extern "C" void ctdm_ctx_destroy(ctdm_ctx *c)
     if (c->copy) cudaStreamDestroy(c->copy);
     if (c->d2h) cudaStreamDestroy(c->d2h);
     if (c->pin) cudaFreeHost(c->pin);
-    for (cudaEvent_t e : {c->geom_done, c->carrier_done, c->inputs_free, c->vol_ready, c->vol_free})
+    for (cudaEvent_t e : {c->geom_done, c->carrier_done, c->inputs_free, c->front_done, c->vol_ready[0],
+                          c->vol_ready[1], c->vol_free[0], c->vol_free[1]})
         if (e) cudaEventDestroy(e);
     for (cudaEvent_t e : c->ready)
         if (e) cudaEventDestroy(e);
@@ -864,6 +878,7 @@ static ctdm_status pipeline_core(ctdm_ctx *c, const ctdm_params *p, int A, int M
     ea.mask = mask_mode ? B<uint8_t>(c, B_MASK) : nullptr;
     CK(launch_ewald(ea, s), "ewald mapping");
     tm.mark(S_EWALD, s);
+    if (feed && feed->front_done) CK(cudaEventRecord(feed->front_done, s), "front end done");
     if (gold_side) {
         // forked after the mapping, whose CTAs lose room on an SM to a resident fill,
         // so that it runs beside the loop passes
@@ -945,6 +960,21 @@ int max_angles() { return kMaxAngles; }
 
 // Host-buffer reconstruction.  bpc: bytes per hologram value, 4 (float) or 1 / 2 (integer
 // camera counts, uploaded as they are and widened to float on the copy stream).
+// The pending volume download on the download stream (once its volume is ready and
+// after whatever that stream already waits for), then the device status word; the
+// volume's slot is free again at vol_free.
+static cudaError_t start_download(ctdm_ctx *c)
+{
+    ctdm_ctx::Download &d = c->dl;
+    cudaError_t e = cudaStreamWaitEvent(c->d2h, c->vol_ready[d.slot], 0);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d.host, c->buf[d.slot ? B_RI2 : B_RI], d.bytes, cudaMemcpyDeviceToHost, c->d2h);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&c->pin->derr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->d2h);
+    if (e == cudaSuccess) e = cudaEventRecord(c->vol_free[d.slot], c->d2h);
+    d.pending = false;
+    return e;
+}
+
 // Host-buffer call, enqueued only: the backgrounds, then the holograms in chunks of
 // angles go up on the copy stream (the front end of a chunk runs while the later chunks
 // are in flight), the pipeline runs on the legacy default stream and the volume comes
@@ -968,9 +998,12 @@ static ctdm_status submit_host(ctdm_ctx *c, const ctdm_params *p, int A, const v
     // QPI Algorithm A reads camera counts as they were uploaded; Algorithm B and the
     // background path take floats, widened on the copy stream
     const bool direct = counts && p->qpi_method == CTDM_QPI_A;
+    const int slot = c->slot, vol = slot ? B_RI2 : B_RI;
+    // a volume of another size: the pending download goes first (a buffer may move)
+    if (c->dl.pending && c->dl.bytes != sizeof(float2) * r3) CK(start_download(c), "volume download");
     if (!direct) CK(ensure(c, B_HOLO, sizeof(float) * A * nn), "alloc holograms");
     CK(ensure(c, B_BG, sizeof(float) * nbg * nn), "alloc background");
-    CK(ensure(c, B_RI, sizeof(float2) * r3), "alloc volume");
+    CK(ensure(c, vol, sizeof(float2) * r3), "alloc volume");
     if (counts) {
         CK(ensure(c, B_STAGE, (size_t)bpc * A * nn), "alloc hologram staging");
         CK(ensure(c, B_STAGEBG, (size_t)bpc * nbg * nn), "alloc background staging");
@@ -982,8 +1015,10 @@ static ctdm_status submit_host(ctdm_ctx *c, const ctdm_params *p, int A, const v
     };
     cudaStream_t s = 0;
     // chunks of at least 32 angles keep each stage's grid full (8-angle chunks measured
-    // 2.5x slower front ends); the first chunk's upload is the one not overlapped
-    const int per = std::max(32, (A + ctdm_ctx::kChunks - 1) / ctdm_ctx::kChunks);
+    // 2.5x slower front ends); the first chunk's upload is the one not overlapped.  With
+    // an earlier call still in flight the uploads finish beside its loop, before this
+    // call starts, and one chunk runs the front end on full grids.
+    const int per = c->in_flight > 0 ? A : std::max(32, (A + ctdm_ctx::kChunks - 1) / ctdm_ctx::kChunks);
     const int nchunks = (A + per - 1) / per;
     // the staging and input buffers: free once every earlier call's front end has read
     // them (a device-buffer or stage call in between ran on the default stream too)
@@ -1000,15 +1035,22 @@ static ctdm_status submit_host(ctdm_ctx *c, const ctdm_params *p, int A, const v
         CK(cudaEventRecord(c->ready[k], c->copy), "holograms uploaded");
     }
     CK(cudaStreamWaitEvent(s, c->ready[ctdm_ctx::kChunks], 0), "wait for the background");
-    const ChunkFeed feed = {c->ready, per, c->inputs_free, c->vol_free, direct ? c->buf[B_STAGE] : nullptr, bpc};
-    st = reconstruct_core(c, p, A, M, B<float>(c, B_HOLO), B<float>(c, B_BG), h_angx, h_angy, B<ctdm_cfloat>(c, B_RI),
+    const ChunkFeed feed = {c->ready, per, c->inputs_free, c->vol_free[slot], c->front_done,
+                            direct ? c->buf[B_STAGE] : nullptr, bpc};
+    st = reconstruct_core(c, p, A, M, B<float>(c, B_HOLO), B<float>(c, B_BG), h_angx, h_angy, B<ctdm_cfloat>(c, vol),
                           s, &feed);
     if (st != CTDM_OK) return st;
-    CK(cudaEventRecord(c->vol_ready, s), "volume ready");
-    CK(cudaStreamWaitEvent(c->d2h, c->vol_ready, 0), "volume ready");
-    CK(cudaMemcpyAsync(h_ri, c->buf[B_RI], sizeof(float2) * r3, cudaMemcpyDeviceToHost, c->d2h), "download volume");
-    CK(cudaMemcpyAsync(&c->pin->derr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->d2h), "device status");
-    CK(cudaEventRecord(c->vol_free, c->d2h), "volume downloaded");
+    // the previous call's volume: downloaded beside this call's loop
+    if (c->dl.pending) {
+        CK(cudaStreamWaitEvent(c->d2h, c->front_done, 0), "front end done");
+        CK(start_download(c), "volume download");
+    }
+    CK(cudaEventRecord(c->vol_ready[slot], s), "volume ready");
+    c->dl.host = h_ri;
+    c->dl.bytes = sizeof(float2) * r3;
+    c->dl.slot = slot;
+    c->dl.pending = true;
+    c->slot ^= 1;
     c->in_flight++;
     g_err.clear();
     return CTDM_OK;
@@ -1021,6 +1063,7 @@ static ctdm_status wait_host(ctdm_ctx *c)
     if (!c) return invalid("ctdm_wait: NULL context");
     CK(cudaSetDevice(c->device), "cudaSetDevice");
     if (c->in_flight == 0) return CTDM_OK;
+    if (c->dl.pending) CK(start_download(c), "volume download");
     CK(cudaStreamSynchronize(c->d2h), "synchronise");
     CK(cudaStreamSynchronize(0), "synchronise");
     c->in_flight = 0;
