@@ -122,11 +122,16 @@ __global__ void __launch_bounds__(QRows<N>::THREADS) qpi_rows_kernel(const T *__
     }
     P::template seq_row<false>(buf, v, tw);
     float2 *line = buf + b * Y::LINE;
+    // park only the points the window reads: k in [k0, k0 + M) mod N and their mirrors
+    const int c = __ldg(&carrier[1]);
+    const int k0 = (c - N / 2 - M / 2 + 2 * N) & (N - 1);
 #pragma unroll
-    for (int i = 0; i < P::E; i++) line[Y::at(fftl::slot_pos<N, P::T, P::RV0>(i, t))] = v[i];
+    for (int i = 0; i < P::E; i++) {
+        const int k = fftl::slot_pos<N, P::T, P::RV0>(i, t);
+        if (((k - k0 + N) & (N - 1)) < M || ((((N - k) & (N - 1)) - k0 + N) & (N - 1)) < M) line[Y::at(k)] = v[i];
+    }
     __syncthreads();
     if (!ok) return;
-    const int c = carrier[1];
     for (int m = t; m < M; m += P::T) {
         int k = (c - N / 2 + m - M / 2) % N;
         if (k < 0) k += N;
