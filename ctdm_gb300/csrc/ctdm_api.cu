@@ -335,7 +335,7 @@ extern "C" ctdm_status ctdm_ctx_create(int device, ctdm_ctx **out)
     ctdm_ctx *c = new ctdm_ctx();
     c->device = device;
     // the side stream carries work the reconstruction does not wait for (Goldstein
-    // beside the DCT path): lowest priority, so the block scheduler serves the
+    // beside the loop passes): lowest priority, so the block scheduler serves the
     // call's stream first
     int prio_lo = 0, prio_hi = 0;
     cudaError_t e = cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
@@ -962,7 +962,8 @@ int max_angles() { return kMaxAngles; }
 }  // namespace ctdm
 
 // Host-buffer reconstruction.  bpc: bytes per hologram value, 4 (float) or 1 / 2 (integer
-// camera counts, uploaded as they are and widened to float on the copy stream).
+// camera counts, uploaded as they are: QPI Algorithm A reads them so, the background
+// and Algorithm B's holograms are widened to float on the copy stream).
 // The pending volume download on the download stream (once its volume is ready and
 // after whatever that stream already waits for), then the device status word; the
 // volume's slot is free again at vol_free.

@@ -148,8 +148,8 @@ cudaError_t resize_maps(const float *ph, const float *am, int A, int M, int N, f
 }
 
 // Camera counts (8- or 16-bit) to float, four per thread (n a multiple of 4, both
-// buffers 16-byte aligned); the host-buffer entries upload integer frames and widen
-// them here.
+// buffers 16-byte aligned): the host-buffer entries widen the backgrounds, and the
+// holograms when QPI Algorithm B reads them, here.
 template <class T>
 __global__ void __launch_bounds__(256) widen_kernel(const T *__restrict__ in, float *out, long n4)
 {
