@@ -718,7 +718,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="wrap_heavy", choices=sorted(CONFIGS))
     ap.add_argument("--loop-scheme", type=int, default=-1, choices=[-1, 0, 1, 2],
-                    help="positivity-loop scheme of the volume side (-1: the autotuner's choice)")
+                    help="positivity-loop scheme of the volume side, with plan variants 0 for its passes "
+                         "(-1: the autotuner's choice; profiles pin 1, the choice without a profiler)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
