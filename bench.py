@@ -620,7 +620,8 @@ def run_ours(args):
     del F2
     bytes_per = {"x_pass": 16 * r3, "y_forward": 16 * r3, "y_inverse": 16 * r3,
                  "z_pass": 16 * r3 + 8.0 * measured + 4 * r3 / 16, "ewald": A * 8.0 * r * r + 16 * r3}
-    kernel_of = {"x_pass": "plane_pass" if scheme in (1, 2) else "x_pass", "y_forward": "y_forward",
+    plane = {1: "plane_pass", 2: "plane_pass_4cta"}
+    kernel_of = {"x_pass": plane.get(scheme, "x_pass"), "y_forward": "y_forward",
                  "y_inverse": "y_inverse", "z_pass": "z_pass_packed", "ewald": "ewald"}
     best = max(bytes_per, key=lambda k: stages[k][0])
     ms_total, cnt = stages[best]

@@ -642,8 +642,9 @@ static ctdm_status do_positivity(ctdm_ctx *c, int R, int iters, int check_mode, 
         la.packed = 1;
     }
     StageTimer &tm = c->timer;
-    if (loop_scheme(R) == 1) {
-        // plane + z passes (the plane pass records under the x-pass stage)
+    if (loop_scheme(R) >= 1) {
+        // plane + z passes, 8- or 4-CTA clusters per plane (schemes 1, 2; the plane pass
+        // records under the x-pass stage)
         for (int it = 0; it < iters; it++) {
             CK(launch_plane(la, false, s), "plane pass");
             tm.mark(S_XPASS, s);

@@ -35,7 +35,7 @@ struct PlaneCfg {
 };
 
 // MINB: resident CTAs per SM the register allocation aims for (3: no spills at
-// R = 256; 4: more latency hiding for some spill traffic; the autotuner picks).
+// R = 256; 4: more latency hiding for some spill traffic).  C: CTAs per plane.
 template <int L, int C, int MINB, bool FINAL>
 __global__ void __launch_bounds__(fftl::Plan<L>::THREADS, MINB) plane_kernel(LoopArgs a, const float2 *__restrict__ tw)
 {
