@@ -58,8 +58,9 @@ def test_autotune_reports_all_variants(ctx):
 
 
 def test_loop_schemes_agree_at_256(ctx, dev, oracle):
-    """The plane + z scheme (cluster plane pass) and the x / y / z / y scheme give the
-    oracle's volume at 256^3, with and without the hit-mask predicate."""
+    """The plane + z schemes (8- and 4-CTA cluster plane passes) and the x / y / z / y
+    scheme give the oracle's volume at 256^3, with and without the hit-mask predicate,
+    and each scheme runs its own passes (the stage timer sees y passes only in scheme 0)."""
     import ctdm_gb300 as C
     import torch
     r, iters = 256, 3
@@ -74,8 +75,15 @@ def test_loop_schemes_agree_at_256(ctx, dev, oracle):
             ref = oracle.positivity(f2, counts, iters, K2, N_MED, mode)
             for scheme in (0, 1, 2):
                 C.set_loop_scheme(r, scheme)
+                ctx.set_timing(True)
                 ctx.positivity(d_f2, r, iters, K2, N_MED, out, check_mode=mode, counts=d_counts)
                 torch.cuda.synchronize()
+                st = ctx.stage_times()
+                ctx.set_timing(False)
+                y_launches = st["y_inverse"][1] + st["y_forward"][1]
+                assert (y_launches == 0) == (scheme >= 1), (scheme, st)
+                if scheme >= 1:
+                    assert st["x_pass"][1] == iters and st["z_pass"][1] == iters, (scheme, st)
                 g = out.cpu().numpy().astype(np.complex128)
                 err = float(np.sqrt(np.mean(np.abs(g - ref) ** 2)))
                 assert err < RI_TOL, (mode, scheme, err)
