@@ -925,7 +925,7 @@ extern "C" ctdm_status ctdm_reconstruct_device(ctdm_ctx *c, const ctdm_params *p
                                                ctdm_cfloat *d_ri, void *stream)
 {
     if (!c || !d_holo || !d_bg || !h_angx || !h_angy || !d_ri) return invalid("ctdm_reconstruct_device: NULL argument");
-    int M;
+    int M = 0;
     ctdm_status st = validate(p, A, M);
     if (st != CTDM_OK) return st;
     CK(cudaSetDevice(c->device), "cudaSetDevice");
@@ -941,7 +941,7 @@ ctdm_status validate_params(const ctdm_params *p, int A, int &M) { return valida
 ctdm_status run_pipeline(ctdm_ctx *c, const ctdm_params *p, int A, const float *d_holo, const float *d_bg,
                          const AngleGeom *d_geom, ctdm_cfloat *d_ri, cudaStream_t s)
 {
-    int M;
+    int M = 0;
     ctdm_status st = validate(p, A, M);
     if (st != CTDM_OK) return st;
     CK(cudaSetDevice(c->device), "cudaSetDevice");
@@ -993,7 +993,7 @@ static ctdm_status submit_host(ctdm_ctx *c, const ctdm_params *p, int A, const v
 {
     if (!c || !p || !h_holo || !h_bg || !h_ri) return invalid("ctdm_reconstruct: NULL argument");
     if (bpc != 1 && bpc != 2 && bpc != 4) return invalid("ctdm_submit: bytes per count must be 1, 2 or 4");
-    int M;
+    int M = 0;
     ctdm_status st = validate(p, A, M);
     if (st != CTDM_OK) return st;
     CK(cudaSetDevice(c->device), "cudaSetDevice");
