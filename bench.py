@@ -41,6 +41,11 @@ CONFIGS = {
 }
 
 
+# Workloads measured on one GPU whatever the launch (the replicated N-GPU contract is the
+# headline workloads'); under torchrun the other ranks exit at once.
+SECONDARY = ("batched", "gradient", "gradient_small", "pocs")
+
+
 def make_workload(name, seed):
     from ctdm_gb300 import phantom
     if name == "plain_small":
@@ -55,6 +60,24 @@ def dist_info():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return rank, world, local
+
+
+def reduce_max(values, device=None):
+    """Per-rank timings -> their maximum over the ranks (the job takes as long as its
+    slowest replica); the values unchanged without an initialised process group."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return [float(v) for v in values]
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.cpu()]
+
+
+def whole_job_rate(world, units_per_rank, ms):
+    """Units of all replicas (each rank processes units_per_rank) per second of the
+    slowest rank's `ms`."""
+    return world * units_per_rank / (ms / 1e3)
 
 
 # ---------------------------------------------------------------- clocks
@@ -257,7 +280,7 @@ def run_batched(args):
         "metric": "tomograms/s (hologram->RI), batched",
         "value": tomos / (ms_graph / 1e3),
         "unit": "tomograms/s",
-        "n_gpus": world,
+        "n_gpus": 1,
         "steps": args.steps,
         "warmup": args.warmup,
         "ms_per_step": ms_graph / args.steps,
@@ -269,7 +292,7 @@ def run_batched(args):
         "config": {"workload": "batched", "tomograms": len(jobs), "lanes": cfg["lanes"],
                    "angles": [m[0] for m in meta], "holograms": [m[1] for m in meta],
                    "volumes": [m[2] for m in meta], "iterations": cfg["iterations"],
-                   "parallelism": f"replicas{world}", "l2": "inputs and volumes far larger than L2"},
+                   "parallelism": "one GPU (secondary workload)", "l2": "inputs and volumes far larger than L2"},
         "one_by_one": {"value": tomos / (ms_single / 1e3), "unit": "tomograms/s",
                        "ms_per_step": ms_single / args.steps},
         "speedup_vs_one_by_one": ms_single / ms_graph,
@@ -600,10 +623,7 @@ def run_ours(args):
     barrier()
     clocks = sampler.stop()
 
-    if world > 1:
-        t = torch.tensor([dev_ms, e2e_ms, sync_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        dev_ms, e2e_ms, sync_ms = float(t[0]), float(t[1]), float(t[2])
+    dev_ms, e2e_ms, sync_ms = reduce_max([dev_ms, e2e_ms, sync_ms], device=dev)
     if rank != 0:
         if world > 1:
             torch.distributed.destroy_process_group()
@@ -630,10 +650,9 @@ def run_ours(args):
     peak, peak_kind = measured_peaks()
     traffic = ncu_traffic(kernel_of[best], args.config)
     cpu_s, cores, text = cpu_sample(acq, cfg["iterations"], cfg["goldstein"])
-    tomos = world * args.steps
     line = {
         "metric": "tomograms/s (hologram->RI)",
-        "value": tomos / (dev_ms / 1e3),
+        "value": whole_job_rate(world, args.steps, dev_ms),
         "unit": "tomograms/s",
         "n_gpus": world,
         "steps": args.steps,
@@ -647,12 +666,12 @@ def run_ours(args):
         "config": {"workload": args.config, "holograms": f"{A}x{acq.n_holo}^2", "window": acq.m_crop,
                    "volume": f"{r}^3", "iterations": cfg["iterations"], "goldstein": cfg["goldstein"],
                    "parallelism": f"replicas{world}", "l2": "flushed between steps (256 MiB write)"},
-        "e2e": {"value": tomos / (e2e_ms / 1e3), "unit": "tomograms/s",
+        "e2e": {"value": whole_job_rate(world, args.steps, e2e_ms), "unit": "tomograms/s",
                 "h2d_bytes_per_step": int(h_holo.numel() * h_holo.element_size() + h_bg.numel() * h_bg.element_size()),
                 "upload": "uint16 counts (exact: integer photon counts)" if exact16 else "float32",
                 "d2h_bytes_per_step": int(r3 * 8),
                 "mode": "stream of tomograms: ctdm_submit per step, one ctdm_wait (host clock)",
-                "one_call_at_a_time": tomos / (sync_ms / 1e3)},
+                "one_call_at_a_time": whole_job_rate(world, args.steps, sync_ms)},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": kernel_of[best], "stage": best, "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "loop_scheme": scheme, "measured_voxels": measured,
@@ -720,10 +739,13 @@ def main():
     ap.add_argument("--config", default="wrap_heavy", choices=sorted(CONFIGS))
     ap.add_argument("--loop-scheme", type=int, default=-1, choices=[-1, 0, 1, 2],
                     help="positivity-loop scheme of the volume side, with plan variants 0 for its passes "
-                         "(-1: the autotuner's choice; profiles pin 1, the choice without a profiler)")
+                         "(-1: the autotuner's choice; profiles pin 2, the choice without a profiler)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    rank, world, _ = dist_info()
+    if args.impl == "ours" and args.config in SECONDARY and world > 1 and rank != 0:
+        return   # secondary workloads measure one GPU: rank 0 alone runs and prints
     if args.impl == "reference":
         run_reference(args)
     elif args.config == "batched":
