@@ -988,8 +988,8 @@ static cudaError_t start_download(ctdm_ctx *c)
 // its loop), and its final pass waits for the previous call's download (which runs
 // beside this call's front end).  With pageable host buffers the copies are staged by
 // the driver and the overlap is lost, the result is the same.
-static ctdm_status submit_host(ctdm_ctx *c, const ctdm_params *p, int A, const void *h_holo, const void *h_bg, int bpc,
-                               const float *h_angx, const float *h_angy, ctdm_cfloat *h_ri)
+static ctdm_status submit_enqueue(ctdm_ctx *c, const ctdm_params *p, int A, const void *h_holo, const void *h_bg,
+                                  int bpc, const float *h_angx, const float *h_angy, ctdm_cfloat *h_ri)
 {
     if (!c || !p || !h_holo || !h_bg || !h_ri) return invalid("ctdm_reconstruct: NULL argument");
     if (bpc != 1 && bpc != 2 && bpc != 4) return invalid("ctdm_submit: bytes per count must be 1, 2 or 4");
@@ -1059,6 +1059,18 @@ static ctdm_status submit_host(ctdm_ctx *c, const ctdm_params *p, int A, const v
     c->in_flight++;
     g_err.clear();
     return CTDM_OK;
+}
+
+static ctdm_status submit_host(ctdm_ctx *c, const ctdm_params *p, int A, const void *h_holo, const void *h_bg, int bpc,
+                               const float *h_angx, const float *h_angy, ctdm_cfloat *h_ri)
+{
+    const ctdm_status st = submit_enqueue(c, p, A, h_holo, h_bg, bpc, h_angx, h_angy, h_ri);
+    if (st != CTDM_OK && c) {
+        // a call that failed part way may have copies in flight from the caller's buffers:
+        // they finish before the error returns (their own errors are not reported)
+        for (cudaStream_t q : {c->copy, c->d2h, (cudaStream_t)0}) cudaStreamSynchronize(q);
+    }
+    return st;
 }
 
 // Waits for every submitted call; reports a bounded device-side wait that ran out in
