@@ -74,3 +74,26 @@ def test_submitted_calls_overlap_and_match(ctx, dev):
     for k in range(2):
         assert np.array_equal(outs[k], want[k])
     ctx.wait()   # nothing in flight: returns at once
+
+
+def test_submit_rejects_bad_arguments_and_recovers(ctx, dev):
+    """A refused submission leaves nothing in flight: the next call runs normally."""
+    import ctypes
+    import ctdm_gb300 as C
+    from ctdm_gb300 import _lib, phantom
+    acq = phantom.acquisition(128, 64, 19, seed=29, pixel=0.2e-6, photons=1e4)
+    p = C.params_for(acq, 2)
+    r = acq.r_vol
+    h = np.ascontiguousarray(acq.holograms.astype(np.uint16))
+    b = np.ascontiguousarray(acq.background.astype(np.uint16))
+    ax, ay = np.ascontiguousarray(acq.ang_x, np.float32), np.ascontiguousarray(acq.ang_y, np.float32)
+    out = np.empty((r, r, r), np.complex64)
+    lib = _lib.load()
+    rc = lib.ctdm_submit(ctx.handle, ctypes.byref(p), len(ax), h.ctypes.data, b.ctypes.data, 3, ax.ctypes.data,
+                         ay.ctypes.data, out.ctypes.data)
+    assert rc != 0 and "bytes per count" in _lib.last_error()
+    assert lib.ctdm_wait(ctx.handle) == 0
+    want = ctx.reconstruct(p, h, b, acq.ang_x, acq.ang_y)
+    ctx.submit(p, h, b, acq.ang_x, acq.ang_y, out)
+    ctx.wait()
+    assert np.array_equal(out, want)
