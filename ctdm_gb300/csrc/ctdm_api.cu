@@ -299,7 +299,12 @@ static cudaError_t ensure(ctdm_ctx *c, int id, size_t bytes)
 {
     c->used[id] = bytes;
     if (c->cap[id] >= bytes && c->buf[id]) return cudaSuccess;
-    if (c->buf[id]) cudaFree(c->buf[id]);
+    if (c->buf[id]) {
+        // calls in flight (submitted, or on the side and copy streams) may still use it
+        cudaError_t e = cudaDeviceSynchronize();
+        if (e != cudaSuccess) return e;
+        cudaFree(c->buf[id]);
+    }
     c->buf[id] = nullptr;
     c->cap[id] = 0;
     if (bytes == 0) return cudaSuccess;
