@@ -73,3 +73,19 @@ def test_reference_arm_rank_zero_reports_unavailable_workloads():
     assert r.returncode == 0, r.stderr
     line = json.loads(r.stdout.strip().splitlines()[-1])
     assert line["impl"] == "reference" and "unavailable" in line
+
+
+def test_reference_arm_line_on_cpu():
+    """The reference arm (the FP64 CPU restatement on the host cores) prints the bench
+    line's contract: the metric, unit and direction of the GPU arm, a cpu_baseline that
+    describes the run, and an e2e entry with no host-device copies."""
+    r = _run_bench(["--impl", "reference", "--config", "plain_small", "--steps", "1", "--warmup", "3"], 0, 1)
+    assert r.returncode == 0, r.stderr
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["metric"] == "tomograms/s (hologram->RI)"
+    assert line["unit"] == "tomograms/s" and line["higher_is_better"] is True and line["value"] > 0
+    assert line["config"]["workload"] == "plain_small"
+    cb = line["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == line["value"] and cb["sample"]
+    assert line["e2e"] == {"value": line["value"], "unit": "tomograms/s", "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
