@@ -143,8 +143,9 @@ CTDM_API ctdm_status ctdm_reconstruct_u8(ctdm_ctx *ctx, const ctdm_params *p, in
  * 2 (uint16) or 1 (uint8) per hologram pixel.  The host buffers must stay valid, and
  * h_ri unread, until ctdm_wait returns.  Calls in flight overlap: a call's uploads run
  * beside the previous call's loop once that call's front end has read the inputs, and
- * its volume download beside the next call's front end; with pageable buffers the copies
- * do not overlap, the results are the same.  ctdm_reconstruct* is ctdm_submit + ctdm_wait. */
+ * its volume download beside the next call's loop (the last call's in ctdm_wait); with
+ * pageable buffers the copies do not overlap, the results are the same.  A refused call
+ * leaves nothing in flight.  ctdm_reconstruct* is ctdm_submit + ctdm_wait. */
 CTDM_API ctdm_status ctdm_submit(ctdm_ctx *ctx, const ctdm_params *p, int n_angles, const void *h_holo,
                                  const void *h_bg, int bytes_per_count, const float *h_angx, const float *h_angy,
                                  ctdm_cfloat *h_ri);
