@@ -105,7 +105,7 @@ class Context:
     def submit(self, params, holo, bg, angx, angy, out):
         """ctdm_submit: enqueue a host-buffer reconstruction into `out` and return.  The
         arrays (numpy, or pinned torch CPU tensors for overlapped copies) must stay alive
-        and `out` unread until wait()."""
+        and `out` unread until wait(); until then only submit() may use this context."""
         def ptr_dtype(a):
             if hasattr(a, "data_ptr"):
                 return a.data_ptr(), {"torch.uint16": 2, "torch.uint8": 1, "torch.float32": 4}[str(a.dtype)]

@@ -145,7 +145,9 @@ CTDM_API ctdm_status ctdm_reconstruct_u8(ctdm_ctx *ctx, const ctdm_params *p, in
  * beside the previous call's loop once that call's front end has read the inputs, and
  * its volume download beside the next call's loop (the last call's in ctdm_wait); with
  * pageable buffers the copies do not overlap, the results are the same.  A refused call
- * leaves nothing in flight.  ctdm_reconstruct* is ctdm_submit + ctdm_wait. */
+ * leaves nothing in flight.  Submitted calls share the context's device buffers: until
+ * ctdm_wait returns, make no other call on the same context than ctdm_submit (another
+ * context serves other work meanwhile).  ctdm_reconstruct* is ctdm_submit + ctdm_wait. */
 CTDM_API ctdm_status ctdm_submit(ctdm_ctx *ctx, const ctdm_params *p, int n_angles, const void *h_holo,
                                  const void *h_bg, int bytes_per_count, const float *h_angx, const float *h_angy,
                                  ctdm_cfloat *h_ri);
