@@ -154,49 +154,46 @@ def ncu_traffic(kernel, workload):
 
 
 # ---------------------------------------------------------------- CPU baseline (oracle)
-def cpu_sample(acq, iters, goldstein=False, threads=None):
-    """FP64 oracle on a bounded sample of one tomogram: the per-angle chain (QPI,
-    DCT unwrap, Goldstein when configured, resize/median, Rytov spectrum) on two
-    angles and the positivity loop with 0 and 1 iterations at full volume size,
-    extrapolated to the whole tomogram.  Returns (seconds per tomogram, threads, text)."""
+def oracle_module():
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     O.build()
-    if threads:
-        O.set_threads(threads)
+    return O
+
+
+def cpu_tomogram(O, acq, iters, goldstein):
+    """One whole tomogram through the FP64 CPU implementation of the path (the oracle's
+    or_tomogram: QPI, Goldstein when configured, DCT unwrap, resize, median, spectra in
+    parallel over the angles on every host thread, then the Ewald mapping and the
+    positivity loop).  Returns its wall time in seconds."""
+    par = O.make_params(acq.n_holo, acq.m_crop, acq.r_vol, iters, acq.fm0, acq.df, acq.dx, acq.k2, acq.n_med)
+    t0 = time.perf_counter()
+    O.tomogram(par, acq.holograms, acq.background, acq.ang_x, acq.ang_y, run_goldstein=goldstein)
+    return time.perf_counter() - t0
+
+
+def cpu_sample(acq, iters, goldstein=False, min_seconds=10.0, max_tomograms=3):
+    """The CPU baseline beside the GPU number: whole tomograms of the same workload,
+    measured (not extrapolated), until `min_seconds` have passed or `max_tomograms` ran.
+    Returns (seconds per tomogram, threads, text)."""
+    O = oracle_module()
     nthr = O.get_threads()
-    A, m, n, r = len(acq.ang_x), acq.m_crop, acq.n_holo, acq.r_vol
-    s = 2
-    t0 = time.perf_counter()
-    car = O.qpi_carrier(acq.background)
-    bgf = O.qpi_field(acq.background, m, *car)
-    t_fixed = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    U = []
-    for a in range(s):
-        ph, am = O.wrap_phase(O.qpi_field(acq.holograms[a], m, *car), bgf)
-        if goldstein:
-            O.goldstein(ph.astype(np.float32))
-        uw = O.dct_unwrap(ph, 0)
-        p1, a1 = O.resize_crop(uw, am, n, r)
-        p2, a2 = O.median_check(p1, a1)
-        U.append(O.rytov_spectrum(p2, a2))
-    t_angle = (time.perf_counter() - t0) / s
-    t0 = time.perf_counter()
-    F2, C = O.ewald_map(np.stack(U), acq.ang_x[:s], acq.ang_y[:s], acq.fm0, acq.df, acq.dx)
-    t_map = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    O.positivity(F2, C, 0, acq.k2, acq.n_med)
-    t_p0 = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    O.positivity(F2, C, 1, acq.k2, acq.n_med)
-    t_p1 = time.perf_counter() - t0
-    t_iter = max(t_p1 - t_p0, 0.0)
-    total = t_fixed + A * t_angle + t_map + t_p0 + iters * t_iter
-    text = (f"oracle on {s} of {A} angles{' incl. Goldstein' if goldstein else ''} + positivity loop with 0 and 1 "
-            f"iterations at {r}^3, extrapolated: {A}x{t_angle:.3f}s/angle + {t_fixed + t_map + t_p0:.2f}s + "
-            f"{iters}x{t_iter:.2f}s/iter")
-    return total, nthr, text
+    times = []
+    while len(times) < max_tomograms and sum(times) < min_seconds:
+        times.append(cpu_tomogram(O, acq, iters, goldstein))
+    per = sum(times) / len(times)
+    text = (f"measured: {len(times)} whole tomogram(s) of this workload through the FP64 oracle "
+            f"({len(acq.ang_x)} angles{' with Goldstein' if goldstein else ''}, {iters} iterations at "
+            f"{acq.r_vol}^3) on {nthr} host threads, {per:.2f} s each")
+    return per, nthr, text
+
+
+def workload_config(name, acq, world):
+    """The `config` object of both arms' lines for workload `name`."""
+    cfg = CONFIGS[name]
+    return {"workload": name, "holograms": f"{len(acq.ang_x)}x{acq.n_holo}^2", "window": acq.m_crop,
+            "volume": f"{acq.r_vol}^3", "iterations": cfg["iterations"], "goldstein": cfg["goldstein"],
+            "parallelism": f"replicas{world}", "l2": "flushed between steps (256 MiB write)"}
 
 
 # ---------------------------------------------------------------- batched workload
@@ -663,9 +660,7 @@ def run_ours(args):
         "vs_baseline": None,
         "dtype": "f32/c64",
         "data": "synthetic (seeded Rytov phantom, Poisson noise)",
-        "config": {"workload": args.config, "holograms": f"{A}x{acq.n_holo}^2", "window": acq.m_crop,
-                   "volume": f"{r}^3", "iterations": cfg["iterations"], "goldstein": cfg["goldstein"],
-                   "parallelism": f"replicas{world}", "l2": "flushed between steps (256 MiB write)"},
+        "config": workload_config(args.config, acq, world),
         "e2e": {"value": whole_job_rate(world, args.steps, e2e_ms), "unit": "tomograms/s",
                 "h2d_bytes_per_step": int(h_holo.numel() * h_holo.element_size() + h_bg.numel() * h_bg.element_size()),
                 "upload": "uint16 counts (exact: integer photon counts)" if exact16 else "float32",
@@ -688,6 +683,9 @@ def run_ours(args):
 
 
 def run_reference(args):
+    """The reference arm: the path's CPU implementation (the FP64 oracle, a restatement
+    of the reference's kernels; the reference itself is CUDA) on all host threads, one
+    whole tomogram of the same workload per step, measured."""
     rank, world, local = dist_info()
     if rank != 0:
         return
@@ -701,13 +699,16 @@ def run_reference(args):
         return
     cfg = CONFIGS[args.config]
     acq = make_workload(args.config, seed=1000)
-    times = []
-    for k in range(args.warmup + args.steps):
-        s, cores, text = cpu_sample(acq, cfg["iterations"], cfg["goldstein"])
-        if k >= args.warmup:
-            times.append(s)
-    per = sum(times) / len(times)
-    value = 1.0 / per
+    O = oracle_module()
+    cores = O.get_threads()
+    for _ in range(args.warmup):
+        cpu_tomogram(O, acq, cfg["iterations"], cfg["goldstein"])
+    times = [cpu_tomogram(O, acq, cfg["iterations"], cfg["goldstein"]) for _ in range(args.steps)]
+    total = sum(times)
+    value = args.steps / total
+    text = (f"measured: {args.steps} whole tomograms ({len(acq.ang_x)} angles"
+            f"{' with Goldstein' if cfg['goldstein'] else ''}, {cfg['iterations']} iterations at {acq.r_vol}^3) "
+            f"through the FP64 oracle on {cores} host threads, {total / args.steps:.2f} s each")
     line = {
         "impl": "reference",
         "metric": "tomograms/s (hologram->RI)",
@@ -716,14 +717,13 @@ def run_reference(args):
         "n_gpus": world,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": per * 1e3,
+        "ms_per_step": total / args.steps * 1e3,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (seeded Rytov phantom, Poisson noise)",
-        "config": {"workload": args.config, "holograms": f"{len(acq.ang_x)}x{acq.n_holo}^2",
-                   "volume": f"{acq.r_vol}^3", "iterations": cfg["iterations"]},
+        "config": workload_config(args.config, acq, world),
         "cpu_baseline": {"value": value, "unit": "tomograms/s", "cores": cores, "kind": "port", "sample": text},
         "e2e": {"value": value, "unit": "tomograms/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }

@@ -150,6 +150,13 @@ class Context:
         check(self.lib.ctdm_ctx_device_status(self.handle, ctypes.byref(st)), "ctdm_ctx_device_status")
         return st.value
 
+    def probe_wait(self, polls=0):
+        """One bounded device-side wait that nothing completes (code 9 in the status
+        word); returns its length in ms.  polls <= 0: the production bound."""
+        ms = ctypes.c_double()
+        check(self.lib.ctdm_ctx_probe_wait(self.handle, int(polls), ctypes.byref(ms)), "ctdm_ctx_probe_wait")
+        return ms.value
+
     def buffer(self, which):
         p, n = ctypes.c_void_p(), ctypes.c_size_t()
         check(self.lib.ctdm_ctx_buffer(self.handle, int(which), ctypes.byref(p), ctypes.byref(n)), "ctdm_ctx_buffer")

@@ -10,6 +10,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "libctdm_gb300.so")
 
 c_int, c_double, c_float, c_void_p, c_size_t = ctypes.c_int, ctypes.c_double, ctypes.c_float, ctypes.c_void_p, ctypes.c_size_t
+c_bool = ctypes.c_bool
 P_int = ctypes.POINTER(ctypes.c_int)
 
 
@@ -70,6 +71,7 @@ _SIGS = {
     "ctdm_ctx_set_timing": (c_int, [c_void_p, c_int]),
     "ctdm_ctx_stage_times": (c_int, [c_void_p, ctypes.POINTER(c_double), P_int, c_int]),
     "ctdm_ctx_device_status": (c_int, [c_void_p, P_int]),
+    "ctdm_ctx_probe_wait": (c_int, [c_void_p, c_int, ctypes.POINTER(c_double)]),
     "ctdm_launch_count": (ctypes.c_ulonglong, []),
     "ctdm_reconstruct_device": (c_int, [c_void_p, ctypes.POINTER(Params), c_int, c_void_p, c_void_p, c_void_p,
                                         c_void_p, c_void_p, c_void_p]),
@@ -85,6 +87,7 @@ _SIGS = {
     "ctdm_qpi": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_int, P_int, c_void_p, c_void_p,
                          c_void_p]),
     "ctdm_qpi_b": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_int, P_int, c_void_p, c_void_p, c_void_p]),
+    "extractQPI_AlgorithmA": (None, [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_int]),
     "extractQPI_AlgorithmB": (None, [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_int]),
     "ctdm_unwrap_dct": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p]),
     "ctdm_unwrap_fast": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p]),
@@ -160,7 +163,7 @@ _SIGS = {
     "HilbertTransform": (None, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, P_int, P_int,
                                 c_int, c_int, c_int, c_int, c_int]),
     "AngCal_GPU": (c_float, [c_void_p, c_int, c_int, c_int, c_int]),
-    "checkArray": (c_int, [c_void_p, c_float, c_float, c_int]),
+    "checkArray": (c_bool, [c_void_p, c_float, c_float, c_int]),
 }
 
 EXPORTED = tuple(_SIGS)

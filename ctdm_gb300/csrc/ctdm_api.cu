@@ -1,6 +1,7 @@
 // Host runtime and C ABI of libctdm_gb300: device tables, contexts, workspace,
 // the fused hologram -> RI pipeline and the reference-named entry points.
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cmath>
 #include <cstdarg>
@@ -26,6 +27,8 @@ cudaError_t compat_est_n(float2 *n, const float2 *F, float k2, float nm, long cn
 cudaError_t compat_modify(const float2 *n, float2 *F, float k2, float nm2, long cnt, cudaStream_t s);
 cudaError_t compat_check(float2 *F, const float2 *F2, long cnt, cudaStream_t s);
 cudaError_t counts_to_mask(const uint32_t *c, uint8_t *m, long n, cudaStream_t s);
+cudaError_t real_parts(const float2 *in, float *out, long n, cudaStream_t s);
+cudaError_t bounded_wait_probe(int *err, int polls, int code, long long *cycles, cudaStream_t s);
 cudaError_t median_stack(const float *ph, const float *am, int A, int R, float *ph_out, float *am_out,
                          cudaStream_t s);
 cudaError_t set_carrier(int *carrier, int r, int c, int rad, cudaStream_t s);
@@ -400,6 +403,10 @@ extern "C" void ctdm_ctx_destroy(ctdm_ctx *c)
     delete c;
 }
 
+// Until ctdm_wait returns, a context serves ctdm_submit alone: the calls in flight
+// still read and write its buffers, so every other entry point on it is refused.
+static bool in_flight(const ctdm_ctx *c) { return c && c->in_flight > 0; }
+
 extern "C" ctdm_status ctdm_ctx_set_timing(ctdm_ctx *c, int on)
 {
     if (!c) return invalid("ctdm_ctx_set_timing: NULL context");
@@ -451,6 +458,28 @@ extern "C" ctdm_status ctdm_ctx_device_status(ctdm_ctx *c, int *status)
     return CTDM_OK;
 }
 
+// One bounded device-side wait that nothing completes, recorded as code 9 in the
+// context's status word (see the header).
+extern "C" ctdm_status ctdm_ctx_probe_wait(ctdm_ctx *c, int polls, double *ms)
+{
+    if (!c) return invalid("ctdm_ctx_probe_wait: NULL context");
+    if (in_flight(c))
+        return invalid("ctdm_ctx_probe_wait: calls submitted on this context are still in flight (ctdm_wait first)");
+    CK(cudaSetDevice(c->device), "cudaSetDevice");
+    long long *cycles = nullptr;
+    CK(cudaMalloc(&cycles, sizeof(long long)), "alloc probe clock");
+    cudaError_t e = bounded_wait_probe(c->d_err, polls, 9, cycles, 0);
+    long long host = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&host, cycles, sizeof host, cudaMemcpyDeviceToHost);
+    int khz = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, c->device);
+    cudaFree(cycles);
+    CK(e, "bounded wait probe");
+    if (ms) *ms = khz > 0 ? (double)host / (double)khz : 0.0;
+    g_err.clear();
+    return CTDM_OK;
+}
+
 extern "C" ctdm_status ctdm_ctx_carrier(ctdm_ctx *c, int *carrier3)
 {
     if (!c || !carrier3) return invalid("ctdm_ctx_carrier: NULL argument");
@@ -465,6 +494,8 @@ extern "C" ctdm_status ctdm_ctx_carrier(ctdm_ctx *c, int *carrier3)
 
 extern "C" ctdm_status ctdm_ctx_read_buffer(ctdm_ctx *c, int which, void *host, size_t bytes)
 {
+    if (in_flight(c))
+        return invalid("ctdm_ctx_read_buffer: calls submitted on this context are still in flight (ctdm_wait first)");
     void *d = nullptr;
     size_t n = 0;
     ctdm_status st = ctdm_ctx_buffer(c, which, &d, &n);
@@ -478,6 +509,8 @@ extern "C" ctdm_status ctdm_ctx_read_buffer(ctdm_ctx *c, int which, void *host, 
 
 extern "C" ctdm_status ctdm_ctx_buffer(ctdm_ctx *c, int which, void **dptr, size_t *bytes)
 {
+    if (in_flight(c))
+        return invalid("ctdm_ctx_buffer: calls submitted on this context are still in flight (ctdm_wait first)");
     static const int map[] = {B_PHASE, B_AMP, B_PHU, B_CHG, B_CUT, B_GOLD, B_U, B_F2, B_COUNTS};
     if (!c || !dptr || which < 0 || which > 8) return invalid("ctdm_ctx_buffer: bad argument");
     *dptr = c->buf[map[which]];
@@ -716,6 +749,8 @@ extern "C" ctdm_status ctdm_qpi_b(ctdm_ctx *c, int N, int A, const float *d_holo
                                   int *center2, float *d_phase, float *d_amp, void *stream)
 {
     if (!c || !d_holo || !d_bg || !d_phase || !d_amp) return invalid("ctdm_qpi_b: NULL argument");
+    if (in_flight(c))
+        return invalid("ctdm_qpi_b: calls submitted on this context are still in flight (ctdm_wait first)");
     CK(cudaSetDevice(c->device), "cudaSetDevice");
     cudaStream_t s = (cudaStream_t)stream;
     ctdm_status st = do_qpi_b(c, N, A, d_holo, d_bg, bg_per_angle, center2, d_phase, d_amp, s);
@@ -745,6 +780,10 @@ static ctdm_status validate(const ctdm_params *p, int A, int &M)
     if (p->iterations < 0) return invalid("negative iteration count");
     if (p->n_med <= 0 || p->wavelength <= 0 || p->dx <= 0) return invalid("non-positive physical parameter");
     if (p->unwrap_method < 0 || p->unwrap_method > 2) return invalid("unknown unwrap method");
+    if (p->unwrap_mode != CTDM_UNWRAP_REF && p->unwrap_mode != CTDM_UNWRAP_EXACT)
+        return invalid("unknown unwrap mode %d", p->unwrap_mode);
+    if (p->check_mode != CTDM_CHECK_REF && p->check_mode != CTDM_CHECK_MASK)
+        return invalid("unknown check mode %d", p->check_mode);
     return CTDM_OK;
 }
 
@@ -933,6 +972,8 @@ extern "C" ctdm_status ctdm_reconstruct_device(ctdm_ctx *c, const ctdm_params *p
     int M = 0;
     ctdm_status st = validate(p, A, M);
     if (st != CTDM_OK) return st;
+    if (in_flight(c))
+        return invalid("ctdm_reconstruct_device: calls submitted on this context are still in flight (ctdm_wait first)");
     CK(cudaSetDevice(c->device), "cudaSetDevice");
     st = reconstruct_core(c, p, A, M, d_holo, d_bg, h_angx, h_angy, d_ri, (cudaStream_t)stream, nullptr);
     if (st != CTDM_OK) return st;
@@ -1089,6 +1130,9 @@ static ctdm_status wait_host(ctdm_ctx *c)
     CK(cudaStreamSynchronize(c->d2h), "synchronise");
     CK(cudaStreamSynchronize(0), "synchronise");
     c->in_flight = 0;
+    // the device is idle: the next call starts again from the first volume buffer, so
+    // a context that never has two calls in flight keeps only that one
+    c->slot = 0;
     const int derr = c->pin->derr;
     if (derr != 0) {
         c->pin->derr = 0;
@@ -1145,6 +1189,8 @@ extern "C" ctdm_status ctdm_qpi(ctdm_ctx *c, int N, int M, int A, const float *d
                                 int bg_per_angle, int *carrier3, float *d_phase, float *d_amp, void *stream)
 {
     if (!c || !d_holo || !d_bg || !d_phase || !d_amp) return invalid("ctdm_qpi: NULL argument");
+    if (in_flight(c))
+        return invalid("ctdm_qpi: calls submitted on this context are still in flight (ctdm_wait first)");
     CK(cudaSetDevice(c->device), "cudaSetDevice");
     cudaStream_t s = (cudaStream_t)stream;
     ctdm_status st = do_qpi(c, N, M, A, d_holo, d_bg, bg_per_angle, carrier3, d_phase, d_amp, s);
@@ -1160,7 +1206,10 @@ extern "C" ctdm_status ctdm_unwrap_dct(ctdm_ctx *c, int A, int M, int mode, cons
                                        void *stream)
 {
     if (!c || !d_phi || !d_out) return invalid("ctdm_unwrap_dct: NULL argument");
+    if (in_flight(c))
+        return invalid("ctdm_unwrap_dct: calls submitted on this context are still in flight (ctdm_wait first)");
     if (!ok_crop(M) || A < 1) return invalid("ctdm_unwrap_dct: size %d unsupported", M);
+    if (mode != CTDM_UNWRAP_REF && mode != CTDM_UNWRAP_EXACT) return invalid("ctdm_unwrap_dct: unknown mode %d", mode);
     CK(cudaSetDevice(c->device), "cudaSetDevice");
     CK(ensure(c, B_TMP, sizeof(float) * A * M * M), "alloc scratch");
     CK(dct_unwrap(d_phi, d_out, B<float>(c, B_TMP), A, M, mode, (cudaStream_t)stream), "dct unwrap");
@@ -1170,6 +1219,8 @@ extern "C" ctdm_status ctdm_unwrap_dct(ctdm_ctx *c, int A, int M, int mode, cons
 extern "C" ctdm_status ctdm_unwrap_fast(ctdm_ctx *c, int A, int M, float *d_phi, float *d_out, void *stream)
 {
     if (!c || !d_phi || !d_out) return invalid("ctdm_unwrap_fast: NULL argument");
+    if (in_flight(c))
+        return invalid("ctdm_unwrap_fast: calls submitted on this context are still in flight (ctdm_wait first)");
     if (!ok_crop(M) || A < 1) return invalid("ctdm_unwrap_fast: size %d unsupported", M);
     CK(cudaSetDevice(c->device), "cudaSetDevice");
     CK(ensure(c, B_FASTW, sizeof(float2) * 3 * 4 * M * M), "alloc scratch");
@@ -1181,6 +1232,8 @@ extern "C" ctdm_status ctdm_goldstein(ctdm_ctx *c, int A, int W, int H, const fl
                                       uint8_t *d_cuts, float *d_out, int *h_status, void *stream)
 {
     if (!c || !d_phi || !d_charges || !d_cuts || !d_out) return invalid("ctdm_goldstein: NULL argument");
+    if (in_flight(c))
+        return invalid("ctdm_goldstein: calls submitted on this context are still in flight (ctdm_wait first)");
     if (W < 4 || H < 4 || W > 1024 || H > 1024 || A < 1) return invalid("ctdm_goldstein: size unsupported");
     CK(cudaSetDevice(c->device), "cudaSetDevice");
     cudaStream_t s = (cudaStream_t)stream;
@@ -1211,6 +1264,8 @@ extern "C" ctdm_status ctdm_goldstein_fill(ctdm_ctx *c, int A, int W, int H, con
                                            const float *d_phi, float *d_out, int *h_status, void *stream)
 {
     if (!c || !d_cuts || !d_phi || !d_out) return invalid("ctdm_goldstein_fill: NULL argument");
+    if (in_flight(c))
+        return invalid("ctdm_goldstein_fill: calls submitted on this context are still in flight (ctdm_wait first)");
     if (W < 4 || H < 4 || W > 1024 || H > 1024 || A < 1) return invalid("ctdm_goldstein_fill: size unsupported");
     CK(cudaSetDevice(c->device), "cudaSetDevice");
     cudaStream_t s = (cudaStream_t)stream;
@@ -1232,6 +1287,8 @@ extern "C" ctdm_status ctdm_prepare_spectra(ctdm_ctx *c, int A, int M, int N, in
                                             const float *d_amp, ctdm_cfloat *d_U, void *stream)
 {
     if (!c || !d_phase || !d_amp || !d_U) return invalid("ctdm_prepare_spectra: NULL argument");
+    if (in_flight(c))
+        return invalid("ctdm_prepare_spectra: calls submitted on this context are still in flight (ctdm_wait first)");
     if (!ok_volume(R) || R > N || M < 2 || A < 1) return invalid("ctdm_prepare_spectra: size unsupported");
     CK(cudaSetDevice(c->device), "cudaSetDevice");
     cudaStream_t s = (cudaStream_t)stream;
@@ -1246,6 +1303,8 @@ extern "C" ctdm_status ctdm_stack_spectra(ctdm_ctx *c, int A, int R, const float
                                           ctdm_cfloat *d_U, void *stream)
 {
     if (!c || !d_ph || !d_am || !d_U) return invalid("ctdm_stack_spectra: NULL argument");
+    if (in_flight(c))
+        return invalid("ctdm_stack_spectra: calls submitted on this context are still in flight (ctdm_wait first)");
     if (!ok_volume(R) || A < 1) return invalid("ctdm_stack_spectra: size unsupported");
     CK(cudaSetDevice(c->device), "cudaSetDevice");
     cudaStream_t s = (cudaStream_t)stream;
@@ -1260,6 +1319,8 @@ extern "C" ctdm_status ctdm_prepare_stack(ctdm_ctx *c, int A, int M, int N, int 
                                           const float *d_amp, float *d_ph_out, float *d_am_out, void *stream)
 {
     if (!c || !d_phase || !d_amp || !d_ph_out || !d_am_out) return invalid("ctdm_prepare_stack: NULL argument");
+    if (in_flight(c))
+        return invalid("ctdm_prepare_stack: calls submitted on this context are still in flight (ctdm_wait first)");
     if (R > N || R < 1 || M < 2 || A < 1) return invalid("ctdm_prepare_stack: size unsupported");
     CK(cudaSetDevice(c->device), "cudaSetDevice");
     CK(prep_stack(d_phase, d_amp, A, M, N, R, d_ph_out, d_am_out, (cudaStream_t)stream), "prep stack");
@@ -1271,6 +1332,8 @@ extern "C" ctdm_status ctdm_map_ewald(ctdm_ctx *c, int A, int R, const ctdm_cflo
                                       uint32_t *d_counts, void *stream)
 {
     if (!c || !d_U || !h_angx || !h_angy || !d_F2) return invalid("ctdm_map_ewald: NULL argument");
+    if (in_flight(c))
+        return invalid("ctdm_map_ewald: calls submitted on this context are still in flight (ctdm_wait first)");
     if (!ok_volume(R) || A < 1 || A > kMaxAngles) return invalid("ctdm_map_ewald: size unsupported");
     CK(cudaSetDevice(c->device), "cudaSetDevice");
     cudaStream_t s = (cudaStream_t)stream;
@@ -1301,6 +1364,8 @@ extern "C" ctdm_status ctdm_map_fi(ctdm_ctx *c, int A, int R, const ctdm_cfloat 
                                    void *stream)
 {
     if (!c || !d_U || !h_angx || !d_F2) return invalid("ctdm_map_fi: NULL argument");
+    if (in_flight(c))
+        return invalid("ctdm_map_fi: calls submitted on this context are still in flight (ctdm_wait first)");
     if (!ok_volume(R) || A < 1 || A > kMaxAngles) return invalid("ctdm_map_fi: size unsupported");
     for (int a = 0; a < A; a++)
         if (!std::isfinite(h_angx[a]) || std::fabs(h_angx[a]) >= 0.5 * CTDM_PI_D)
@@ -1364,6 +1429,8 @@ extern "C" ctdm_status ctdm_pocs(ctdm_ctx *c, int R, const ctdm_pocs_params *p, 
                                  const ctdm_cfloat *d_F2, ctdm_cfloat *d_ri, double *h_hist, void *stream)
 {
     if (!c || !p || !d_F2 || !d_ri) return invalid("ctdm_pocs: NULL argument");
+    if (in_flight(c))
+        return invalid("ctdm_pocs: calls submitted on this context are still in flight (ctdm_wait first)");
     if (!ok_volume(R)) return invalid("ctdm_pocs: volume side %d unsupported", R);
     if (p->iterations < 0 || p->iterations > 100000 || p->tv_steps < 1 || p->tv_steps > 1000)
         return invalid("ctdm_pocs: iterations or tv_steps out of range");
@@ -1422,6 +1489,8 @@ extern "C" ctdm_status ctdm_positivity(ctdm_ctx *c, int R, int iterations, int c
                                        void *stream)
 {
     if (!c || !d_F2 || !d_ri) return invalid("ctdm_positivity: NULL argument");
+    if (in_flight(c))
+        return invalid("ctdm_positivity: calls submitted on this context are still in flight (ctdm_wait first)");
     if (!ok_volume(R) || iterations < 0) return invalid("ctdm_positivity: size unsupported");
     if (check_mode == CTDM_CHECK_MASK && !d_counts) return invalid("ctdm_positivity: mask mode needs counts");
     CK(cudaSetDevice(c->device), "cudaSetDevice");
@@ -1504,6 +1573,68 @@ extern "C" void ctdm_set_recon_globals(int recon_size, double n_med, double wave
     g_iter_time = iter_time;
     g_recon_save = recon_save;
     g_save_dir = save_dir ? save_dir : ".";
+}
+
+// Carrier {row, column, radius} of Algorithm A per device, set by frame 1 (the reference
+// keeps rCircle, cCircle and radiusCircle as globals that obtainRadius sets when
+// frame == 1, cTDM/HilbertTransform.cu:1572).
+static std::map<int, std::array<int, 3>> g_qpia_carrier;
+
+// extractQPI_AlgorithmA (cTDM/HilbertTransform.cu:1546-1585): host holograms as
+// cufftComplex with zero imaginary parts (the job loop fills them that way,
+// :711-716,879-883); the M x M fields (M = N / 4) after the inverse transform, 1/M^2 and
+// the conjugation of scaleFFT2D go to cuSP_FFT / cuBG_FFT on the device.  The reference
+// writes them into its globals cuSP2 / cuBG2, which its call sites pass as these two
+// arguments (:969,972), so the caller sees the same arrays.
+extern "C" void extractQPI_AlgorithmA(ctdm_cfloat *SP, ctdm_cfloat *BG, ctdm_cfloat *cuSP_FFT, ctdm_cfloat *cuBG_FFT,
+                                      int Nx, int Ny, int frame)
+{
+    ctdm_ctx *c = default_ctx();
+    if (!c) return;
+    if (!SP || !BG || !cuSP_FFT || !cuBG_FFT) { invalid("extractQPI_AlgorithmA: NULL argument"); return; }
+    if (Nx != Ny || Nx < 64 || Nx > 2048 || (Nx & (Nx - 1))) {
+        invalid("extractQPI_AlgorithmA: square power-of-two holograms of 64..2048 only");
+        return;
+    }
+    const int N = Nx, M = N / 4;
+    const long nn = (long)N * N, mm = (long)M * M;
+    const int *known = nullptr;
+    std::array<int, 3> kept{};
+    if (frame != 1) {
+        auto it = g_qpia_carrier.find(c->device);
+        if (it == g_qpia_carrier.end()) { invalid("extractQPI_AlgorithmA: frame 1 has not run on this device"); return; }
+        kept = it->second;
+        known = kept.data();
+    }
+    if (wait_host(c) != CTDM_OK) return;   // host-buffer calls in flight still own B_HOLO / B_BG
+    if (ensure(c, B_HOLO, sizeof(float) * nn) != cudaSuccess || ensure(c, B_BG, sizeof(float) * nn) != cudaSuccess ||
+        ensure(c, B_TMP, sizeof(float2) * nn) != cudaSuccess) {
+        cuda_fail(cudaErrorMemoryAllocation, "extractQPI_AlgorithmA");
+        return;
+    }
+    float2 *stage = B<float2>(c, B_TMP);
+    cudaError_t e = cudaMemcpy(stage, BG, sizeof(float2) * nn, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = real_parts(stage, B<float>(c, B_BG), nn, 0);
+    if (e == cudaSuccess) e = cudaMemcpy(stage, SP, sizeof(float2) * nn, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = real_parts(stage, B<float>(c, B_HOLO), nn, 0);
+    if (e != cudaSuccess) { cuda_fail(e, "extractQPI_AlgorithmA upload"); return; }
+    // carrier (detected from the background on frame 1) and the background field
+    if (qpi_setup(c, N, M, 1, B<float>(c, B_BG), 0, known, 0) != CTDM_OK) return;
+    if (frame == 1) {
+        int host[3] = {0, 0, 0};
+        e = cudaMemcpy(host, c->buf[B_CARRIER], sizeof host, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) { cuda_fail(e, "extractQPI_AlgorithmA carrier"); return; }
+        g_qpia_carrier[c->device] = {host[0], host[1], host[2]};
+    }
+    e = cudaMemcpyAsync(cuBG_FFT, c->buf[B_BGF], sizeof(float2) * mm, cudaMemcpyDeviceToDevice, 0);
+    if (e == cudaSuccess)
+        e = qpi_forward_window(B<float>(c, B_HOLO), 4, 1, N, M, B<int>(c, B_CARRIER), B<float2>(c, B_T1),
+                               B<float2>(c, B_S), 0);
+    if (e == cudaSuccess)
+        e = qpi_inverse_window(B<float2>(c, B_S), 1, M, reinterpret_cast<float2 *>(cuSP_FFT), nullptr, 0, nullptr,
+                               nullptr, 0);
+    if (e != cudaSuccess) { cuda_fail(e, "extractQPI_AlgorithmA"); return; }
+    finish("extractQPI_AlgorithmA");
 }
 
 // Carrier column of Algorithm B per device, set by frame 1 (the reference keeps it in

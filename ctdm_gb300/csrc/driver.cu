@@ -788,8 +788,8 @@ extern "C" float AngCal_GPU(float *src, int sizeX, int sizeY, int frame, int tot
     return a;
 }
 
-extern "C" int checkArray(float *array2D, float limitSTD, float limitRange, int size)
+extern "C" bool checkArray(float *array2D, float limitSTD, float limitRange, int size)
 {
-    if (!array2D || size < 1) return 1;
-    return check_array(array2D, size, limitSTD, limitRange) ? 1 : 0;
+    if (!array2D || size < 1) return true;
+    return check_array(array2D, size, limitSTD, limitRange);
 }

@@ -5,6 +5,7 @@
 
 #include "kernels_front.cuh"
 #include "point_ops.cuh"
+#include "tma.cuh"
 
 namespace ctdm {
 
@@ -71,6 +72,32 @@ __global__ void check_kernel(float2 *F, const float2 *__restrict__ F2, long cnt)
     }
 }
 
+// Real parts of complex holograms: the reference passes camera frames to
+// extractQPI_AlgorithmA as cufftComplex with zero imaginary parts
+// (cTDM/HilbertTransform.cu:711-716,879-883).
+__global__ void real_parts_kernel(const float2 *__restrict__ in, float *out, long n)
+{
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        out[i] = in[i].x;
+}
+
+// A bounded device-side wait that nothing completes: thread 0 initialises an
+// mbarrier for one arrival that never comes and waits on its first phase with the
+// wait the z pass uses for its TMA tiles (polls <= 0: its production bound).  The
+// wait runs out and records `code` in *err; no copy was issued, so nothing is in
+// flight when the kernel returns.  cycles[0] receives the wait's length in SM clocks.
+__global__ void bounded_wait_probe_kernel(int *err, int polls, int code, long long *cycles)
+{
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x != 0) return;
+    tma::mbar_init(&bar, 1);
+    tma::fence_barrier_init();
+    const long long t0 = clock64();
+    if (polls > 0) tma::mbar_wait(&bar, 0, err, code, polls);
+    else tma::mbar_wait(&bar, 0, err, code);
+    cycles[0] = clock64() - t0;
+}
+
 __global__ void counts_to_mask_kernel(const uint32_t *__restrict__ c, uint8_t *m, long n)
 {
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
@@ -120,6 +147,18 @@ cudaError_t compat_modify(const float2 *n, float2 *F, float k2, float nm2, long 
 cudaError_t compat_check(float2 *F, const float2 *F2, long cnt, cudaStream_t s)
 {
     check_kernel<<<grid_for(cnt), 256, 0, s>>>(F, F2, cnt); note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t real_parts(const float2 *in, float *out, long n, cudaStream_t s)
+{
+    real_parts_kernel<<<grid_for(n), 256, 0, s>>>(in, out, n); note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t bounded_wait_probe(int *err, int polls, int code, long long *cycles, cudaStream_t s)
+{
+    bounded_wait_probe_kernel<<<1, 32, 0, s>>>(err, polls, code, cycles); note_launch();
     return cudaGetLastError();
 }
 

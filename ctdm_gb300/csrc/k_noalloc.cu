@@ -6,10 +6,15 @@
 // cudaMalloc calls.  ctdm_unwrap_dct_noalloc serves them.  Its intermediate map and
 // its transform tables live in file-scope __device__ arrays that are part of the
 // loaded module, so a call allocates nothing; the caller passes only the input and
-// output maps.  The price: every GPU that loads the library holds these arrays
-// (about 16.1 MiB) until the process exits, the size is capped, and all calls share
-// one scratch array, so two calls that overlap on the GPU (on different streams,
-// or from different threads) race on it.
+// output maps.  The price: every GPU on which the library's kernels are loaded
+// holds these arrays (about 16.1 MiB) until the process exits, the size is capped,
+// and all calls share one scratch array, so two calls that overlap on the GPU (on
+// different streams, or from different threads) race on it.  Each .cu file of the
+// library is its own module; under CUDA's default lazy module loading this file's
+// module, arrays included, is loaded on a device by the first call there (the
+// address look-up below), not when the library is opened.  That first call is the
+// one that takes device memory, so a caller makes it as a warm-up before its pool
+// claims the memory or its loop starts.
 #include <cmath>
 #include <cstdio>
 #include <mutex>
@@ -136,6 +141,11 @@ extern "C" ctdm_status ctdm_unwrap_dct_noalloc(int A, int M, int mode, const flo
     const int idx = side_index(M);
     if (idx < 0) {
         snprintf(g_msg, sizeof g_msg, "ctdm_unwrap_dct_noalloc: map side %d not in {16, 32, 64, 128, 256}", M);
+        return fail(CTDM_ERR_INVALID);
+    }
+    if (mode != CTDM_UNWRAP_REF && mode != CTDM_UNWRAP_EXACT) {
+        snprintf(g_msg, sizeof g_msg, "ctdm_unwrap_dct_noalloc: unknown mode %d (0 reference IDCT, 1 exact DCT-III)",
+                 mode);
         return fail(CTDM_ERR_INVALID);
     }
     if (A < 1 || (long)A * M * M > kScratchFloats) {

@@ -67,12 +67,13 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
 }
 
 // Bounded wait for phase `parity` of `bar`.  Returns false (and records `code` in
-// *err when err is given) if the phase has not completed after kMaxPolls polls;
-// each poll is a hardware try_wait, so the bound is well above any real copy.
+// *err when err is given) if the phase has not completed after `polls` polls
+// (kMaxPolls unless a diagnostic asks for fewer); each poll is a hardware try_wait,
+// so the bound is well above any real copy.
 constexpr int kMaxPolls = 1 << 22;
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err, int code)
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err, int code, int polls = kMaxPolls)
 {
-    for (int i = 0; i < kMaxPolls; i++)
+    for (int i = 0; i < polls; i++)
         if (mbar_try_wait(bar, parity)) return true;
     if (err) atomicExch(err, code);
     return false;

@@ -22,6 +22,9 @@
 
 #include <stddef.h>
 #include <stdint.h>
+#ifndef __cplusplus
+#include <stdbool.h>
+#endif
 
 #if defined(CTDM_BUILD) && defined(__GNUC__)
 #define CTDM_API __attribute__((visibility("default")))
@@ -109,10 +112,19 @@ CTDM_API ctdm_status ctdm_ctx_read_buffer(ctdm_ctx *ctx, int which, void *host, 
  * are kept; later ones are not recorded. */
 CTDM_API ctdm_status ctdm_ctx_set_timing(ctdm_ctx *ctx, int on);
 CTDM_API ctdm_status ctdm_ctx_stage_times(ctdm_ctx *ctx, double *ms, int *counts, int n);
-/* Status word of the context's bounded device-side waits: 0, or the code of the
- * first wait that ran out since the last read (1: a TMA tile of the positivity
- * loop's z pass did not arrive).  Synchronises the device; reading clears it. */
+/* Status word of the context's bounded device-side waits: 0, or the code of a wait
+ * that ran out since the last read (1: a TMA tile of the positivity loop's dense z
+ * pass did not arrive, 3: one of its packed z pass, 9: ctdm_ctx_probe_wait).
+ * Synchronises the device; reading clears it.  A submitted call that saw a code makes
+ * ctdm_wait return CTDM_ERR_TIMEOUT (and clears it). */
 CTDM_API ctdm_status ctdm_ctx_device_status(ctdm_ctx *ctx, int *status);
+/* Diagnostic (no reference counterpart): one device-side wait that nothing completes,
+ * on an mbarrier with the bounded wait the z pass uses for its TMA tiles, `polls`
+ * polls long (<= 0: that wait's production bound).  The wait runs out, records code 9
+ * in the status word above and the kernel returns (no copy was issued, so none is left
+ * in flight); the context stays usable.  ms (may be NULL) receives the wait's length.
+ * Synchronises the device. */
+CTDM_API ctdm_status ctdm_ctx_probe_wait(ctdm_ctx *ctx, int polls, double *ms);
 /* Number of kernels this library has launched in the process so far (a batch graph
  * launch counts the kernels captured in it). */
 CTDM_API unsigned long long ctdm_launch_count(void);
@@ -146,8 +158,10 @@ CTDM_API ctdm_status ctdm_reconstruct_u8(ctdm_ctx *ctx, const ctdm_params *p, in
  * its volume download beside the next call's loop (the last call's in ctdm_wait); with
  * pageable buffers the copies do not overlap, the results are the same.  A refused call
  * leaves nothing in flight.  Submitted calls share the context's device buffers: until
- * ctdm_wait returns, make no other call on the same context than ctdm_submit (another
- * context serves other work meanwhile).  ctdm_reconstruct* is ctdm_submit + ctdm_wait. */
+ * ctdm_wait returns, the context serves ctdm_submit alone, and its other entry points
+ * (stages, device-buffer reconstructions, buffer reads) return CTDM_ERR_INVALID without
+ * doing anything (another context serves other work meanwhile).  ctdm_reconstruct* is
+ * ctdm_submit + ctdm_wait. */
 CTDM_API ctdm_status ctdm_submit(ctdm_ctx *ctx, const ctdm_params *p, int n_angles, const void *h_holo,
                                  const void *h_bg, int bytes_per_count, const float *h_angx, const float *h_angy,
                                  ctdm_cfloat *h_ri);
@@ -317,13 +331,17 @@ CTDM_API ctdm_status ctdm_contrast_to_ri(int R, const ctdm_cfloat *d_V, double n
  * For callers that cannot allocate device memory: an acquisition loop that must not
  * allocate once it runs, or a host that owns all GPU memory through its own pool.
  * The scratch map and the transform tables are file-scope __device__ arrays of the
- * library (about 16.1 MiB held on every GPU that loads it, until the process exits).
- * Limits: M in {16, 32, 64, 128, 256} and A * M * M <= 4194304 points; larger
- * requests return CTDM_ERR_INVALID with a message in ctdm_last_error().  The first
- * call on a device resolves the arrays' device addresses and fills the tables with
- * synchronous copies, so make it before any stream capture on that device.  All
+ * library (about 16.1 MiB per GPU, held until the process exits).
+ * Limits: M in {16, 32, 64, 128, 256}, A * M * M <= 4194304 points and mode 0 or 1;
+ * other requests return CTDM_ERR_INVALID with a message in ctdm_last_error().  The
+ * first call on a device loads the arrays there (under CUDA's default lazy module
+ * loading that is when their 16.1 MiB is taken, not when the library is opened),
+ * resolves their device addresses and fills the tables with synchronous copies: make
+ * it as a warm-up before a memory pool claims the device's memory, before the loop
+ * that must not allocate starts, and before any stream capture on that device.  All
  * calls share one scratch array, which keeps the last call's contents (nothing in
- * it needs clearing); calls that overlap on the GPU race on it. */
+ * it needs clearing); calls that overlap on the GPU (other streams or threads) race
+ * on it, so serialise them. */
 CTDM_API ctdm_status ctdm_unwrap_dct_noalloc(int A, int M, int mode, const float *d_phi, float *d_out, void *stream);
 /* Unnormalised batched FFT of the library's line lengths.  rank 1..3, dims
  * fastest-first; inverse = 1 uses exp(+i), no scaling. */
@@ -404,6 +422,16 @@ CTDM_API ctdm_status ctdm_run_job(const ctdm_job_file *job, ctdm_job_result *res
 CTDM_API void ctdm_set_recon_globals(int recon_size, double n_med, double wavelength_nm, double camera_pixel_um, double mag,
                             int iter_time, int recon_save, const char *save_dir);
 
+/* cTDM/HilbertTransform.cuh:170 (defined at HilbertTransform.cu:1546) -- host SP/BG
+ * holograms as complex Nx*Ny arrays whose imaginary parts are zero (the reference's job
+ * loop fills them that way; the imaginary parts are not read), Nx == Ny a power of two
+ * of 64..2048.  The M x M fields (M = Nx/4) after the inverse transform, 1/M^2 and the
+ * conjugation go to the device arrays cuSP_FFT / cuBG_FFT (the reference writes its
+ * globals cuSP2 / cuBG2, which its call sites pass as these arguments).  frame == 1
+ * detects the carrier from BG (rows from 600*N/1024, as obtainRadius does at N = 1024)
+ * and keeps it per device for the later frames. */
+CTDM_API void extractQPI_AlgorithmA(ctdm_cfloat *SP, ctdm_cfloat *BG, ctdm_cfloat *cuSP_FFT, ctdm_cfloat *cuBG_FFT, int Nx,
+                                    int Ny, int frame);
 /* cTDM/HilbertTransform.cu:1587 (declared in HilbertTransform.cuh) -- host SP/BG
  * holograms (Nx*Ny float, Nx == Ny), device fields out (Nx/4 * Ny/4).  frame == 1
  * detects the carrier columns (kept per device for the later frames). */
@@ -455,8 +483,9 @@ CTDM_API void HilbertTransform(char *SPDir, char *BGDir, char *AngDir, char *Sav
 /* cTDM/HilbertTransform.cu:2920 -- host N x N angle image (sizeX == sizeY), optics
  * from the last parsed parameter file or the defaults. */
 CTDM_API float AngCal_GPU(float *src, int sizeX, int sizeY, int frame, int totalFrame);
-/* cTDM/HilbertTransform.cu:3056 -- nonzero when the std or range exceeds its limit. */
-CTDM_API int checkArray(float *array2D, float limitSTD, float limitRange, int size);
+/* cTDM/HilbertTransform.cuh:158 (defined at HilbertTransform.cu:3056) -- true when the
+ * standard deviation or the range exceeds its limit (also for NULL or size < 1). */
+CTDM_API bool checkArray(float *array2D, float limitSTD, float limitRange, int size);
 /* cTDM/HilbertTransform.cuh:132 -- host stacks (R*R*frames) and angles (radians);
  * reconstructs with the globals above and writes 3D-RI-*.rimap into SaveDir. */
 CTDM_API void BatchRecon(float *PhaseStack, float *AmpStack, float *sampleAngleRadX, float *sampleAngleRadY, int ReconFrame);

@@ -1096,6 +1096,57 @@ void or_pipeline(const or_params *p, const float *sp, const float *bg, int na, i
     free(ph); free(am); free(U); free(F2); free(C);
 }
 
+/* A whole tomogram as the reference runs it (cTDM/HilbertTransform.cu:963-976 per
+ * frame: QPI Algorithm A, calcWrapPhase, the unwrap; Combine2Stack; BatchRecon
+ * :1825-2047), for the timed CPU baseline: the per-angle chain (QPI A, wrapped phase,
+ * Goldstein residues / cuts / flood fill on the float phase when run_goldstein, DCT
+ * unwrap, resize + crop, median + checkMaps, Rytov spectrum) runs in parallel over the
+ * angles, then the Ewald mapping and the positivity loop.  Same results as
+ * or_pipeline; charges (may be NULL) receive the residue maps (na * M * M). */
+void or_tomogram(const or_params *p, const float *sp, const float *bg, int na, const float *angx, const float *angy,
+                 int run_goldstein, cplx *n_out, int8_t *charges, int *carrier)
+{
+    int n = p->n, m = p->m, r = p->r;
+    int cr = p->carrier_r, cc = p->carrier_c, rad = p->carrier_radius;
+    if (cr < 0 || cc < 0 || rad < 0) or_qpi_carrier(bg, n, &cr, &cc, &rad);
+    if (carrier) { carrier[0] = cr; carrier[1] = cc; carrier[2] = rad; }
+    long mm = (long)m * m, r2 = (long)r * r, r3 = r2 * r;
+    cplx *bgf = (cplx *)malloc(sizeof(cplx) * mm);
+    or_qpi_field(bg, n, m, cr, cc, rad, bgf);
+    cplx *U = (cplx *)malloc(sizeof(cplx) * na * r2);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int a = 0; a < na; a++) {
+        cplx *spf = (cplx *)malloc(sizeof(cplx) * mm);
+        double *ph = (double *)malloc(sizeof(double) * mm), *am = (double *)malloc(sizeof(double) * mm);
+        double *uw = (double *)malloc(sizeof(double) * mm);
+        double *pr = (double *)malloc(sizeof(double) * r2), *ar = (double *)malloc(sizeof(double) * r2);
+        double *pm = (double *)malloc(sizeof(double) * r2), *amd = (double *)malloc(sizeof(double) * r2);
+        or_qpi_field(sp + (long)a * n * n, n, m, cr, cc, rad, spf);
+        or_wrap_phase(spf, bgf, (int)mm, ph, am);
+        if (run_goldstein) {
+            float *phf = (float *)malloc(sizeof(float) * mm), *gout = (float *)malloc(sizeof(float) * mm);
+            int8_t *q = charges ? charges + (long)a * mm : (int8_t *)malloc(mm);
+            uint8_t *cut = (uint8_t *)malloc(mm), *ub = (uint8_t *)malloc(mm);
+            for (long i = 0; i < mm; i++) phf[i] = (float)ph[i];
+            or_goldstein_residues(phf, m, m, q);
+            or_goldstein_cuts(q, m, m, cut);
+            or_goldstein_floodfill(cut, phf, m, m, gout, ub);
+            if (!charges) free(q);
+            free(phf); free(gout); free(cut); free(ub);
+        }
+        or_dct_unwrap(ph, m, m, p->unwrap_mode, uw);
+        or_resize_crop(uw, am, m, m, n, n, r, pr, ar);
+        or_median_check(pr, ar, r, r, pm, amd);
+        or_rytov_spectrum(pm, amd, r, U + a * r2);
+        free(spf); free(ph); free(am); free(uw); free(pr); free(ar); free(pm); free(amd);
+    }
+    cplx *F2 = (cplx *)malloc(sizeof(cplx) * r3);
+    uint32_t *C = (uint32_t *)malloc(sizeof(uint32_t) * r3);
+    or_ewald_map(U, angx, angy, na, r, p->fm0, p->df, p->dx, F2, C);
+    or_positivity(F2, C, r, p->iters, p->k2, p->n_med, p->check_mode, n_out);
+    free(bgf); free(U); free(F2); free(C);
+}
+
 /* ------------------------------------------------------------------------- */
 /* ASD-POCS with total variation (BatchReconPOCS, cTDM/HilbertTransform.cu:    */
 /* 2049-2402; FrquencyInterpolation / FI_kernel / calF and the POCS kernels,   */

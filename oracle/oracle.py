@@ -288,6 +288,22 @@ def pipeline(params, sp, bg, angx, angy, bg_per_angle=False):
     return out, tuple(car)
 
 
+def tomogram(params, sp, bg, angx, angy, run_goldstein=False, want_charges=False):
+    """A whole tomogram (the timed CPU baseline): the per-angle chain in parallel over
+    the angles, Goldstein on every angle when run_goldstein, then the mapping and the
+    loop.  Returns (volume, carrier, charges or None)."""
+    sp, bg = _f32(sp), _f32(bg)
+    angx, angy = _f32(angx), _f32(angy)
+    na = sp.shape[0]
+    r, m = params.r, params.m
+    out = np.zeros((r, r, r), np.complex128)
+    car = (ctypes.c_int * 3)()
+    q = np.zeros((na, m, m), np.int8) if want_charges else None
+    lib().or_tomogram(ctypes.byref(params), _p(sp), _p(bg), na, _p(angx), _p(angy), int(run_goldstein), _p(out),
+                      _p(q) if q is not None else None, car)
+    return out, tuple(car), q
+
+
 # ---- job driver pieces (numpy restatements) ------------------------------------------
 def angcal_peak(img):
     """AngCal_GPU (cTDM/HilbertTransform.cu:2920-2983): flat index of the first maximum

@@ -31,4 +31,6 @@ def main(root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <reference root (the y-h-Lin/cTDM checkout)>")
+    main(sys.argv[1])

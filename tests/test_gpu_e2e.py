@@ -97,3 +97,32 @@ def test_submit_rejects_bad_arguments_and_recovers(ctx, dev):
     ctx.submit(p, h, b, acq.ang_x, acq.ang_y, out)
     ctx.wait()
     assert np.array_equal(out, want)
+
+
+def test_context_refuses_other_calls_while_submissions_are_in_flight(ctx, dev):
+    """Between ctdm_submit and ctdm_wait the context's buffers belong to the calls in
+    flight: any other entry point on that context is refused with a message (and
+    nothing is enqueued), and after ctdm_wait the context serves every call again."""
+    import torch
+    import ctdm_gb300 as C
+    from ctdm_gb300 import _lib, phantom
+    acq = phantom.acquisition(128, 64, 19, seed=41, pixel=0.2e-6, photons=1e4)
+    p = C.params_for(acq, 2)
+    r = acq.r_vol
+    h, b = acq.holograms.astype(np.uint16), acq.background.astype(np.uint16)
+    want = ctx.reconstruct(p, h, b, acq.ang_x, acq.ang_y)
+    out = np.empty((r, r, r), np.complex64)
+    phi = torch.zeros((1, 64, 64), dtype=torch.float32, device=dev)
+    dst = torch.zeros_like(phi)
+    ctx.submit(p, h, b, acq.ang_x, acq.ang_y, out)
+    with pytest.raises(C.CtdmError):
+        ctx.unwrap_dct(phi, dst, 1, 64)
+    assert "in flight" in _lib.last_error()
+    vol = torch.empty((r, r, r), dtype=torch.complex64, device=dev)
+    with pytest.raises(C.CtdmError):
+        ctx.reconstruct_device(p, torch.from_numpy(acq.holograms).to(dev), torch.from_numpy(acq.background).to(dev),
+                               acq.ang_x, acq.ang_y, vol)
+    ctx.wait()
+    assert np.array_equal(out, want)
+    ctx.unwrap_dct(phi, dst, 1, 64)
+    torch.cuda.synchronize()

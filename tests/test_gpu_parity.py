@@ -91,6 +91,36 @@ def test_qpi_matches_oracle(ctx, dev, oracle, n, angles):
         assert rmse(am[a].cpu().numpy(), oam) < 1e-5
 
 
+@pytest.mark.parametrize("n", [256, 1024])
+def test_extract_qpi_algorithm_a_drop_in(ctx, dev, oracle, n):
+    """The reference-named symbol (cTDM/HilbertTransform.cu:1546-1585): host complex
+    holograms with zero imaginary parts in, the conjugated 1/M^2-scaled window fields
+    out on the device; frame 1 detects the carrier from the background and frame 2
+    reuses it."""
+    import ctdm_gb300 as C
+    import torch
+    from ctdm_gb300 import phantom
+    acq = phantom.acquisition(n, n, 2, seed=n + 7, pixel=0.1e-6 * 256 / n)
+    L = C.load()
+    m = n // 4
+    sp_f = torch.zeros((m, m), dtype=torch.complex64, device=dev)
+    bg_f = torch.zeros_like(sp_f)
+    car = oracle.qpi_carrier(acq.background)
+    bg = np.ascontiguousarray(acq.background.astype(np.complex64))
+    for frame in (1, 2):
+        sp = np.ascontiguousarray(acq.holograms[frame - 1].astype(np.complex64))
+        L.extractQPI_AlgorithmA(sp.ctypes.data, bg.ctypes.data, sp_f.data_ptr(), bg_f.data_ptr(), n, n, frame)
+        assert L.ctdm_last_error() == b""
+        osp = oracle.qpi_field(acq.holograms[frame - 1], m, *car)
+        obg = oracle.qpi_field(acq.background, m, *car)
+        scale = np.abs(obg).max()
+        assert rmse(sp_f.cpu().numpy(), osp) / scale < 1e-5
+        assert rmse(bg_f.cpu().numpy(), obg) / scale < 1e-5
+        oph, _ = oracle.wrap_phase(osp, obg)
+        gph, _ = oracle.wrap_phase(sp_f.cpu().numpy(), bg_f.cpu().numpy())
+        assert np.sqrt(np.mean(wrap(gph - oph) ** 2)) < PHASE_TOL
+
+
 def test_qpi_explicit_carrier_and_bg_per_angle(ctx, dev, oracle, small):
     import torch
     acq = small

@@ -109,9 +109,9 @@ def test_frame_check_matches_oracle(lib, oracle, resize_flag):
             assert jobs.check_frame(ph, resize_flag, lim_std, lim_rng) == want
     # the reference-named entry on a plain array
     v = np.array([0, 0, 0, 4], np.float32)
-    assert lib.checkArray(v.ctypes.data, 1.0, 100.0, 4) == 1     # std = sqrt(3) > 1
-    assert lib.checkArray(v.ctypes.data, 2.0, 100.0, 4) == 0
-    assert lib.checkArray(v.ctypes.data, 2.0, 3.5, 4) == 1       # range 4 > 3.5
+    assert lib.checkArray(v.ctypes.data, 1.0, 100.0, 4) is True     # std = sqrt(3) > 1
+    assert lib.checkArray(v.ctypes.data, 2.0, 100.0, 4) is False
+    assert lib.checkArray(v.ctypes.data, 2.0, 3.5, 4) is True       # range 4 > 3.5
 
 
 def test_job_defaults(lib):
