@@ -68,9 +68,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
 
 // Bounded wait for phase `parity` of `bar`.  Returns false (and records `code` in
 // *err when err is given) if the phase has not completed after `polls` polls
-// (kMaxPolls unless a diagnostic asks for fewer); each poll is a hardware try_wait,
-// so the bound is well above any real copy.
-constexpr int kMaxPolls = 1 << 22;
+// (kMaxPolls unless a diagnostic asks for fewer).  Each poll is a hardware try_wait
+// that suspends the thread for a while when the phase is still open: measured on a
+// GB300, 3.8 us per poll, so kMaxPolls gives up after about one second, far above
+// any real tile copy (microseconds).
+constexpr int kMaxPolls = 1 << 18;
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err, int code, int polls = kMaxPolls)
 {
     for (int i = 0; i < polls; i++)
