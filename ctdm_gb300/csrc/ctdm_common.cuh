@@ -6,11 +6,8 @@
 #define CTDM_PI_F 3.14159265358979323846f
 #define CTDM_PI_D 3.14159265358979323846
 
-// Complex add / subtract as one packed two-lane float instruction each (Blackwell's
-// f32x2 arithmetic, sm_100 and later): the same IEEE round-to-nearest results as two
-// scalar operations, in half the issue slots.  a - b is b * -1 + a with one rounding.
-__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 csub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a); }
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
 __device__ __forceinline__ float2 cmul(float2 a, float2 b)
 {
     return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);

@@ -44,19 +44,11 @@ __device__ __forceinline__ void dft2(float2 &a, float2 &b)
 template <bool INV>
 __device__ __forceinline__ void dft4(float2 &a0, float2 &a1, float2 &a2, float2 &a3)
 {
-    // Sums and differences as packed pairs; the two outputs that take the -i (+i)
-    // rotation of d = a1 - a3 are formed component-wise, so the rotation is only a
-    // choice of operands (a packed form would first have to swap d's halves).
-    const float2 t0 = cadd(a0, a2), t1 = csub(a0, a2), t2 = cadd(a1, a3), d = csub(a1, a3);
+    float2 t0 = cadd(a0, a2), t1 = csub(a0, a2), t2 = cadd(a1, a3), t3 = cmul_mi<INV>(csub(a1, a3));
     a0 = cadd(t0, t2);
     a2 = csub(t0, t2);
-    if (INV) {   // t1 + i d, t1 - i d
-        a1 = make_float2(t1.x - d.y, t1.y + d.x);
-        a3 = make_float2(t1.x + d.y, t1.y - d.x);
-    } else {     // t1 - i d, t1 + i d
-        a1 = make_float2(t1.x + d.y, t1.y - d.x);
-        a3 = make_float2(t1.x - d.y, t1.y + d.x);
-    }
+    a1 = cadd(t1, t3);
+    a3 = csub(t1, t3);
 }
 
 // exp(-+ 2 pi i k / 8) for k = 1, 3
@@ -85,43 +77,26 @@ __device__ __forceinline__ void dft8(float2 *a)
     a[3] = cadd(e3, o3); a[7] = csub(e3, o3);
 }
 
-// exp(-+ i theta) * a for theta = 2 pi k / 16 given as (cos, sin).
-template <bool INV>
-__device__ __forceinline__ float2 rot(float2 a, float c, float s)
-{
-    return cmul(a, make_float2(c, INV ? s : -s));
-}
-
 template <bool INV>
 __device__ __forceinline__ void dft16(float2 *a)
 {
-    // 4 x 4: DFT4 over n1 of a[n2 + 4 n1] for each n2, twiddles W16^(n2 k1), DFT4
-    // over n2; X[k1 + 4 k2] ends in slot 4 k1 + k2 and is renamed into place.
-    const float c1 = 0.92387953251128675613f, s1 = 0.38268343236508977173f, h = 0.70710678118654752440f;
+    // cos(2 pi k/16), sin(2 pi k/16), k = 0..7
+    const float c[8] = {1.0f, 0.92387953251128675613f, 0.70710678118654752440f, 0.38268343236508977173f,
+                        0.0f, -0.38268343236508977173f, -0.70710678118654752440f, -0.92387953251128675613f};
+    const float s[8] = {0.0f, 0.38268343236508977173f, 0.70710678118654752440f, 0.92387953251128675613f,
+                        1.0f, 0.92387953251128675613f, 0.70710678118654752440f, 0.38268343236508977173f};
+    float2 e[8], o[8];
 #pragma unroll
-    for (int n2 = 0; n2 < 4; n2++) dft4<INV>(a[n2], a[n2 + 4], a[n2 + 8], a[n2 + 12]);
-    // a[n2 + 4 k1] = Y[n2][k1]
-    a[5] = rot<INV>(a[5], c1, s1);     // W^1
-    a[9] = rot<INV>(a[9], h, h);       // W^2
-    a[13] = rot<INV>(a[13], s1, c1);   // W^3
-    a[6] = rot<INV>(a[6], h, h);       // W^2
-    a[10] = cmul_mi<INV>(a[10]);       // W^4
-    a[14] = rot<INV>(a[14], -h, h);    // W^6
-    a[7] = rot<INV>(a[7], s1, c1);     // W^3
-    a[11] = rot<INV>(a[11], -h, h);    // W^6
-    a[15] = rot<INV>(a[15], -c1, -s1); // W^9
-    float2 y[16];
+    for (int k = 0; k < 8; k++) { e[k] = a[2 * k]; o[k] = a[2 * k + 1]; }
+    dft8<INV>(e);
+    dft8<INV>(o);
 #pragma unroll
-    for (int k1 = 0; k1 < 4; k1++) {
-        float2 b0 = a[4 * k1], b1 = a[4 * k1 + 1], b2 = a[4 * k1 + 2], b3 = a[4 * k1 + 3];
-        dft4<INV>(b0, b1, b2, b3);
-        y[k1] = b0;
-        y[k1 + 4] = b1;
-        y[k1 + 8] = b2;
-        y[k1 + 12] = b3;
+    for (int k = 0; k < 8; k++) {
+        float2 w = make_float2(c[k], INV ? s[k] : -s[k]);
+        float2 t = (k == 0) ? o[k] : cmul(o[k], w);
+        a[k] = cadd(e[k], t);
+        a[k + 8] = csub(e[k], t);
     }
-#pragma unroll
-    for (int k = 0; k < 16; k++) a[k] = y[k];
 }
 
 template <bool INV>
@@ -132,7 +107,7 @@ __device__ __forceinline__ void dft3(float2 *a)
     float2 d = csub(a[1], a[2]);
     // forward: (a1 - a2) * (-i s3); inverse: * (+i s3)
     float2 t2 = INV ? make_float2(-s3 * d.y, s3 * d.x) : make_float2(s3 * d.y, -s3 * d.x);
-    float2 m = __ffma2_rn(t1, make_float2(-0.5f, -0.5f), a[0]);
+    float2 m = make_float2(a[0].x - 0.5f * t1.x, a[0].y - 0.5f * t1.y);
     a[0] = cadd(a[0], t1);
     a[1] = cadd(m, t2);
     a[2] = csub(m, t2);
