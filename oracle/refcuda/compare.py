@@ -1,0 +1,186 @@
+"""The reference's own CUDA pipeline (cuFFT) beside this library on the same seeded
+tomograms, on one GPU: wall time per tomogram and RI error of both against the FP64
+oracle.  COMPARISON INFRASTRUCTURE ONLY.
+
+Needs the sources assembled by oracle/refcuda/assemble.py (oracle/_ref/refcuda/src)
+and nvcc; builds oracle/_ref/refcuda/ref_pipeline with oracle/refcuda/Makefile, then
+for each workload writes the holograms to a file, runs the binary (its wall clock
+covers hologram upload -> RI volume back on the host, as the reference's job loop
+does it), and times this library through its host-buffer entry point
+(ctdm_reconstruct_u16: integer photon counts uploaded as 16-bit, volume downloaded,
+one call at a time) and with the holograms resident in HBM.
+
+    python oracle/refcuda/compare.py [--configs plain_small,wrap_heavy,plain_512] [--reps 3] [--out FILE]
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+REF = os.path.join(os.path.dirname(HERE), "_ref", "refcuda")
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.dirname(HERE))
+
+CONFIGS = {
+    # name: (iterations, run Goldstein in the benchmarked form of this library)
+    "plain_small": (10, False),
+    "wrap_heavy": (20, True),
+    "plain_512": (10, False),
+}
+
+
+def workload(name):
+    """Seeded acquisitions with the benchmark configurations' shapes: 49 x 256^2 -> 256^3;
+    121 x 1024^2 -> 256^2 windows -> 256^3 (RI 1.40, 10 um cell); 181 x 1024^2 on a cone
+    at NA 1.2 -> 512^3 (the differentiable configuration's acquisition, plain method)."""
+    from ctdm_gb300 import phantom
+    if name == "plain_small":
+        return phantom.config_plain_small(seed=1000)
+    if name == "wrap_heavy":
+        return phantom.config_wrap_heavy(seed=1000)
+    return phantom.acquisition(1024, 512, 181, na=1.2, seed=4000)
+
+
+def build():
+    """The Release-flag binary (--use_fast_math, as the reference ships) and an IEEE one."""
+    if not os.path.isdir(os.path.join(REF, "src")):
+        raise SystemExit("oracle/_ref/refcuda/src is missing: run oracle/refcuda/assemble.py <reference root> first")
+    subprocess.check_call(["make", "-s", "-j4", "-C", HERE])
+    subprocess.check_call(["make", "-s", "-j4", "-C", HERE, "VARIANT=ieee"])
+    return {"release": os.path.join(REF, "ref_pipeline"), "ieee": os.path.join(REF, "ieee", "ref_pipeline")}
+
+
+def run_reference(exe, fin, reps, R):
+    with tempfile.TemporaryDirectory() as tmp:
+        fout = os.path.join(tmp, "out.bin")
+        r = subprocess.run([exe, fin, fout, str(reps)], capture_output=True, text=True, timeout=3000)
+        if r.returncode != 0:
+            raise SystemExit(f"ref_pipeline failed ({r.returncode}): {r.stderr[-2000:]}")
+        timing = json.loads(r.stdout.strip().splitlines()[-1])
+        return timing, np.fromfile(fout, np.complex64).reshape(R, R, R)
+
+
+def finite_rmse(a, ref):
+    """RMSE over the voxels where `a` is finite, and the count of the others."""
+    ok = np.isfinite(a.real) & np.isfinite(a.imag)
+    bad = int(ok.size - np.count_nonzero(ok))
+    if not ok.any():
+        return None, bad
+    d = a[ok].astype(np.complex128) - ref[ok]
+    return float(np.sqrt(np.mean(np.abs(d) ** 2))), bad
+
+
+def write_input(path, acq, iters, carrier):
+    with open(path, "wb") as f:
+        f.write(b"CTDMREF1")
+        f.write(np.array([acq.n_holo, acq.r_vol, len(acq.ang_x), iters, *carrier], np.int32).tobytes())
+        f.write(np.array([acq.n_med, acq.wavelength, acq.dx], np.float64).tobytes())
+        f.write(np.ascontiguousarray(acq.ang_x, np.float32).tobytes())
+        f.write(np.ascontiguousarray(acq.ang_y, np.float32).tobytes())
+        f.write(np.ascontiguousarray(acq.background, np.float32).tobytes())
+        f.write(np.ascontiguousarray(acq.holograms, np.float32).tobytes())
+
+
+def rmse(a, b):
+    return float(np.sqrt(np.mean(np.abs(a.astype(np.complex128) - b.astype(np.complex128)) ** 2)))
+
+
+def ours(acq, iters, goldstein, reps):
+    import torch
+    import ctdm_gb300 as C
+    ctx = C.Context(0)
+    dev = torch.device("cuda", 0)
+    r = acq.r_vol
+    out = {}
+    for gold in sorted({False, goldstein}):
+        p = C.params_for(acq, iters, run_goldstein=int(gold))
+        h16, b16 = acq.holograms.astype(np.uint16), acq.background.astype(np.uint16)
+        vol = ctx.reconstruct(p, h16, b16, acq.ang_x, acq.ang_y)          # warm (autotune, buffers)
+        torch.cuda.synchronize()
+        t = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            vol = ctx.reconstruct(p, h16, b16, acq.ang_x, acq.ang_y)
+            t.append((time.perf_counter() - t0) * 1e3)
+        holo, bg = torch.from_numpy(acq.holograms).to(dev), torch.from_numpy(acq.background).to(dev)
+        d = torch.empty((r, r, r), dtype=torch.complex64, device=dev)
+        ctx.reconstruct_device(p, holo, bg, acq.ang_x, acq.ang_y, d)
+        torch.cuda.synchronize()
+        td = []
+        for _ in range(reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            ctx.reconstruct_device(p, holo, bg, acq.ang_x, acq.ang_y, d)
+            b.record()
+            b.synchronize()
+            td.append(a.elapsed_time(b))
+        out["goldstein" if gold else "plain"] = {"host_buffers_ms_mean": float(np.mean(t)),
+                                                 "device_resident_ms_mean": float(np.mean(td)), "volume": vol}
+        del holo, bg, d
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--configs", default="plain_small,wrap_heavy,plain_512")
+    ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--out", default=None)
+    args = ap.parse_args()
+    import oracle as O
+    from ctdm_gb300 import build as cbuild
+    cbuild.build()
+    exes = build()
+    lines = []
+    for name in args.configs.split(","):
+        iters, gold = CONFIGS[name]
+        acq = workload(name)
+        car = O.qpi_carrier(acq.background)
+        R = acq.r_vol
+        refs = {}
+        with tempfile.TemporaryDirectory() as tmp:
+            fin = os.path.join(tmp, "in.bin")
+            write_input(fin, acq, iters, car)
+            for kind, exe in exes.items():
+                refs[kind] = run_reference(exe, fin, args.reps, R)
+        par = O.make_params(acq.n_holo, acq.m_crop, R, iters, acq.fm0, acq.df, acq.dx, acq.k2, acq.n_med)
+        fp64, ocar, _ = O.tomogram(par, acq.holograms, acq.background, acq.ang_x, acq.ang_y)
+        mine = ours(acq, iters, gold, args.reps)
+        plain = mine["plain"]
+        ref_out = {}
+        for kind, (timing, vol) in refs.items():
+            err, bad = finite_rmse(vol, fp64)
+            ref_out[kind] = {"ms_per_tomogram": timing["ms_mean"], "ms_best": timing["ms_best"],
+                             "front_end_ms": timing["front_ms_mean"], "batchrecon_ms": timing["recon_ms_mean"],
+                             "ri_rmse_vs_fp64_finite_voxels": err, "non_finite_voxels": bad,
+                             "non_finite_map_values": timing.get("non_finite_map_values"),
+                             "build": ("nvcc --use_fast_math (the reference's Release flags)" if kind == "release"
+                                       else "nvcc without fast math") + ", cuFFT",
+                             "span": "host holograms -> RI volume on the host"}
+        ieee_vol = refs["ieee"][1]
+        line = {
+            "workload": name, "holograms": f"{len(acq.ang_x)}x{acq.n_holo}^2", "volume": f"{R}^3",
+            "iterations": iters, "carrier": list(car), "reference_cuda": ref_out,
+            "this_library": {k: {"host_buffers_ms": v["host_buffers_ms_mean"],
+                                 "device_resident_ms": v["device_resident_ms_mean"],
+                                 "ri_rmse_vs_fp64": rmse(v["volume"], fp64),
+                                 "ri_rmse_vs_reference_cuda_ieee": finite_rmse(v["volume"], ieee_vol.astype(np.complex128))[0]
+                                 if np.isfinite(ieee_vol).all() else None} for k, v in mine.items()},
+            "speedup_host_buffers_same_work": refs["release"][0]["ms_mean"] / plain["host_buffers_ms_mean"],
+            "reps": args.reps,
+        }
+        print(json.dumps(line))
+        lines.append(line)
+    if args.out:
+        with open(args.out, "w") as f:
+            json.dump(lines, f, indent=1)
+
+
+if __name__ == "__main__":
+    main()
