@@ -15,6 +15,7 @@ see ctdm_gb300.phantom):
          its volume before the next call.
 `--impl reference` times the FP64 CPU implementation of the path on the host
 cores (the reference's path is CUDA; its CPU restatement is the oracle).
+`--config cufft` compares this library's transforms and loop with cuFFT on the same GPU.
 """
 import argparse
 import ctypes
@@ -38,12 +39,13 @@ CONFIGS = {
     "gradient": dict(iterations=10, goldstein=False),
     "gradient_small": dict(iterations=10, goldstein=False),
     "pocs": dict(iterations=10, goldstein=False, angles=121, pocs_iterations=100, tv_steps=20),
+    "cufft": dict(iterations=0, goldstein=False),
 }
 
 
 # Workloads measured on one GPU whatever the launch (the replicated N-GPU contract is the
 # headline workloads'); under torchrun the other ranks exit at once.
-SECONDARY = ("batched", "gradient", "gradient_small", "pocs")
+SECONDARY = ("batched", "gradient", "gradient_small", "pocs", "cufft")
 
 
 def make_workload(name, seed):
@@ -514,6 +516,109 @@ def run_pocs(args):
     print(json.dumps(line))
 
 
+# ---------------------------------------------------------------- cuFFT comparison
+def run_cufft_compare(args):
+    """This library's transforms and positivity loop beside the same work built on cuFFT
+    (through torch.fft, which calls cuFFT; comparison only, never on the product path),
+    same GPU, same run, same data.  Per volume side R: one unnormalised 3-D transform
+    (ctdm_fft's x / y / z line passes against a cuFFT 3-D plan), and one positivity-loop
+    iteration (IFFT3, est_n, modify, FFT3, replacement of the measured voxels): the fused
+    plane / z passes against cuFFT with the point operators as elementwise kernels.  Also
+    the batched 2-D transforms of the front end (the per-angle spectra at 256^2 and the
+    QPI hologram transforms at 1024^2).  Achieved GB/s counts one read and one write of
+    the array per transform (16 bytes per complex point)."""
+    import torch
+    import ctdm_gb300 as C
+    from ctdm_gb300 import build
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    build.build()
+    peak, peak_kind = measured_peaks()
+    ctx = C.Context(local)
+    k2 = float((2 * np.pi * 1.337 / 532e-9) ** 2)
+    n_med = 1.337
+    reps = max(args.steps, 3)
+
+    def timed(fn, n=reps):
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(n):
+            fn()
+        b.record()
+        b.synchronize()
+        return a.elapsed_time(b) / n
+
+    def gbs(nbytes, ms):
+        return nbytes / (ms * 1e-3) / 1e9
+
+    def torch_loop_iteration(G, F2, keep):
+        V = torch.fft.ifftn(G, dim=(0, 1, 2))
+        c = 1.0 - V / k2
+        n = n_med * torch.sqrt(c)                        # principal root
+        n = torch.complex(torch.clamp(n.real, min=n_med), torch.clamp(n.imag, min=0.0))
+        f = (n * n / (n_med * n_med) - 1.0) * (-k2)
+        G2 = torch.fft.fftn(f, dim=(0, 1, 2))
+        return torch.where(keep, F2, G2)
+
+    rows = []
+    for r in (256, 384, 512):
+        rng = np.random.default_rng(r)
+        n3 = r ** 3
+        x = torch.from_numpy((rng.standard_normal((r, r, r)) + 1j * rng.standard_normal((r, r, r)))
+                             .astype(np.complex64)).to(dev)
+        y = torch.empty_like(x)
+        t_ours = timed(lambda: C.fft(x, [r, r, r]))
+        t_cufft = timed(lambda: torch.fft.fftn(x, dim=(0, 1, 2), out=y))
+        # loop iteration: measured data on 5 % of the voxels, ~1e-2 contrast
+        keep_np = rng.random((r, r, r)) < 0.05
+        f2 = np.where(keep_np, (rng.standard_normal((r, r, r)) + 1j * rng.standard_normal((r, r, r))) * 20e-2 * k2,
+                      0).astype(np.complex64)
+        del x, y
+        F2 = torch.from_numpy(f2).to(dev)
+        out = torch.empty_like(F2)
+        keep = torch.from_numpy(keep_np).to(dev)
+        ctx.positivity(F2, r, 2, k2, n_med, out)          # tune / allocate
+        t2 = timed(lambda: ctx.positivity(F2, r, 2, k2, n_med, out))
+        t12 = timed(lambda: ctx.positivity(F2, r, 12, k2, n_med, out))
+        t_ours_iter = (t12 - t2) / 10
+        G = F2.clone()
+        t_torch_iter = timed(lambda: torch_loop_iteration(G, F2, keep))
+        rows.append({"R": r,
+                     "fft3d": {"ctdm_ms": t_ours, "cufft_ms": t_cufft,
+                               "ctdm_gbs": gbs(16.0 * n3, t_ours), "cufft_gbs": gbs(16.0 * n3, t_cufft)},
+                     "loop_iteration": {"ctdm_fused_ms": t_ours_iter, "cufft_elementwise_ms": t_torch_iter,
+                                        "speedup": t_torch_iter / t_ours_iter,
+                                        "loop_scheme": C.loop_scheme(r, device=local)}})
+        del F2, out, keep, G
+        torch.cuda.empty_cache()
+    batched = []
+    for count, n in ((121, 256), (49, 256), (16, 1024)):
+        rng = np.random.default_rng(n + count)
+        x = torch.from_numpy((rng.standard_normal((count, n, n)) + 1j * rng.standard_normal((count, n, n)))
+                             .astype(np.complex64)).to(dev)
+        y = torch.empty_like(x)
+        t_ours = timed(lambda: C.fft(x, [n, n], batch=count))
+        t_cufft = timed(lambda: torch.fft.fft2(x, out=y))
+        batched.append({"batch": count, "side": n, "ctdm_ms": t_ours, "cufft_ms": t_cufft,
+                        "ctdm_gbs": gbs(16.0 * count * n * n, t_ours),
+                        "cufft_gbs": gbs(16.0 * count * n * n, t_cufft)})
+        del x, y
+    line = {
+        "metric": "FFT and positivity-loop time, this library vs cuFFT on the same GPU",
+        "value": None, "unit": "ms", "n_gpus": 1, "steps": reps, "warmup": 2, "higher_is_better": False,
+        "dtype": "c64", "data": "synthetic (seeded random volumes; measured data on 5% of the voxels)",
+        "config": {"workload": "cufft", "parallelism": "one GPU (comparison workload)",
+                   "l2": "volumes of 128 MiB and more (256^3 up)"},
+        "peak_gbs": peak, "peak_source": peak_kind, "volumes": rows, "batched_2d": batched,
+        "cufft": "torch.fft (cuFFT) with torch elementwise kernels; comparison only",
+    }
+    print(json.dumps(line))
+
+
 # ---------------------------------------------------------------- GPU arm
 def run_ours(args):
     import torch
@@ -693,7 +798,7 @@ def run_reference(args):
         print(json.dumps({"impl": "reference", "unavailable": "the reference's BatchReconPOCS is disabled in its "
                           "driver and does not compute a usable reconstruction as written"}))
         return
-    if args.config == "batched" or args.config.startswith("gradient"):
+    if args.config in ("batched", "cufft") or args.config.startswith("gradient"):
         print(json.dumps({"impl": "reference", "unavailable": f"the {args.config} workload has no reference "
                           "counterpart (the reference has one positivity-loop reconstruction per BatchRecon call)"}))
         return
@@ -754,6 +859,8 @@ def main():
         run_gradient(args)
     elif args.config == "pocs":
         run_pocs(args)
+    elif args.config == "cufft":
+        run_cufft_compare(args)
     else:
         run_ours(args)
 
