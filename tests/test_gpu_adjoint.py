@@ -234,3 +234,59 @@ def test_tape_rejects_bad_arguments(ctx, dev):
         C.Tape(F2, 32, 1.0)
     with pytest.raises(RuntimeError, match="unsupported"):
         C.Tape(F2, 48, 1.0)
+
+
+def test_gradient_checks_at_512_on_the_differentiable_configuration(ctx, dev):
+    """The differentiable configuration's own checks at its size: 181 x 1024^2
+    holograms on a cone at NA 1.2 reconstructed into 512^3; the measurement operator
+    built from that tomogram's mapped data; V from 5 TV-regularised FISTA steps
+    (lambda 1e-3).  At that V:
+    * the GPU gradient of 1/2 ||A V - y||^2 + 1e-3 TV(V) equals the FP64 host gradient
+      (relative L2 over the whole volume, and at 64 random voxels);
+    * central differences of the GPU loss (h = 1e-3, real and imaginary parts) at the
+      64 voxels agree with the GPU gradient within 5e-3 of its largest component."""
+    import torch
+    import ctdm_gb300 as C
+    from ctdm_gb300 import phantom
+    r, lam, eps, h = 512, 1e-3, 1e-3, 1e-3
+    acq = phantom.acquisition(1024, r, 181, na=1.2, seed=4000)
+    p = C.params_for(acq, 2)
+    out = torch.empty((r, r, r), dtype=torch.complex64, device=dev)
+    ctx.reconstruct_device(p, T(acq.holograms, dev), T(acq.background, dev), acq.ang_x, acq.ang_y, out)
+    torch.cuda.synchronize()
+    del out
+    f2_ptr, _ = ctx.buffer(7)                     # the mapped data F2 of that call
+    tape = C.Tape(f2_ptr, r, acq.k2)
+    y, idx = tape.data()
+    V = torch.zeros((r, r, r), dtype=torch.complex64, device=dev)
+    tape.reconstruct(V, 5, lam, eps)
+    grad = torch.zeros_like(V)
+    tape.loss_grad(V, grad, lam, eps)
+    torch.cuda.synchronize()
+    g = grad.cpu().numpy()
+    Vh = V.cpu().numpy()
+    # FP64 host gradient at the same V
+    Lr, gr = AD.loss_grad(Vh, idx, y.astype(np.complex128), lam, eps)
+    assert rel(g, gr) < 1e-5
+    rng = np.random.default_rng(512)
+    picks = rng.choice(r ** 3, 64, replace=False)
+    gflat, grflat = g.ravel(), gr.ravel()
+    assert rel(gflat[picks], grflat[picks]) < 1e-4
+    del gr, grflat
+    # central differences of the GPU loss
+    gmax = np.abs(gflat).max()
+    err = []
+    for pk in picks:
+        z, yy, x = np.unravel_index(pk, (r, r, r))
+        for unit, comp in ((1.0, gflat[pk].real), (1j, gflat[pk].imag)):
+            base = V[z, yy, x].item()
+            V[z, yy, x] = base + h * unit
+            Lp = tape.loss_grad(V, grad, lam, eps)
+            V[z, yy, x] = base - h * unit
+            Lm = tape.loss_grad(V, grad, lam, eps)
+            V[z, yy, x] = base
+            err.append((Lp - Lm) / (2 * h) - comp)
+    err = np.abs(np.array(err))
+    print(f"512^3: {idx.size} samples, FD max error {err.max():.3e} of max |g| {gmax:.3e}")
+    assert err.max() <= 5e-3 * gmax
+    tape.close()

@@ -93,3 +93,37 @@ def test_batch_rejects_invalid_job(jobs_and_refs):
         b.plan([jobs[1], tuple(bad)])
     b.close()
     del p
+
+
+def test_batch_of_256_and_384_volumes_matches_single_calls(ctx):
+    """A batch at the batched configuration's sizes (512^2 and 1024^2 holograms, 256^3
+    and 384^3 volumes; few angles to bound the test's time), one job with Goldstein:
+    each volume equals its own single call bit for bit, from the graph and eagerly."""
+    import torch
+    import ctdm_gb300 as C
+    from ctdm_gb300 import phantom
+    dev = torch.device("cuda:0")
+    specs = [(512, 384, 6, 2, 0, 11), (1024, 256, 5, 2, 1, 12), (512, 256, 7, 3, 0, 13), (1024, 384, 4, 2, 0, 14)]
+    jobs, refs = [], []
+    for n, r, a, it, gold, seed in specs:
+        acq = phantom.acquisition(n, r, a, seed=seed, pixel=0.1e-6 * 1024 / n)
+        p = C.params_for(acq, it, run_goldstein=gold)
+        holo = torch.from_numpy(acq.holograms).to(dev)
+        bg = torch.from_numpy(acq.background).to(dev)
+        ref = torch.empty((r, r, r), dtype=torch.complex64, device=dev)
+        ctx.reconstruct_device(p, holo, bg, acq.ang_x, acq.ang_y, ref)
+        jobs.append((p, holo, bg, acq.ang_x, acq.ang_y, torch.zeros_like(ref)))
+        refs.append(ref)
+    torch.cuda.synchronize()
+    b = C.Batch(lanes=2)
+    b.plan(jobs)
+    _check(jobs, refs)
+    _clear(jobs)
+    b.run()
+    _check(jobs, refs)
+    _clear(jobs)
+    b.run_eager()
+    _check(jobs, refs)
+    b.close()
+    del jobs, refs
+    torch.cuda.empty_cache()

@@ -180,7 +180,7 @@ def test_dct_drop_in(ctx, dev, oracle):
 
 
 # ---------------------------------------------------------------- FastUnwrapping
-@pytest.mark.parametrize("m", [32, 64])
+@pytest.mark.parametrize("m", [32, 64, 128, 256])
 def test_fast_unwrap(ctx, dev, oracle, m):
     import torch
     y, x = np.mgrid[0:m, 0:m] / m
