@@ -224,9 +224,12 @@ class Context:
         check(self.lib.ctdm_map_ewald(self.handle, len(angx), r, _ptr(U), _ptr(angx), _ptr(angy), fm0, df, dx,
                                       _ptr(F2), _ptr(counts), _stream(stream)), "ctdm_map_ewald")
 
-    def positivity(self, F2, r, iterations, k2, n_med, out, check_mode=CTDM_CHECK_REF, counts=None, stream=None):
-        check(self.lib.ctdm_positivity(self.handle, r, iterations, check_mode, k2, n_med, _ptr(F2), _ptr(counts),
-                                       _ptr(out), _stream(stream)), "ctdm_positivity")
+    def positivity(self, F2, r, iterations, k2, n_med, out, check_mode=CTDM_CHECK_REF, counts=None, stream=None,
+                   accelerated=False):
+        """The positivity loop from the mapped data F2 into out (octant-shifted RI);
+        accelerated=True adds Nesterov momentum to the projection step (ctdm_positivity_ex)."""
+        check(self.lib.ctdm_positivity_ex(self.handle, r, iterations, check_mode, int(accelerated), k2, n_med, _ptr(F2),
+                                          _ptr(counts), _ptr(out), _stream(stream)), "ctdm_positivity_ex")
 
     def map_fi(self, U, angx, fm0, df, dx, F2, counts=None, stream=None):
         """Frequency-interpolation mapping of the AngX scan (BatchReconPOCS's FI)."""

@@ -21,6 +21,7 @@ class Params(ctypes.Structure):
         ("unwrap_mode", c_int), ("check_mode", c_int), ("unwrap_method", c_int), ("run_goldstein", c_int),
         ("bg_per_angle", c_int), ("carrier_r", c_int), ("carrier_c", c_int), ("carrier_radius", c_int),
         ("n_med", c_double), ("wavelength", c_double), ("dx", c_double), ("qpi_method", c_int),
+        ("accelerated", c_int),
     ]
 
 
@@ -101,6 +102,8 @@ _SIGS = {
                                c_void_p, c_void_p, c_void_p]),
     "ctdm_positivity": (c_int, [c_void_p, c_int, c_int, c_int, c_double, c_double, c_void_p, c_void_p, c_void_p,
                                 c_void_p]),
+    "ctdm_positivity_ex": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_double, c_double, c_void_p, c_void_p,
+                                   c_void_p, c_void_p]),
     "ctdm_fft": (c_int, [c_void_p, c_int, P_int, c_int, c_int, c_void_p]),
     "ctdm_unwrap_dct_noalloc": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p]),
     "ctdm_tape_create": (c_int, [c_int, c_int, c_void_p, c_void_p, c_double, ctypes.POINTER(c_void_p)]),

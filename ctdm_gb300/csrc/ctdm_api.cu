@@ -200,7 +200,7 @@ const float *dct_eigen(int M)
 enum BufId {
     B_PHASE, B_AMP, B_PHU, B_CHG, B_CUT, B_GOLD, B_U, B_F2, B_COUNTS, B_G, B_T1, B_S, B_BGF, B_DCT, B_MASK, B_GEOM,
     B_CARRIER, B_KEY, B_SCRATCH, B_HOLO, B_BG, B_RI, B_GSTATE, B_GLIST, B_GSTATUS, B_FASTW, B_FASTIN, B_TMP, B_GWORK,
-    B_TMASK, B_TCOUNT, B_TVALS, B_QMAG, B_FIT, B_PV, B_PG, B_PV2, B_PG2, B_PVP, B_PPART, B_PCTL, B_PHIST, B_STAGE, B_STAGEBG, B_TPRE, B_RI2, NBUF
+    B_TMASK, B_TCOUNT, B_TVALS, B_QMAG, B_FIT, B_PV, B_PG, B_PV2, B_PG2, B_PVP, B_PPART, B_PCTL, B_PHIST, B_STAGE, B_STAGEBG, B_TPRE, B_RI2, B_XPREV, NBUF
 };
 
 // Stage boundaries recorded with CUDA events when timing is enabled.
@@ -644,8 +644,16 @@ static ctdm_status do_qpi(ctdm_ctx *c, int N, int M, int A, const float *holo, c
     return qpi_angles(c, N, M, A, 0, A, holo, 4, bg_per_angle, phase, amp, s);
 }
 
+// The positivity loop (BatchRecon, cTDM/HilbertTransform.cu:1943-2004), or with
+// accelerated = 1 the same projection step with Nesterov momentum (projected FISTA
+// with the data-replacement step, no regulariser): the pass that applies est_n and
+// modify keeps the projected iterate x_k and sends x_k + beta_k (x_k - x_{k-1}) on,
+// beta_k = (t_{k-1} - 1) / t_k, t_0 = 1, t_k = (1 + sqrt(1 + 4 t_{k-1}^2)) / 2.  It is
+// the gradient form's projected iteration at lambda 0 and unit step, fused into the
+// loop passes (one extra read and write of x per iteration).
 static ctdm_status do_positivity(ctdm_ctx *c, int R, int iters, int check_mode, double k2, double n_med,
-                                 const float2 *F2, const uint8_t *mask, float2 *G, float2 *ri, cudaStream_t s)
+                                 const float2 *F2, const uint8_t *mask, float2 *G, float2 *ri, cudaStream_t s,
+                                 int accelerated = 0)
 {
     LoopArgs la = {};
     la.G = G;
@@ -679,11 +687,24 @@ static ctdm_status do_positivity(ctdm_ctx *c, int R, int iters, int check_mode, 
         la.tvals = B<float2>(c, B_TVALS);
         la.packed = 1;
     }
+    la.xprev = nullptr;
+    la.beta = 0.f;
+    if (accelerated && iters > 0) {
+        CK(ensure(c, B_XPREV, sizeof(float2) * (size_t)R * R * R), "alloc accelerated iterate");
+        la.xprev = B<float2>(c, B_XPREV);
+    }
+    double t_k = 1.0;
+    auto next_beta = [&]() {   // beta of this iteration (0 for the first: x_{-1} is not used)
+        const double t_n = 0.5 * (1.0 + std::sqrt(1.0 + 4.0 * t_k * t_k));
+        la.beta = (float)((t_k - 1.0) / t_n);
+        t_k = t_n;
+    };
     StageTimer &tm = c->timer;
     if (loop_scheme(R) >= 1) {
         // plane + z passes, 8- or 4-CTA clusters per plane (schemes 1, 2; the plane pass
         // records under the x-pass stage)
         for (int it = 0; it < iters; it++) {
+            next_beta();
             CK(launch_plane(la, false, s), "plane pass");
             tm.mark(S_XPASS, s);
             CK(launch_zpass(la, check_mode, s), "z pass");
@@ -696,6 +717,7 @@ static ctdm_status do_positivity(ctdm_ctx *c, int R, int iters, int check_mode, 
     CK(launch_ypass(la, true, s), "y inverse pass");
     tm.mark(S_YINV, s);
     for (int it = 0; it < iters; it++) {
+        next_beta();
         CK(launch_xpass(la, false, s), "x pass");
         tm.mark(S_XPASS, s);
         CK(launch_ypass(la, false, s), "y forward pass");
@@ -784,6 +806,7 @@ static ctdm_status validate(const ctdm_params *p, int A, int &M)
         return invalid("unknown unwrap mode %d", p->unwrap_mode);
     if (p->check_mode != CTDM_CHECK_REF && p->check_mode != CTDM_CHECK_MASK)
         return invalid("unknown check mode %d", p->check_mode);
+    if (p->accelerated != 0 && p->accelerated != 1) return invalid("accelerated must be 0 or 1");
     return CTDM_OK;
 }
 
@@ -941,7 +964,7 @@ static ctdm_status pipeline_core(ctdm_ctx *c, const ctdm_params *p, int A, int M
     if (feed && feed->out_free) CK(cudaStreamWaitEvent(s, feed->out_free, 0), "wait for the volume download");
     st = do_positivity(c, R, p->iterations, p->check_mode, k * k, p->n_med, B<float2>(c, B_F2),
                        mask_mode ? B<uint8_t>(c, B_MASK) : nullptr, B<float2>(c, B_G),
-                       reinterpret_cast<float2 *>(d_ri), s);
+                       reinterpret_cast<float2 *>(d_ri), s, p->accelerated);
     if (st != CTDM_OK) return st;
     if (gold_side) CK(cudaStreamWaitEvent(s, c->join, 0), "join wait");
     return CTDM_OK;
@@ -1484,14 +1507,26 @@ extern "C" ctdm_status ctdm_pocs(ctdm_ctx *c, int R, const ctdm_pocs_params *p, 
     return CTDM_OK;
 }
 
+extern "C" ctdm_status ctdm_positivity_ex(ctdm_ctx *c, int R, int iterations, int check_mode, int accelerated,
+                                          double k2, double n_med, const ctdm_cfloat *d_F2, const uint32_t *d_counts,
+                                          ctdm_cfloat *d_ri, void *stream);
+
 extern "C" ctdm_status ctdm_positivity(ctdm_ctx *c, int R, int iterations, int check_mode, double k2, double n_med,
                                        const ctdm_cfloat *d_F2, const uint32_t *d_counts, ctdm_cfloat *d_ri,
                                        void *stream)
+{
+    return ctdm_positivity_ex(c, R, iterations, check_mode, 0, k2, n_med, d_F2, d_counts, d_ri, stream);
+}
+
+extern "C" ctdm_status ctdm_positivity_ex(ctdm_ctx *c, int R, int iterations, int check_mode, int accelerated,
+                                          double k2, double n_med, const ctdm_cfloat *d_F2, const uint32_t *d_counts,
+                                          ctdm_cfloat *d_ri, void *stream)
 {
     if (!c || !d_F2 || !d_ri) return invalid("ctdm_positivity: NULL argument");
     if (in_flight(c))
         return invalid("ctdm_positivity: calls submitted on this context are still in flight (ctdm_wait first)");
     if (!ok_volume(R) || iterations < 0) return invalid("ctdm_positivity: size unsupported");
+    if (accelerated != 0 && accelerated != 1) return invalid("ctdm_positivity: accelerated must be 0 or 1");
     if (check_mode == CTDM_CHECK_MASK && !d_counts) return invalid("ctdm_positivity: mask mode needs counts");
     CK(cudaSetDevice(c->device), "cudaSetDevice");
     cudaStream_t s = (cudaStream_t)stream;
@@ -1508,7 +1543,7 @@ extern "C" ctdm_status ctdm_positivity(ctdm_ctx *c, int R, int iterations, int c
     }
     c->timer.start(s);
     return do_positivity(c, R, iterations, check_mode, k2, n_med, reinterpret_cast<const float2 *>(d_F2), mask, G,
-                         reinterpret_cast<float2 *>(d_ri), s);
+                         reinterpret_cast<float2 *>(d_ri), s, accelerated);
 }
 
 extern "C" ctdm_status ctdm_fft(ctdm_cfloat *d_data, int rank, const int *dims, int batch, int inverse, void *stream)

@@ -64,6 +64,11 @@ struct LoopArgs {
     const int *tprefix;     // tprefix[tile * R + z]: kept samples of the tile before row z
     const float2 *tvals;
     int packed;
+    // accelerated loop (projected FISTA): the pass that applies est_n and modify keeps
+    // the projected iterate x_k in xprev and sends w_k = x_k + beta (x_k - x_{k-1}) on
+    // to the forward transform; xprev == nullptr: the plain loop
+    float2 *xprev;
+    float beta;
 };
 
 // Packs F2 (mode 0: re != 0 && im != 0; mode 1: mask != 0) into per-tile masks,

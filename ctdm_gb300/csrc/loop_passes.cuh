@@ -46,7 +46,7 @@ static cudaError_t prep_plan_kernel(K kernel, int L, size_t smem)
 // its first-stage points straight from HBM (unit stride across the warp), the
 // inverse transform ends in registers, the point operators run on the registers,
 // and the forward transform in the reversed radix order stores straight back.
-template <class P, bool FINAL>
+template <class P, bool FINAL, bool MOM = false>
 __global__ void __launch_bounds__(P::THREADS, fftl::plan_min_ctas<P>(4)) xpass_kernel(LoopArgs a,
                                                                                       const float2 *__restrict__ tw)
 {
@@ -72,6 +72,16 @@ __global__ void __launch_bounds__(P::THREADS, fftl::plan_min_ctas<P>(4)) xpass_k
     } else {
 #pragma unroll
         for (int i = 0; i < P::E; i++) v[i] = modify_f_scaled(est_n_scaled(v[i], a.s1, a.n_med), a.s2, a.k2);
+        if constexpr (MOM) {
+            float2 *xp = a.xprev + l * L;
+#pragma unroll
+            for (int i = 0; i < P::E; i++) {
+                const int o = fftl::slot_pos<L, P::T, P::RV0>(i, t);
+                const float2 prev = xp[o];
+                xp[o] = v[i];
+                v[i] = momentum_step(v[i], prev, a.beta);
+            }
+        }
         P::template seqr_row<false>(buf, v, tw);
         float2 *dst = a.G + l * L;
 #pragma unroll
@@ -262,7 +272,8 @@ static cudaError_t run_loop_pass(int kind, const LoopArgs &a, int flag, cudaStre
     cudaError_t e;
     if (kind == LOOP_X || kind == LOOP_X_FINAL) {
         const size_t smem = fftl::plan_smem_row<P>();
-        auto k = kind == LOOP_X_FINAL ? xpass_kernel<P, true> : xpass_kernel<P, false>;
+        auto k = kind == LOOP_X_FINAL ? xpass_kernel<P, true>
+                                      : (a.xprev ? xpass_kernel<P, false, true> : xpass_kernel<P, false>);
         e = prep_plan_kernel(k, L, smem);
         if (e != cudaSuccess) return e;
         k<<<grid, P::THREADS, smem, s>>>(a, twiddles(L));

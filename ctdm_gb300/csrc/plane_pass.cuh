@@ -36,7 +36,8 @@ struct PlaneCfg {
 
 // MINB: resident CTAs per SM the register allocation aims for (3: no spills at
 // R = 256; 4: more latency hiding for some spill traffic).  C: CTAs per plane.
-template <int L, int C, int MINB, bool FINAL>
+// MOM: the accelerated loop (momentum on the projected iterate, LoopArgs::xprev).
+template <int L, int C, int MINB, bool FINAL, bool MOM = false>
 __global__ void __launch_bounds__(fftl::Plan<L>::THREADS, MINB) plane_kernel(LoopArgs a, const float2 *__restrict__ tw)
 {
     namespace cg = cooperative_groups;
@@ -89,6 +90,16 @@ __global__ void __launch_bounds__(fftl::Plan<L>::THREADS, MINB) plane_kernel(Loo
             } else {
 #pragma unroll
                 for (int i = 0; i < P::E; i++) v[i] = modify_f_scaled(est_n_scaled(v[i], a.s1, a.n_med), a.s2, a.k2);
+                if constexpr (MOM) {
+                    float2 *xp = a.xprev + (long)z * L * L + x;
+#pragma unroll
+                    for (int i = 0; i < P::E; i++) {
+                        const long o = (long)L * fftl::slot_pos<L, P::T, P::RV0>(i, t);
+                        const float2 prev = xp[o];
+                        xp[o] = v[i];
+                        v[i] = momentum_step(v[i], prev, a.beta);
+                    }
+                }
                 P::template seqr<false, false, false>(scr, v, tw);
 #pragma unroll
                 for (int i = 0; i < P::E; i++) __stcg(&col[(long)fftl::slot_pos<L, P::T, P::F0>(i, t) * L], v[i]);
@@ -119,7 +130,8 @@ template <int L, int C, int MINB>
 static cudaError_t run_plane_pass(const LoopArgs &a, bool final_pass, cudaStream_t s)
 {
     using Cfg = PlaneCfg<L, C>;
-    auto k = final_pass ? plane_kernel<L, C, MINB, true> : plane_kernel<L, C, MINB, false>;
+    auto k = final_pass ? plane_kernel<L, C, MINB, true>
+                        : (a.xprev ? plane_kernel<L, C, MINB, false, true> : plane_kernel<L, C, MINB, false>);
     if (!twiddles(L)) return cudaErrorInitializationError;
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);

@@ -61,6 +61,12 @@ __device__ __forceinline__ float2 modify_f_scaled(float2 n, float s2, float k2)
     return make_float2(fmaf(n.x * n.x - n.y * n.y, s2, k2), 2.0f * n.x * n.y * s2);
 }
 
+// Nesterov momentum on the projected iterate: w = x + beta (x - x_prev).
+__device__ __forceinline__ float2 momentum_step(float2 x, float2 prev, float beta)
+{
+    return make_float2(fmaf(beta, x.x - prev.x, x.x), fmaf(beta, x.y - prev.y, x.y));
+}
+
 // Modify_F3D (cTDM/Recon_kernel.cu:370-383), called with n_med^2.
 __device__ __forceinline__ float2 modify_f(float2 n, float k2, float nm2)
 {

@@ -84,6 +84,8 @@ typedef struct {
     double wavelength;   /* vacuum wavelength (m) */
     double dx;           /* reconstruction voxel (m) */
     int qpi_method;      /* reference QPI_Method numbering: CTDM_QPI_B (0) or CTDM_QPI_A (1, default) */
+    int accelerated;     /* 0: the reference's positivity loop; 1: the same projection step with
+                            Nesterov momentum (see ctdm_positivity_ex); no reference counterpart */
 } ctdm_params;
 
 /* Default parameters (reference defaults where they exist). */
@@ -266,6 +268,17 @@ CTDM_API ctdm_status ctdm_map_ewald(ctdm_ctx *ctx, int A, int R, const ctdm_cflo
  * d_counts required for CTDM_CHECK_MASK (else may be NULL). */
 CTDM_API ctdm_status ctdm_positivity(ctdm_ctx *ctx, int R, int iterations, int check_mode, double k2, double n_med,
                             const ctdm_cfloat *d_F2, const uint32_t *d_counts, ctdm_cfloat *d_ri, void *stream);
+/* The same loop with accelerated = 1 (no reference counterpart): projected FISTA at
+ * lambda 0 and unit step, fused into the loop passes.  The pass that applies est_n and
+ * modify keeps the projected iterate x_k and sends x_k + beta_k (x_k - x_{k-1}) to the
+ * forward transform, beta_k = (t_{k-1} - 1) / t_k, t_0 = 1,
+ * t_k = (1 + sqrt(1 + 4 t_{k-1}^2)) / 2 (beta_1 = 0); the output is the RI of the next
+ * projected iterate.  It is ctdm_reconstruct_gradient_ex(positivity = 1, lambda = 0,
+ * step = 1) run with iterations + 1 steps, at one extra read and write of R^3 values
+ * per iteration.  accelerated = 0 is ctdm_positivity. */
+CTDM_API ctdm_status ctdm_positivity_ex(ctdm_ctx *ctx, int R, int iterations, int check_mode, int accelerated,
+                                        double k2, double n_med, const ctdm_cfloat *d_F2, const uint32_t *d_counts,
+                                        ctdm_cfloat *d_ri, void *stream);
 /* --- ASD-POCS with total variation (BatchReconPOCS, cTDM/HilbertTransform.cu:2049-2402,
  * cTDM/Recon_kernel.cu:414-1106, with its mathematics fixed) -------------------------
  * Frequency-interpolation mapping: like ctdm_map_ewald for a one-axis scan of tilts

@@ -290,3 +290,43 @@ def test_gradient_checks_at_512_on_the_differentiable_configuration(ctx, dev):
     print(f"512^3: {idx.size} samples, FD max error {err.max():.3e} of max |g| {gmax:.3e}")
     assert err.max() <= 5e-3 * gmax
     tape.close()
+
+
+@pytest.mark.parametrize("r,iters", [(64, 6), (256, 4)])
+def test_accelerated_loop_is_projected_fista(ctx, dev, r, iters):
+    """The accelerated positivity loop (momentum fused into the loop passes; 256^3 runs
+    the plane scheme, 64^3 the line passes) equals projected FISTA at lambda 0 and unit
+    step with one more step (FP64 restatement, and the library's own gradient driver),
+    RI RMSE <= 1e-5; and differs from the plain loop."""
+    import torch
+    import ctdm_gb300 as C
+    k2 = float((2 * np.pi * 1.337 / 532e-9) ** 2)
+    n_med = 1.337
+    rng = np.random.default_rng(r + iters)
+    keep = rng.random((r, r, r)) < 0.15
+    amp = 1e-2 * k2 * np.sqrt(r ** 3 / 0.15)
+    F2 = np.where(keep, (rng.standard_normal((r, r, r)) + 1j * rng.standard_normal((r, r, r))) * amp, 0)
+    F2 = F2.astype(np.complex64)
+    dF2 = T(F2, dev)
+    out = torch.empty_like(dF2)
+    ctx.positivity(dF2, r, iters, k2, n_med, out, accelerated=True)
+    plain = torch.empty_like(dF2)
+    ctx.positivity(dF2, r, iters, k2, n_med, plain)
+    torch.cuda.synchronize()
+    got = out.cpu().numpy()
+    idx = AD.measured_indices(F2)
+    y = AD.tape_data(F2, idx, r, k2)
+    V, _ = AD.fista(np.zeros((r, r, r), np.complex64), idx, y, iters + 1, 0.0, 1.0, step=1.0, positivity=True)
+    ref = AD.contrast_to_ri(V, n_med, clamp=True)
+    err = np.sqrt(np.mean(np.abs(got.astype(np.complex128) - ref) ** 2))
+    assert err < 1e-5, err
+    tape = C.Tape(dF2, r, k2)
+    Vg = torch.zeros((r, r, r), dtype=torch.complex64, device=dev)
+    tape.reconstruct(Vg, iters + 1, 0.0, 1.0, step=1.0, positivity=True)
+    ng = torch.empty_like(Vg)
+    C.contrast_to_ri(Vg, r, n_med, ng, clamp=True)
+    torch.cuda.synchronize()
+    assert np.sqrt(np.mean(np.abs(ng.cpu().numpy().astype(np.complex128) - ref) ** 2)) < 1e-5
+    diff = np.sqrt(np.mean(np.abs(plain.cpu().numpy().astype(np.complex128) - ref) ** 2))
+    assert diff > 10 * err        # momentum changes the iterates
+    tape.close()
