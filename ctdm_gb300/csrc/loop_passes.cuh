@@ -56,6 +56,11 @@ __global__ void __launch_bounds__(P::THREADS, fftl::plan_min_ctas<P>(4)) xpass_k
     const int t = threadIdx.x % P::T, b = threadIdx.x / P::T;
     const long l = (long)blockIdx.x * P::B + b;   // row y + L z (the grid covers the L^2 rows exactly)
     const float2 *src = a.G + l * L;
+    if constexpr (MOM && !FINAL) {
+        // the previous iterate of this row comes from HBM during the inverse transform
+#pragma unroll
+        for (int i = 0; i < P::E; i++) prefetch_l2(a.xprev + l * L + fftl::slot_pos<L, P::T, P::RV0>(i, t));
+    }
     float2 v[P::E];
 #pragma unroll
     for (int i = 0; i < P::E; i++) v[i] = __ldcs(&src[fftl::slot_pos<L, P::T, P::F0>(i, t)]);

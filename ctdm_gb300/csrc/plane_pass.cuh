@@ -75,6 +75,12 @@ __global__ void __launch_bounds__(fftl::Plan<L>::THREADS, MINB) plane_kernel(Loo
         for (int sb = 0; sb < Cfg::SB; sb++) {
             const int x = rank * RL + sb * P::B + b;
             float2 *col = plane + x;
+            if constexpr (MOM && !FINAL) {
+                // the previous iterate of these columns comes from HBM during the transform
+                const float2 *xp = a.xprev + (long)z * L * L + x;
+#pragma unroll
+                for (int i = 0; i < P::E; i++) prefetch_l2(xp + (long)L * fftl::slot_pos<L, P::T, P::RV0>(i, t));
+            }
             float2 v[P::E];
 #pragma unroll
             for (int i = 0; i < P::E; i++) v[i] = __ldcg(&col[(long)fftl::slot_pos<L, P::T, P::F0>(i, t) * L]);

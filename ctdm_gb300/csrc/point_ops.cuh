@@ -61,6 +61,13 @@ __device__ __forceinline__ float2 modify_f_scaled(float2 n, float s2, float k2)
     return make_float2(fmaf(n.x * n.x - n.y * n.y, s2, k2), 2.0f * n.x * n.y * s2);
 }
 
+// Brings the line containing p towards L2 without holding a register for the data
+// (the accelerated loop's previous iterate, read after the transforms that follow).
+__device__ __forceinline__ void prefetch_l2(const void *p)
+{
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 // Nesterov momentum on the projected iterate: w = x + beta (x - x_prev).
 __device__ __forceinline__ float2 momentum_step(float2 x, float2 prev, float beta)
 {
