@@ -144,6 +144,12 @@ class Context:
         check(self.lib.ctdm_ctx_stage_times(self.handle, ms, cnt, n), "ctdm_ctx_stage_times")
         return {name: (ms[i], cnt[i]) for i, name in enumerate(self.STAGES)}
 
+    def workspace(self):
+        """Device bytes this context's workspace holds now."""
+        b = ctypes.c_size_t()
+        check(self.lib.ctdm_ctx_workspace(self.handle, ctypes.byref(b)), "ctdm_ctx_workspace")
+        return b.value
+
     def device_status(self):
         """Status word of the bounded device-side waits (0 = none ran out); clears it."""
         st = ctypes.c_int()
@@ -263,6 +269,13 @@ def launch_count():
     return int(load().ctdm_launch_count())
 
 
+def workspace_bytes(params, n_angles):
+    """Upper bound of a context's device memory for one device-buffer reconstruction."""
+    b = ctypes.c_size_t()
+    check(load().ctdm_workspace_bytes(ctypes.byref(params), int(n_angles), ctypes.byref(b)), "ctdm_workspace_bytes")
+    return b.value
+
+
 def fft(data, dims, batch=1, inverse=False, stream=None):
     """Unnormalised in-place FFT of a device buffer (dims fastest-first)."""
     d = (ctypes.c_int * len(dims))(*dims)
@@ -350,6 +363,17 @@ class Batch:
 
     def run_eager(self, stream=None):
         check(self.lib.ctdm_batch_run_eager(self.handle, _stream(stream)), "ctdm_batch_run_eager")
+
+    def set_memory_limit(self, nbytes):
+        """Cap the device memory the next plan may give its lanes (0: free memory alone)."""
+        check(self.lib.ctdm_batch_set_memory_limit(self.handle, int(nbytes)), "ctdm_batch_set_memory_limit")
+
+    def admission(self):
+        """(lanes used, workspace bound per lane, bytes available) of the last plan."""
+        n, per, avail = ctypes.c_int(), ctypes.c_size_t(), ctypes.c_size_t()
+        check(self.lib.ctdm_batch_admission(self.handle, ctypes.byref(n), ctypes.byref(per), ctypes.byref(avail)),
+              "ctdm_batch_admission")
+        return n.value, per.value, avail.value
 
     def lanes(self):
         out = (ctypes.c_int * self.n_jobs)()

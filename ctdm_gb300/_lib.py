@@ -124,6 +124,10 @@ _SIGS = {
     "ctdm_batch_run": (c_int, [c_void_p, c_void_p]),
     "ctdm_batch_run_eager": (c_int, [c_void_p, c_void_p]),
     "ctdm_batch_lanes": (c_int, [c_void_p, P_int, c_int]),
+    "ctdm_batch_set_memory_limit": (c_int, [c_void_p, c_size_t]),
+    "ctdm_batch_admission": (c_int, [c_void_p, P_int, ctypes.POINTER(c_size_t), ctypes.POINTER(c_size_t)]),
+    "ctdm_workspace_bytes": (c_int, [ctypes.POINTER(Params), c_int, ctypes.POINTER(c_size_t)]),
+    "ctdm_ctx_workspace": (c_int, [c_void_p, ctypes.POINTER(c_size_t)]),
     "ctdm_plan_count": (c_int, [c_int]),
     "ctdm_autotune": (c_int, [c_int, c_int, c_int, P_int, ctypes.POINTER(c_double), c_int]),
     "ctdm_plans": (c_int, [c_int, c_int, P_int, P_int]),

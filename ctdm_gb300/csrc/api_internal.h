@@ -10,6 +10,11 @@
 namespace ctdm {
 // Parameter checks of the whole path; M receives the window side.
 ctdm_status validate_params(const ctdm_params *p, int A, int &M);
+// Upper bound of the device bytes a context holds for one device-buffer reconstruction.
+size_t workspace_bytes(const ctdm_params *p, int A, int M);
+// Device bytes a context holds now; release_workspace frees them (device idle first).
+size_t held_bytes(const ctdm_ctx *c);
+void release_workspace(ctdm_ctx *c);
 // The whole path on stream s with device-resident angle geometry (A entries).
 // Capture-safe once the context's workspace has grown to the call's sizes.
 ctdm_status run_pipeline(ctdm_ctx *c, const ctdm_params *p, int A, const float *d_holo, const float *d_bg,

@@ -12,12 +12,21 @@
 // Goldstein, Ewald mapping) of the others, and the graph removes the per-kernel
 // launch gaps of the ~5 R^3-sized passes per iteration.
 //
+// Admission by free HBM.  Before planning, each job's workspace is bounded
+// (workspace_bytes), and the batch uses only as many lanes as fit beside each other in
+// the device memory that is free plus what the lanes already hold (capped by
+// ctdm_batch_set_memory_limit), keeping back room for the autotuner's scratch volumes.
+// A batch whose largest job does not fit alone is refused before anything is
+// allocated.  The reference makes the same decision for its one volume from free device
+// memory (ReconMode, cTDM/HilbertTransform.cu:1932-1939).
+//
 // Planning runs every job once eagerly (growing each lane's workspace to its
 // largest job and validating everything), then captures the same launch sequence.
 // The graph keeps the job pointers it was planned with: to reconstruct new data,
 // write it into the same input buffers and launch again.
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <vector>
 
 #include "api_internal.h"
@@ -39,6 +48,9 @@ struct ctdm_batch {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     unsigned long long graph_kernels = 0;   // kernel launches captured into the graph
+    size_t mem_limit = 0;                   // 0: free device memory decides alone
+    int active = 0;                         // lanes admitted by the last plan
+    size_t lane_bytes = 0, avail_bytes = 0; // largest job's workspace; memory the plan could use
 };
 
 #define BK(x, what)                                          \
@@ -158,6 +170,35 @@ extern "C" ctdm_status ctdm_batch_plan(ctdm_batch *b, const ctdm_job *jobs, int 
         if (!jb.d_holo || !jb.d_bg || !jb.h_angx || !jb.h_angy || !jb.d_ri)
             return fail_invalid("ctdm_batch_plan: a job has a NULL pointer");
     }
+    // admission: lanes whose workspaces fit beside each other in the available memory
+    size_t w_max = 0, r_max = 0;
+    for (int j = 0; j < n_jobs; j++) {
+        int M;
+        validate_params(&jobs[j].params, jobs[j].n_angles, M);
+        w_max = std::max(w_max, workspace_bytes(&jobs[j].params, jobs[j].n_angles, M));
+        r_max = std::max(r_max, (size_t)jobs[j].params.r_vol);
+    }
+    size_t held = 0;
+    for (ctdm_ctx *c : b->ctx) held += held_bytes(c);
+    size_t free_b = 0, total_b = 0;
+    BK(cudaMemGetInfo(&free_b, &total_b), "free device memory");
+    size_t avail = free_b + held;
+    if (b->mem_limit && b->mem_limit < avail) avail = b->mem_limit;
+    const size_t margin = 24 * r_max * r_max * r_max + (256ull << 20);   // tuner scratch volumes, plan state
+    const size_t fit = avail > margin ? (avail - margin) / w_max : 0;
+    b->lane_bytes = w_max;
+    b->avail_bytes = avail;
+    b->active = (int)std::min<size_t>((size_t)b->lanes, fit);
+    if (b->active < 1) {
+        char msg[256];
+        snprintf(msg, sizeof msg,
+                 "ctdm_batch_plan: the largest job needs %.2f GB of workspace (+ %.2f GB reserve), %.2f GB available",
+                 w_max / 1e9, margin / 1e9, avail / 1e9);
+        ctdm_status st = fail_invalid(msg);
+        (void)st;
+        return CTDM_ERR_NOMEM;
+    }
+    for (int l = b->active; l < b->lanes; l++) release_workspace(b->ctx[l]);
     b->jobs.assign(jobs, jobs + n_jobs);
     // geometry per job (device, owned by the plan)
     for (int j = 0; j < n_jobs; j++) {
@@ -175,7 +216,7 @@ extern "C" ctdm_status ctdm_batch_plan(ctdm_batch *b, const ctdm_job *jobs, int 
     for (int j = 0; j < n_jobs; j++) idx[j] = j;
     std::stable_sort(idx.begin(), idx.end(),
                      [&](int x, int y) { return job_bytes(b->jobs[x]) > job_bytes(b->jobs[y]); });
-    std::vector<double> load(b->lanes, 0.0);
+    std::vector<double> load(b->active, 0.0);
     b->lane_of.assign(n_jobs, 0);
     for (int j : idx) {
         const int l = (int)(std::min_element(load.begin(), load.end()) - load.begin());
@@ -224,6 +265,25 @@ extern "C" ctdm_status ctdm_batch_run_eager(ctdm_batch *b, void *stream)
     ctdm_status st = issue(b, (cudaStream_t)stream);
     if (st == CTDM_OK) clear_error();
     return st;
+}
+
+extern "C" ctdm_status ctdm_batch_set_memory_limit(ctdm_batch *b, size_t bytes)
+{
+    if (!b) return fail_invalid("ctdm_batch_set_memory_limit: NULL batch");
+    b->mem_limit = bytes;
+    clear_error();
+    return CTDM_OK;
+}
+
+extern "C" ctdm_status ctdm_batch_admission(const ctdm_batch *b, int *lanes_used, size_t *bytes_per_lane,
+                                            size_t *bytes_available)
+{
+    if (!b || b->active < 1) return fail_invalid("ctdm_batch_admission: no plan");
+    if (lanes_used) *lanes_used = b->active;
+    if (bytes_per_lane) *bytes_per_lane = b->lane_bytes;
+    if (bytes_available) *bytes_available = b->avail_bytes;
+    clear_error();
+    return CTDM_OK;
 }
 
 extern "C" ctdm_status ctdm_batch_lanes(const ctdm_batch *b, int *lane_of_job, int n_jobs)

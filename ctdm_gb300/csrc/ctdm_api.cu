@@ -458,6 +458,25 @@ extern "C" ctdm_status ctdm_ctx_device_status(ctdm_ctx *c, int *status)
     return CTDM_OK;
 }
 
+extern "C" ctdm_status ctdm_workspace_bytes(const ctdm_params *p, int n_angles, size_t *bytes)
+{
+    if (!p || !bytes) return invalid("ctdm_workspace_bytes: NULL argument");
+    int M = 0;
+    ctdm_status st = validate_params(p, n_angles, M);
+    if (st != CTDM_OK) return st;
+    *bytes = workspace_bytes(p, n_angles, M);
+    g_err.clear();
+    return CTDM_OK;
+}
+
+extern "C" ctdm_status ctdm_ctx_workspace(ctdm_ctx *c, size_t *bytes)
+{
+    if (!c || !bytes) return invalid("ctdm_ctx_workspace: NULL argument");
+    *bytes = held_bytes(c);
+    g_err.clear();
+    return CTDM_OK;
+}
+
 // One bounded device-side wait that nothing completes, recorded as code 9 in the
 // context's status word (see the header).
 extern "C" ctdm_status ctdm_ctx_probe_wait(ctdm_ctx *c, int polls, double *ms)
@@ -1007,6 +1026,45 @@ extern "C" ctdm_status ctdm_reconstruct_device(ctdm_ctx *c, const ctdm_params *p
 // ---------------------------------------------------------------- internal interface (batch scheduler)
 namespace ctdm {
 ctdm_status validate_params(const ctdm_params *p, int A, int &M) { return validate(p, A, M); }
+
+// Device bytes a context holds after a device-buffer reconstruction of this job: an
+// upper bound of what pipeline_core and do_positivity allocate (the buffers of the
+// front end, the volumes of the loop, the packed measured samples at the finest tile,
+// the accelerated iterate).  The reference sizes its single reconstruction the same
+// way from free device memory (ReconMode, cTDM/HilbertTransform.cu:1932-1939).
+size_t workspace_bytes(const ctdm_params *p, int A, int M)
+{
+    const size_t N = (size_t)p->n_holo, R = (size_t)p->r_vol, mm = (size_t)M * M, rr = R * R, r3 = rr * R;
+    size_t b = 16 * (size_t)A * mm;                          // phase, amplitude, unwrapped, DCT scratch
+    b += 8 * (size_t)A * rr;                                 // per-angle spectra
+    b += 16 * r3;                                            // F2, G
+    if (p->check_mode == CTDM_CHECK_MASK) b += 5 * r3;       // hit counts, hit mask
+    if (p->run_goldstein || p->unwrap_method == CTDM_METHOD_GOLDSTEIN)
+        b += (size_t)A * mm * (1 + 1 + 4 + 1 + 20 + 1) + 4 * (size_t)A;   // charges, cuts, out, state, lists, work
+    if (p->unwrap_method == CTDM_METHOD_FAST) b += 4 * (size_t)A * mm + 96 * mm;
+    const size_t chunk = (size_t)qpi_chunk((int)N, M, A);
+    b += chunk * N * M * 8 + chunk * mm * 8 + (p->bg_per_angle ? (size_t)A : 1) * mm * 8 + N * N * 8 + 64;
+    if (p->qpi_method == CTDM_QPI_B) b += N * N + N * N * 2;          // column histogram scratch, window rows
+    b += 9 * r3 + 4 * rr;                                    // packed samples, masks, prefixes (tiles of >= 8)
+    if (p->accelerated && p->iterations > 0) b += 8 * r3;    // the accelerated loop's iterate
+    b += sizeof(AngleGeom) * (size_t)A + 4096;
+    return b;
+}
+
+size_t held_bytes(const ctdm_ctx *c)
+{
+    size_t b = 0;
+    for (int i = 0; i < NBUF; i++) b += c->cap[i];
+    return b;
+}
+
+// Frees every workspace buffer of c once the device is idle (a lane left out of a plan).
+void release_workspace(ctdm_ctx *c)
+{
+    cudaSetDevice(c->device);
+    cudaDeviceSynchronize();
+    for (int i = 0; i < NBUF; i++) ensure(c, i, 0);
+}
 ctdm_status run_pipeline(ctdm_ctx *c, const ctdm_params *p, int A, const float *d_holo, const float *d_bg,
                          const AngleGeom *d_geom, ctdm_cfloat *d_ri, cudaStream_t s)
 {

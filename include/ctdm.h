@@ -90,6 +90,11 @@ typedef struct {
 
 /* Default parameters (reference defaults where they exist). */
 CTDM_API void ctdm_params_default(ctdm_params *p);
+/* Upper bound of the device memory a context holds for one device-buffer reconstruction
+ * of this job (ctdm_reconstruct_device; host-buffer calls add the uploaded holograms and
+ * two volumes), for a caller's own admission of tomograms by free memory.  No reference
+ * counterpart. */
+CTDM_API ctdm_status ctdm_workspace_bytes(const ctdm_params *p, int n_angles, size_t *bytes);
 
 CTDM_API const char *ctdm_last_error(void);
 CTDM_API const char *ctdm_version(void);
@@ -120,6 +125,9 @@ CTDM_API ctdm_status ctdm_ctx_stage_times(ctdm_ctx *ctx, double *ms, int *counts
  * Synchronises the device; reading clears it.  A submitted call that saw a code makes
  * ctdm_wait return CTDM_ERR_TIMEOUT (and clears it). */
 CTDM_API ctdm_status ctdm_ctx_device_status(ctdm_ctx *ctx, int *status);
+/* Device bytes the context's workspace holds now (its buffers grow to the largest call
+ * and are kept). */
+CTDM_API ctdm_status ctdm_ctx_workspace(ctdm_ctx *ctx, size_t *bytes);
 /* Diagnostic (no reference counterpart): one device-side wait that nothing completes,
  * on an mbarrier with the bounded wait the z pass uses for its TMA tiles, `polls`
  * polls long (<= 0: that wait's production bound).  The wait runs out, records code 9
@@ -197,6 +205,18 @@ CTDM_API ctdm_status ctdm_batch_plan(ctdm_batch *batch, const ctdm_job *jobs, in
 CTDM_API ctdm_status ctdm_batch_run(ctdm_batch *batch, void *stream);
 /* The planned schedule launched kernel by kernel (no graph), for comparison. */
 CTDM_API ctdm_status ctdm_batch_run_eager(ctdm_batch *batch, void *stream);
+/* Admission by free device memory (no reference counterpart; the reference chooses its
+ * ReconMode from free memory, cTDM/HilbertTransform.cu:1932-1939): ctdm_batch_plan bounds
+ * every job's workspace (ctdm_workspace_bytes), keeps back 24 R^3 + 256 MiB bytes for
+ * the autotuner's scratch volumes, and uses only as many of the batch's lanes as fit in
+ * the device memory that is free plus what its lanes already hold, at most `bytes` when a
+ * limit is set (0: no limit); lanes left out give their buffers back.  A plan whose
+ * largest job does not fit alone returns CTDM_ERR_NOMEM before it allocates anything. */
+CTDM_API ctdm_status ctdm_batch_set_memory_limit(ctdm_batch *batch, size_t bytes);
+/* The last plan's admission: lanes used, workspace bound of its largest job, and the
+ * memory the plan could use. */
+CTDM_API ctdm_status ctdm_batch_admission(const ctdm_batch *batch, int *lanes_used, size_t *bytes_per_lane,
+                                          size_t *bytes_available);
 /* Lane each job was assigned to (longest job first onto the least-loaded lane). */
 CTDM_API ctdm_status ctdm_batch_lanes(const ctdm_batch *batch, int *lane_of_job, int n_jobs);
 

@@ -73,3 +73,23 @@ def test_plan_table_without_gpu(lib):
     assert C.plans(512, device=3) == ((1, 2, 0), False)
     with pytest.raises(C.CtdmError):
         C.set_plans(512, (0, 3, 0), device=3)
+
+
+def test_workspace_bound_without_gpu(lib):
+    """ctdm_workspace_bytes is host arithmetic: it grows with the volume, the angles,
+    Goldstein and the accelerated loop, and refuses what the pipeline refuses."""
+    import ctdm_gb300 as C
+    base = C.default_params(n_holo=1024, m_crop=256, r_vol=256, iterations=10, dx=0.1e-6)
+    w = C.workspace_bytes(base, 121)
+    r3 = 256 ** 3
+    assert 25 * r3 * 1 < w < 60 * r3
+    bigger = C.default_params(n_holo=1024, m_crop=256, r_vol=512, iterations=10, dx=0.1e-6)
+    assert C.workspace_bytes(bigger, 121) > 4 * w
+    assert C.workspace_bytes(base, 181) > w
+    gold = C.default_params(n_holo=1024, m_crop=256, r_vol=256, iterations=10, dx=0.1e-6, run_goldstein=1)
+    assert C.workspace_bytes(gold, 121) > w + 121 * 256 * 256 * 20
+    acc = C.default_params(n_holo=1024, m_crop=256, r_vol=256, iterations=10, dx=0.1e-6, accelerated=1)
+    assert C.workspace_bytes(acc, 121) == w + 8 * r3
+    bad = C.default_params(n_holo=1024, m_crop=256, r_vol=100, iterations=10, dx=0.1e-6)
+    with pytest.raises(C.CtdmError):
+        C.workspace_bytes(bad, 121)
