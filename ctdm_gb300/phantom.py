@@ -121,19 +121,32 @@ def rytov_field(ells, n_med, wavelength, n, pixel, ang_x, ang_y):
     return ut.T                                # CopyDataArray transposes: hologram [y, x]
 
 
+def intensity(u, photons, carrier=(0.125, 0.125)):
+    """Mean photon counts I0 |exp(-i 2 pi f_R . r) + exp(u)|^2 of one off-axis hologram
+    (float64, before the shot noise)."""
+    n = u.shape[-1]
+    yy, xx = np.mgrid[0:n, 0:n]
+    ref = np.exp(-2j * np.pi * (carrier[0] * xx + carrier[1] * yy))
+    return (photons / 2.0) * np.abs(ref + np.exp(u)) ** 2
+
+
 def holograms_from_fields(fields, photons, rng, carrier=(0.125, 0.125)):
     """Off-axis holograms; carrier (cycles per pixel along x, y), by default a quarter
     of Nyquist on both axes (the 2-D window of Algorithm A); Algorithm B filters along
     x only and wants the carrier along x, e.g. (0.25, 0)."""
-    n = fields.shape[-1]
-    yy, xx = np.mgrid[0:n, 0:n]
-    ref = np.exp(-2j * np.pi * (carrier[0] * xx + carrier[1] * yy))
-    i0 = photons / 2.0
-    out = []
-    for u in fields:
-        inten = i0 * np.abs(ref + np.exp(u)) ** 2
-        out.append(rng.poisson(inten).astype(np.float32) if photons > 0 else inten.astype(np.float32))
-    return np.stack(out)
+    return noisy(np.stack([intensity(u, photons, carrier) for u in fields]), photons, rng)
+
+
+def noisy(intens, photons, rng):
+    """Poisson shot noise on mean counts (angle by angle, in order, from rng)."""
+    return np.stack([rng.poisson(i).astype(np.float32) if photons > 0 else i.astype(np.float32) for i in intens])
+
+
+def _intensities(args):
+    """Worker: mean counts of a run of angles (fields are deterministic)."""
+    ells, n_med, wavelength, n, pixel, ax, ay, photons, carrier = args
+    return np.stack([intensity(rytov_field(ells, n_med, wavelength, n, pixel, ax[k], ay[k]), photons, carrier)
+                     for k in range(len(ax))])
 
 
 def cell_phantom(rng, scale=1.0, n_cell=1.37, n_nuc=1.39, semi=(4e-6, 3e-6, 2.5e-6), nucleoli=3):
@@ -167,15 +180,26 @@ def scan_angles(count, na, n_med):
 
 
 def acquisition(n, r, angles, na=0.9, seed=0, pixel=0.1e-6, wavelength=532e-9, n_med=1.337,
-                photons=1000.0, ells=None, scale=1.0, carrier=(0.125, 0.125), scan="cone", **cell):
+                photons=1000.0, ells=None, scale=1.0, carrier=(0.125, 0.125), scan="cone", workers=1, **cell):
     """One tomogram: `angles` SP holograms of N x N plus one background; scan "cone"
-    (illumination on a circular cone) or "line" (a one-axis AngX scan)."""
+    (illumination on a circular cone) or "line" (a one-axis AngX scan).  workers > 1
+    computes the fields in that many spawned processes (the same holograms)."""
     rng = np.random.default_rng(seed)
     if ells is None:
         ells = cell_phantom(rng, scale=scale, **cell)
     ax, ay = (cone_angles if scan == "cone" else scan_angles)(angles, na, n_med)
-    fields = np.stack([rytov_field(ells, n_med, wavelength, n, pixel, ax[a], ay[a]) for a in range(angles)])
-    holo = holograms_from_fields(fields, photons, rng, carrier)
+    if workers > 1 and angles > 1:
+        import concurrent.futures as cf
+        import multiprocessing as mp
+        runs = [c for c in np.array_split(np.arange(angles), workers) if len(c)]
+        jobs = [(ells, n_med, wavelength, n, pixel, ax[c], ay[c], photons, carrier) for c in runs]
+        with cf.ProcessPoolExecutor(len(jobs), mp_context=mp.get_context("spawn")) as ex:
+            intens = np.concatenate(list(ex.map(_intensities, jobs)))
+        holo = noisy(intens, photons, rng)
+        del intens
+    else:
+        fields = np.stack([rytov_field(ells, n_med, wavelength, n, pixel, ax[a], ay[a]) for a in range(angles)])
+        holo = holograms_from_fields(fields, photons, rng, carrier)
     bg = holograms_from_fields(np.zeros((1, n, n), np.complex128), photons, rng, carrier)[0]
     return Acquisition(holo, bg, ax, ay, n, n // 4, r, pixel, wavelength, n_med, ells)
 
