@@ -351,7 +351,10 @@ def run_large(args):
                         "spectra": A * (8.0 * m * m + 8.0 * r * r), "ewald": A * 8.0 * r * r + 16 * r3,
                         # the accelerated x pass also reads and writes the previous iterate
                         "x_pass": 16 * r3 + 16 * r3, "y_forward": 16 * r3, "y_inverse": 16 * r3,
-                        "z_pass": 16 * r3 + 8.0 * measured + 4 * r3 / 16, "x_final": 16 * r3}
+                        # no z-pass plan at 768 reads packed samples (a 768-line tile of 16 lines
+                        # exceeds the staging budget): the dense z pass reads F2 whole
+                        "z_pass": 24 * r3 if r > 512 else 16 * r3 + 8.0 * measured + 4 * r3 / 16,
+                        "x_final": 16 * r3}
     kernels = {}
     for k, (ms, cnt) in stages.items():
         if cnt and k in per_launch_bytes:
