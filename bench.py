@@ -278,6 +278,18 @@ def run_batched(args):
     launches = C.launch_count() - launches0
     clocks = sampler.stop()
     tomos = len(jobs) * args.steps
+    # where the one-by-one time goes: the latency-bound per-angle front end (the part other
+    # lanes can hide) against the bandwidth-bound volume passes (which share HBM when lanes
+    # overlap them, so they cannot gain from running side by side)
+    ctx.set_timing(True)
+    one_by_one()
+    torch.cuda.synchronize()
+    st = ctx.stage_times()
+    ctx.set_timing(False)
+    front = sum(st[k][0] for k in ("qpi", "unwrap", "goldstein", "spectra", "ewald"))
+    volume = sum(st[k][0] for k in ("y_inverse", "x_pass", "y_forward", "z_pass", "x_final"))
+    split = {"front_end_ms": front, "volume_passes_ms": volume, "front_end_fraction": front / (front + volume),
+             "gain_bound_if_front_ends_hidden": (front + volume) / volume}
     line = {
         "metric": "tomograms/s (hologram->RI), batched",
         "value": tomos / (ms_graph / 1e3),
@@ -298,6 +310,7 @@ def run_batched(args):
         "one_by_one": {"value": tomos / (ms_single / 1e3), "unit": "tomograms/s",
                        "ms_per_step": ms_single / args.steps},
         "speedup_vs_one_by_one": ms_single / ms_graph,
+        "one_by_one_stage_split": split,
         "e2e": None,
         "gpu_launches": int(launches),
         "clocks": clocks,
