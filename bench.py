@@ -250,7 +250,8 @@ def run_batched(args):
         for (p, h, bg, ax, ay, out) in jobs:
             ctx.reconstruct_device(p, h, bg, ax, ay, out, stream=stream)
 
-    batch = C.Batch(lanes=cfg["lanes"], device=local)
+    lanes = args.lanes if args.lanes > 0 else cfg["lanes"]
+    batch = C.Batch(lanes=lanes, device=local)
     batch.plan(jobs)
     for _ in range(args.warmup):
         batch.run(stream)
@@ -303,7 +304,7 @@ def run_batched(args):
         "vs_baseline": None,
         "dtype": "f32/c64",
         "data": "synthetic (two seeded random multi-ellipsoid cells acquired at 181 cone angles, Poisson noise)",
-        "config": {"workload": "batched", "tomograms": len(jobs), "lanes": cfg["lanes"],
+        "config": {"workload": "batched", "tomograms": len(jobs), "lanes": lanes,
                    "angles": [m[0] for m in meta], "holograms": [m[1] for m in meta],
                    "volumes": [m[2] for m in meta], "iterations": cfg["iterations"],
                    "parallelism": "one GPU (secondary workload)", "l2": "inputs and volumes far larger than L2"},
@@ -984,6 +985,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="wrap_heavy", choices=sorted(CONFIGS))
+    ap.add_argument("--lanes", type=int, default=0, help="batched workload: concurrent lanes (0: the default 4)")
     ap.add_argument("--loop-scheme", type=int, default=-1, choices=[-1, 0, 1, 2],
                     help="positivity-loop scheme of the volume side, with plan variants 0 for its passes "
                          "(-1: the autotuner's choice; profiles pin 2, the choice without a profiler)")
