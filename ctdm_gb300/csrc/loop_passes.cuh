@@ -209,7 +209,7 @@ template <class P>
 constexpr bool zpass_packable()
 {
     return (P::B == 8 || P::B == 16 || P::B == 32) && P::B <= P::L &&
-           sizeof(float2) * P::B * P::L <= 64 * 1024 && P::THREADS >= P::L / 2 && (P::L * 4) % 16 == 0;
+           sizeof(float2) * P::B * P::L <= 64 * 1024 && (P::L * 4) % 16 == 0;
 }
 
 template <class P>

@@ -137,3 +137,37 @@ def test_packed_measured_samples_bit_identical(ctx, dev, r):
     for mode in (0, 1):
         assert np.array_equal(outs[("1", mode)], outs[("0", mode)]), mode
     assert not np.array_equal(outs[("1", 0)], outs[("1", 1)])
+
+
+@pytest.mark.parametrize("r,variant", [(384, 2), (768, 1)])
+def test_packed_z_pass_at_large_sides_bit_identical(ctx, dev, r, variant):
+    """The z-pass plans with 8 or 16 lines per tile read packed measured samples at
+    384^3 and 768^3 too: the volume equals the dense pass's bit for bit (F2 drawn on the
+    device, 5% of the voxels measured)."""
+    import os
+    import torch
+    import ctdm_gb300 as C
+    gen = torch.Generator(device=dev).manual_seed(r)
+    keep = torch.rand((r, r, r), generator=gen, device=dev) < 0.05
+    f2 = torch.randn((r, r, r), dtype=torch.complex64, generator=gen, device=dev) * (1e-2 * K2 * 100)
+    f2 = torch.where(keep, f2, torch.zeros_like(f2))
+    del keep
+    saved, _ = C.plans(r)
+    outs = {}
+    try:
+        C.set_plans(r, (saved[0], saved[1], variant))
+        for packed in ("1", "0"):
+            os.environ["CTDM_PACKED_Z"] = packed
+            try:
+                out = torch.empty_like(f2)
+                ctx.positivity(f2, r, 2, K2, N_MED, out)
+                torch.cuda.synchronize()
+                outs[packed] = out
+            finally:
+                os.environ.pop("CTDM_PACKED_Z", None)
+        assert torch.equal(outs["1"], outs["0"])
+        assert ctx.device_status() == 0
+    finally:
+        C.set_plans(r, saved)
+    del outs, f2
+    torch.cuda.empty_cache()
