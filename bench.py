@@ -361,13 +361,14 @@ def run_large(args):
     measured = int(np.count_nonzero((F2.real != 0) & (F2.imag != 0)))
     del F2
     scheme = C.loop_scheme(r, device=local)
+    ztile = C.z_tile(r, device=local)
     per_launch_bytes = {"qpi": (A + 1) * (4.0 * n * n + 8.0 * m * m), "unwrap": A * 8.0 * m * m,
                         "spectra": A * (8.0 * m * m + 8.0 * r * r), "ewald": A * 8.0 * r * r + 16 * r3,
                         # the accelerated x pass also reads and writes the previous iterate
                         "x_pass": 16 * r3 + 16 * r3, "y_forward": 16 * r3, "y_inverse": 16 * r3,
-                        # no z-pass plan at 768 reads packed samples (a 768-line tile of 16 lines
-                        # exceeds the staging budget): the dense z pass reads F2 whole
-                        "z_pass": 24 * r3 if r > 512 else 16 * r3 + 8.0 * measured + 4 * r3 / 16,
+                        # the z pass reads the measured samples packed per tile when its plan
+                        # allows (z_tile > 0), else F2 whole
+                        "z_pass": (16 * r3 + 8.0 * measured + 4 * r3 / ztile) if ztile else 24 * r3,
                         "x_final": 16 * r3}
     kernels = {}
     for k, (ms, cnt) in stages.items():
@@ -416,7 +417,7 @@ def run_large(args):
                    "l2": "volumes of 3.6 GB (far larger than L2)"},
         "admission": {"lanes_requested": T, "lanes_admitted": lanes, "workspace_bound_per_lane_gb": per_lane / 1e9,
                       "available_gb": avail / 1e9, "free_before_plan_gb": free0 / 1e9},
-        "one_tomogram": {"ms": t_one, "loop_scheme": scheme, "kernels": kernels, "peak_gbs": peak,
+        "one_tomogram": {"ms": t_one, "loop_scheme": scheme, "z_tile": ztile, "kernels": kernels, "peak_gbs": peak,
                          "peak_source": peak_kind},
         "ri_rmse_vs_fp64": "tests/test_gpu_large.py: 768^3 from 2048^2 holograms against the FP64 oracle",
         "gpu_launches": int(launches),
@@ -880,11 +881,13 @@ def run_ours(args):
     # the z pass reads the measured samples packed per tile (G in and out, the kept
     # values, one mask word per (tile of 16 lines, z)).
     scheme = C.loop_scheme(r, device=local)
+    ztile = C.z_tile(r, device=local)
     F2 = ctx.read_buffer(7, np.complex64)
     measured = int(np.count_nonzero((F2.real != 0) & (F2.imag != 0)))
     del F2
     bytes_per = {"x_pass": 16 * r3, "y_forward": 16 * r3, "y_inverse": 16 * r3,
-                 "z_pass": 16 * r3 + 8.0 * measured + 4 * r3 / 16, "ewald": A * 8.0 * r * r + 16 * r3}
+                 "z_pass": (16 * r3 + 8.0 * measured + 4 * r3 / ztile) if ztile else 24 * r3,
+                 "ewald": A * 8.0 * r * r + 16 * r3}
     plane = {1: "plane_pass", 2: "plane_pass_4cta"}
     kernel_of = {"x_pass": plane.get(scheme, "x_pass"), "y_forward": "y_forward",
                  "y_inverse": "y_inverse", "z_pass": "z_pass_packed", "ewald": "ewald"}

@@ -326,6 +326,13 @@ def plans(r, device=0):
     return tuple(v), bool(t.value)
 
 
+def z_tile(r, device=0):
+    """Lines per packed z-pass tile of the current plan for side r (0: dense F2 reads)."""
+    v = ctypes.c_int()
+    check(load().ctdm_z_tile(int(device), int(r), ctypes.byref(v)), "ctdm_z_tile")
+    return v.value
+
+
 def set_plans(r, variants, device=0):
     v = (ctypes.c_int * 3)(*variants)
     check(load().ctdm_set_plans(int(device), int(r), v), "ctdm_set_plans")

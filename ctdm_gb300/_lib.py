@@ -130,6 +130,7 @@ _SIGS = {
     "ctdm_ctx_workspace": (c_int, [c_void_p, ctypes.POINTER(c_size_t)]),
     "ctdm_plan_count": (c_int, [c_int]),
     "ctdm_autotune": (c_int, [c_int, c_int, c_int, P_int, ctypes.POINTER(c_double), c_int]),
+    "ctdm_z_tile": (c_int, [c_int, c_int, P_int]),
     "ctdm_plans": (c_int, [c_int, c_int, P_int, P_int]),
     "ctdm_set_plans": (c_int, [c_int, c_int, P_int]),
     "ctdm_loop_scheme": (c_int, [c_int, c_int, P_int]),

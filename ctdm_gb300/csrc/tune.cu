@@ -355,6 +355,20 @@ extern "C" ctdm_status ctdm_autotune(int device, int R, int check_mode, int *var
     return CTDM_OK;
 }
 
+extern "C" ctdm_status ctdm_z_tile(int device, int R, int *lines)
+{
+    if (!lines || loop_plan_count(R) == 0) return fail_invalid("ctdm_z_tile: bad argument");
+    int v = 0;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_choice.find({device, R});
+        if (it != g_choice.end()) v = it->second.v[2];
+    }
+    *lines = ztile_of(R, v);
+    clear_error();
+    return CTDM_OK;
+}
+
 extern "C" ctdm_status ctdm_plans(int device, int R, int *variants3, int *tuned)
 {
     if (!variants3 || loop_plan_count(R) == 0) return fail_invalid("ctdm_plans: bad argument");

@@ -231,6 +231,9 @@ CTDM_API int ctdm_plan_count(int R);
  * receives the median time of pass p, variant v at ms[3 * p + v] (n_ms entries). */
 CTDM_API ctdm_status ctdm_autotune(int device, int R, int check_mode, int *variants3, double *ms, int n_ms);
 /* Current choice for (device, R); tuned = 1 when it came from the autotuner. */
+/* Lines per tile of the z pass's packed measured samples with the current plan of
+ * (device, R); 0 when that plan reads the measured data densely. */
+CTDM_API ctdm_status ctdm_z_tile(int device, int R, int *lines);
 CTDM_API ctdm_status ctdm_plans(int device, int R, int *variants3, int *tuned);
 /* Pin a choice (also disables tuning of that side on that device). */
 CTDM_API ctdm_status ctdm_set_plans(int device, int R, const int *variants3);
