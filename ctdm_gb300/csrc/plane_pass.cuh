@@ -24,9 +24,10 @@
 
 namespace ctdm {
 
-template <int L, int C>
+// PP: the line plan (lines per CTA, threads per line, radices) of the rows and columns.
+template <int L, int C, class PP = fftl::Plan<L>>
 struct PlaneCfg {
-    using P = fftl::Plan<L>;
+    using P = PP;
     static constexpr int RL = L / C;   // rows (and columns) per CTA
     static constexpr int SB = RL / P::B;
     static constexpr size_t SMEM = fftl::plan_smem_row<P>() > fftl::plan_smem<P>() ? fftl::plan_smem_row<P>()
@@ -37,11 +38,11 @@ struct PlaneCfg {
 // MINB: resident CTAs per SM the register allocation aims for (3: no spills at
 // R = 256; 4: more latency hiding for some spill traffic).  C: CTAs per plane.
 // MOM: the accelerated loop (momentum on the projected iterate, LoopArgs::xprev).
-template <int L, int C, int MINB, bool FINAL, bool MOM = false>
-__global__ void __launch_bounds__(fftl::Plan<L>::THREADS, MINB) plane_kernel(LoopArgs a, const float2 *__restrict__ tw)
+template <int L, int C, int MINB, bool FINAL, bool MOM = false, class PP = fftl::Plan<L>>
+__global__ void __launch_bounds__(PP::THREADS, MINB) plane_kernel(LoopArgs a, const float2 *__restrict__ tw)
 {
     namespace cg = cooperative_groups;
-    using Cfg = PlaneCfg<L, C>;
+    using Cfg = PlaneCfg<L, C, PP>;
     using P = typename Cfg::P;
     constexpr int RL = Cfg::RL;
     cg::cluster_group cluster = cg::this_cluster();
@@ -132,12 +133,12 @@ __global__ void __launch_bounds__(fftl::Plan<L>::THREADS, MINB) plane_kernel(Loo
 }
 
 // Launches the plane pass of side L with C-CTA clusters over all L planes.
-template <int L, int C, int MINB>
+template <int L, int C, int MINB, class PP = fftl::Plan<L>>
 static cudaError_t run_plane_pass(const LoopArgs &a, bool final_pass, cudaStream_t s)
 {
-    using Cfg = PlaneCfg<L, C>;
-    auto k = final_pass ? plane_kernel<L, C, MINB, true>
-                        : (a.xprev ? plane_kernel<L, C, MINB, false, true> : plane_kernel<L, C, MINB, false>);
+    using Cfg = PlaneCfg<L, C, PP>;
+    auto k = final_pass ? plane_kernel<L, C, MINB, true, false, PP>
+                        : (a.xprev ? plane_kernel<L, C, MINB, false, true, PP> : plane_kernel<L, C, MINB, false, false, PP>);
     if (!twiddles(L)) return cudaErrorInitializationError;
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -151,7 +152,7 @@ static cudaError_t run_plane_pass(const LoopArgs &a, bool final_pass, cudaStream
     }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)(L * C), 1, 1);
-    cfg.blockDim = dim3(fftl::Plan<L>::THREADS, 1, 1);
+    cfg.blockDim = dim3(PP::THREADS, 1, 1);
     cfg.dynamicSmemBytes = Cfg::SMEM;
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
@@ -168,16 +169,16 @@ static cudaError_t run_plane_pass(const LoopArgs &a, bool final_pass, cudaStream
 }
 
 // Number of clusters of the plane pass that fit on the device at once (0: none).
-template <int L, int C, int MINB>
+template <int L, int C, int MINB, class PP = fftl::Plan<L>>
 static int plane_pass_clusters()
 {
-    using Cfg = PlaneCfg<L, C>;
-    auto k = plane_kernel<L, C, MINB, false>;
+    using Cfg = PlaneCfg<L, C, PP>;
+    auto k = plane_kernel<L, C, MINB, false, false, PP>;
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM) != cudaSuccess) return 0;
     if (C > 8 && cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) return 0;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)(L * C), 1, 1);
-    cfg.blockDim = dim3(fftl::Plan<L>::THREADS, 1, 1);
+    cfg.blockDim = dim3(PP::THREADS, 1, 1);
     cfg.dynamicSmemBytes = Cfg::SMEM;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
