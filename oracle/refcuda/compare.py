@@ -57,14 +57,58 @@ def build():
     return {"release": os.path.join(REF, "ref_pipeline"), "ieee": os.path.join(REF, "ieee", "ref_pipeline")}
 
 
-def run_reference(exe, fin, reps, R):
+def run_reference(exe, fin, reps, R, dump=None):
+    """Runs the binary; with `dump` (a folder) it also writes the reference's
+    intermediate arrays there (one more, untimed repetition)."""
     with tempfile.TemporaryDirectory() as tmp:
         fout = os.path.join(tmp, "out.bin")
-        r = subprocess.run([exe, fin, fout, str(reps)], capture_output=True, text=True, timeout=3000)
+        cmd = [exe, fin, fout, str(reps + 1 if dump else reps)] + ([dump] if dump else [])
+        r = subprocess.run(cmd, capture_output=True, text=True, timeout=3000)
         if r.returncode != 0:
             raise SystemExit(f"ref_pipeline failed ({r.returncode}): {r.stderr[-2000:]}")
         timing = json.loads(r.stdout.strip().splitlines()[-1])
         return timing, np.fromfile(fout, np.complex64).reshape(R, R, R)
+
+
+def wrap(x):
+    return np.angle(np.exp(1j * x))
+
+
+def stage_parity(O, acq, car, dump):
+    """The reference's own intermediate arrays (IEEE build) against the FP64 oracle on the
+    same holograms: wrapped phase and amplitude of calcWrapPhase, the DCT unwrap, the Ewald
+    hit counts and F2 of initial_F_and_F2."""
+    A, m, R = len(acq.ang_x), acq.m_crop, acq.r_vol
+    ph = np.fromfile(os.path.join(dump, "phase.f32"), np.float32).reshape(A, m, m)
+    am = np.fromfile(os.path.join(dump, "amp.f32"), np.float32).reshape(A, m, m)
+    uw = np.fromfile(os.path.join(dump, "unwrapped.f32"), np.float32).reshape(A, m, m)
+    bgf = O.qpi_field(acq.background, m, *car)
+    ph_err, am_err, uw_err = [], [], []
+    for a in range(A):
+        oph, oam = O.wrap_phase(O.qpi_field(acq.holograms[a], m, *car), bgf)
+        ph_err.append(float(np.sqrt(np.mean(wrap(ph[a] - oph) ** 2))))
+        am_err.append(float(np.sqrt(np.mean((am[a] - oam) ** 2))))
+        ouw = O.dct_unwrap(oph, 0)
+        uw_err.append(float(np.sqrt(np.mean((uw[a] - ouw) ** 2))))
+    del ph, am, uw
+    par = O.make_params(acq.n_holo, m, R, 0, acq.fm0, acq.df, acq.dx, acq.k2, acq.n_med, carrier=car)
+    oph, oam, _ = O.front_end(par, acq.holograms, acq.background)
+    U = np.stack([O.rytov_spectrum(oph[a], oam[a]) for a in range(A)])
+    del oph, oam
+    oF2, oC = O.ewald_map(U, acq.ang_x, acq.ang_y, acq.fm0, acq.df, acq.dx)
+    del U
+    rc = np.fromfile(os.path.join(dump, "counts.f32"), np.float32).reshape(R, R, R)
+    rf2 = np.fromfile(os.path.join(dump, "f2.c64"), np.complex64).reshape(R, R, R)
+    same = rc.astype(np.int64) == oC.astype(np.int64)
+    both = same & (oC > 0)
+    d = rf2[both].astype(np.complex128) - oF2[both]
+    f2_rel = float(np.linalg.norm(d) / np.linalg.norm(oF2[both]))
+    return {"wrapped_phase_rms_rad_max": max(ph_err), "wrapped_phase_rms_rad_mean": float(np.mean(ph_err)),
+            "amplitude_rmse_max": max(am_err), "dct_unwrapped_rmse_rad_max": max(uw_err),
+            "hit_count_voxels_equal_fraction": float(np.mean(same)),
+            "hit_voxels_reference": int(np.count_nonzero(rc)), "hit_voxels_oracle": int(np.count_nonzero(oC)),
+            "hit_voxels_differing": int(np.count_nonzero(~same)),
+            "f2_rel_l2_on_equal_hit_voxels": f2_rel}
 
 
 def finite_rmse(a, ref):
@@ -147,8 +191,11 @@ def main():
         with tempfile.TemporaryDirectory() as tmp:
             fin = os.path.join(tmp, "in.bin")
             write_input(fin, acq, iters, car)
+            dump = os.path.join(tmp, "dump")
+            os.makedirs(dump)
             for kind, exe in exes.items():
-                refs[kind] = run_reference(exe, fin, args.reps, R)
+                refs[kind] = run_reference(exe, fin, args.reps, R, dump=dump if kind == "ieee" else None)
+            stages = stage_parity(O, acq, car, dump)
         par = O.make_params(acq.n_holo, acq.m_crop, R, iters, acq.fm0, acq.df, acq.dx, acq.k2, acq.n_med)
         fp64, ocar, _ = O.tomogram(par, acq.holograms, acq.background, acq.ang_x, acq.ang_y)
         mine = ours(acq, iters, gold, args.reps)
@@ -172,6 +219,7 @@ def main():
                                  "ri_rmse_vs_fp64": rmse(v["volume"], fp64),
                                  "ri_rmse_vs_reference_cuda_ieee": finite_rmse(v["volume"], ieee_vol.astype(np.complex128))[0]
                                  if np.isfinite(ieee_vol).all() else None} for k, v in mine.items()},
+            "reference_stages_vs_fp64": stages,
             "speedup_host_buffers_same_work": refs["release"][0]["ms_mean"] / plain["host_buffers_ms_mean"],
             "reps": args.reps,
         }

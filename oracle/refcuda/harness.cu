@@ -22,7 +22,12 @@
 // Input (little-endian): "CTDMREF1", int32 N, R, A, iterations, carrier row, column,
 // radius; float64 n_med, wavelength (m), dx (m); float32 angx[A], angy[A],
 // background[N*N], holograms[A][N*N].  Output: R^3 complex64 (octant-shifted n, as
-// BatchRecon exports it).  Usage: ref_pipeline <in> <out> <repetitions>
+// BatchRecon exports it).  Usage: ref_pipeline <in> <out> <repetitions> [dump folder]
+//
+// With a dump folder the first repetition also writes the reference's intermediate
+// arrays there (it is then left out of the timing): phase.f32 and amp.f32 (the wrapped
+// phase and amplitude of calcWrapPhase, A * M * M), unwrapped.f32 (DCT_UWLS_Unwrapped),
+// counts.f32 (the Ewald hit counts C, R^3) and f2.c64 (initial_F_and_F2's F2, R^3).
 #include <chrono>
 #include <cmath>
 #include <cstdint>
@@ -30,6 +35,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <ctime>
+#include <string>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -112,8 +118,8 @@ static bool read_input(const char *path, Input &in)
 
 int main(int argc, char **argv)
 {
-    if (argc != 4) {
-        std::fprintf(stderr, "usage: %s <input> <output> <repetitions>\n", argv[0]);
+    if (argc != 4 && argc != 5) {
+        std::fprintf(stderr, "usage: %s <input> <output> <repetitions> [dump folder]\n", argv[0]);
         return 2;
     }
     Input in;
@@ -122,6 +128,11 @@ int main(int argc, char **argv)
         return 2;
     }
     const int reps = std::atoi(argv[3]);
+    const char *dump_dir = argc == 5 ? argv[4] : nullptr;
+    if (reps < (dump_dir ? 2 : 1)) {
+        std::fprintf(stderr, "repetitions must be at least %d\n", dump_dir ? 2 : 1);
+        return 2;
+    }
     const int Nx = in.N, Ny = in.N, R = in.R, A = in.A;
     const long nn = (long)Nx * Ny;
     // the window the carrier selects must lie inside the spectrum (get1stOrder_new reads it)
@@ -185,7 +196,13 @@ int main(int argc, char **argv)
 
     double best_ms = 1e30, sum_ms = 0, front_ms = 0, recon_ms = 0;
     long bad_maps = 0, bad_stack = 0;   // non-finite map values before / after the Combine2Stack fix-up
+    const long mm = (long)Nx2 * Ny2;
+    std::vector<float> d_phase, d_amp, d_unw, d_counts;
+    std::vector<cufftComplex> d_f2;
+    if (dump_dir) d_phase.resize(mm * A), d_amp.resize(mm * A), d_unw.resize(mm * A);
+    int timed = 0;
     for (int rep = 0; rep < reps; rep++) {
+        const bool dumping = dump_dir && rep == 0;
         CK(cudaDeviceSynchronize());
         const auto t0 = std::chrono::steady_clock::now();
         std::vector<float> phase_stack(r2 * A), amp_stack(r2 * A);
@@ -194,6 +211,12 @@ int main(int argc, char **argv)
             extractQPI_AlgorithmA(sp_cu.data() + (size_t)(frame - 1) * nn, bg_cu.data(), cuSP2, cuBG2, Nx, Ny, 2);
             calcWrapPhase<<<grid3, block>>>(UnWrapPhaseSP2, cuAmpMap2, cuSP2, cuBG2, Nx2, Ny2);
             DCT_UWLS_Unwrapped(cuPhaseMap2, UnWrapPhaseSP2, Nx2, Ny2);
+            if (dumping) {   // the DCT reads the wrapped phase without changing it
+                const long o = (long)(frame - 1) * mm;
+                CK(cudaMemcpy(d_phase.data() + o, UnWrapPhaseSP2, sizeof(float) * mm, cudaMemcpyDeviceToHost));
+                CK(cudaMemcpy(d_amp.data() + o, cuAmpMap2, sizeof(float) * mm, cudaMemcpyDeviceToHost));
+                CK(cudaMemcpy(d_unw.data() + o, cuPhaseMap2, sizeof(float) * mm, cudaMemcpyDeviceToHost));
+            }
             bilinear_interpolation_kernel<<<grid, block>>>(cuPhaseMap, cuPhaseMap2, cuAmpMap, cuAmpMap2, Nx2, Ny2, Nx,
                                                            Ny);
             CK(cudaMemcpy(final_phase.data(), cuPhaseMap, sizeof(float) * nn, cudaMemcpyDeviceToHost));
@@ -238,6 +261,11 @@ int main(int argc, char **argv)
         CK(cudaFree(CUDA_Amp));
         CK(cudaMalloc(&CUDA_F2, sizeof(cufftComplex) * r3));
         initial_F_and_F2(CUDA_C, CUDA_F, CUDA_F2, (float)dx, R, R, R);
+        if (dumping) {
+            d_counts.resize(r3), d_f2.resize(r3);
+            CK(cudaMemcpy(d_counts.data(), CUDA_C, sizeof(float) * r3, cudaMemcpyDeviceToHost));
+            CK(cudaMemcpy(d_f2.data(), CUDA_F2, sizeof(cufftComplex) * r3, cudaMemcpyDeviceToHost));
+        }
         CK(cudaFree(CUDA_C));
         cuFFT3D(CUDA_F, R, R, R, 1);
         CK(cudaMalloc(&CUDA_n, sizeof(cufftComplex) * r3));
@@ -258,6 +286,8 @@ int main(int argc, char **argv)
         CK(cudaGetLastError());
         const auto t2 = std::chrono::steady_clock::now();
         const double ms = std::chrono::duration<double, std::milli>(t2 - t0).count();
+        if (dumping) continue;   // the dumps' copies are not part of the pipeline
+        timed++;
         best_ms = ms < best_ms ? ms : best_ms;
         sum_ms += ms;
         front_ms += std::chrono::duration<double, std::milli>(t1 - t0).count();
@@ -269,11 +299,27 @@ int main(int argc, char **argv)
         return 2;
     }
     std::fclose(f);
+    if (dump_dir) {
+        auto put = [&](const char *name, const void *data, size_t bytes) {
+            std::string path = std::string(dump_dir) + "/" + name;
+            FILE *g = std::fopen(path.c_str(), "wb");
+            const bool ok = g && std::fwrite(data, 1, bytes, g) == bytes;
+            if (g) std::fclose(g);
+            if (!ok) std::fprintf(stderr, "cannot write %s\n", path.c_str());
+            return ok;
+        };
+        if (!put("phase.f32", d_phase.data(), sizeof(float) * d_phase.size()) ||
+            !put("amp.f32", d_amp.data(), sizeof(float) * d_amp.size()) ||
+            !put("unwrapped.f32", d_unw.data(), sizeof(float) * d_unw.size()) ||
+            !put("counts.f32", d_counts.data(), sizeof(float) * d_counts.size()) ||
+            !put("f2.c64", d_f2.data(), sizeof(cufftComplex) * d_f2.size()))
+            return 2;
+    }
     long bad_out = 0;
     for (long i = 0; i < r3; i++) bad_out += !std::isfinite(n3d[i].x) || !std::isfinite(n3d[i].y);
     std::printf("{\"reps\": %d, \"ms_mean\": %.3f, \"ms_best\": %.3f, \"front_ms_mean\": %.3f, "
                 "\"recon_ms_mean\": %.3f, \"non_finite_map_values\": %ld, \"non_finite_stack_values\": %ld, "
                 "\"non_finite_voxels\": %ld}\n",
-                reps, sum_ms / reps, best_ms, front_ms / reps, recon_ms / reps, bad_maps, bad_stack, bad_out);
+                timed, sum_ms / timed, best_ms, front_ms / timed, recon_ms / timed, bad_maps, bad_stack, bad_out);
     return 0;
 }
