@@ -626,7 +626,7 @@ __device__ bool sweep_owned(uint8_t *st, const FFLists &ls, int L, int Lprev, in
 constexpr int FF_SMEM_MAX = 3072, FF_SMEM_CAP = 1024;
 static int g_fill_cap = FF_SMEM_CAP;   // set by ctdm_set_fill_list_capacity
 
-// The fill of one map (FloodFill, cTDM/PhaseUnwrapping.cu).  Returns the status (0
+// The fill of one map (FloodFill, cTDM/Goldstein.cu:643-1095).  Returns the status (0
 // done, 1 sweep limit, 2 no seed) or -1 when a list outgrew ls.cap.
 // s_cnt[2]: list lengths; the list of sweep j is counted in s_cnt[j & 1] while sweep j
 // counts the next one in s_cnt[(j + 1) & 1].
@@ -643,17 +643,11 @@ __device__ int fill_map(uint8_t *st, const uint8_t *cut, const float *ph, float 
     }
     const int nbc = __syncthreads_count(nbc_local > 0);
     if (t == 0) {
-        // seed (FloodFill :656-691): walk the diagonal from (W/2, 2) off the cuts,
-        // then seed at the transposed coordinates as the reference does
-        int xr = W / 2, yr = 2;
-        int ok = xr < W && yr < H;
-        while (ok && cut[xr + (long)W * yr] == 1) {
-            xr++;
-            yr++;
-            if (xr >= W || yr >= H) ok = 0;
-        }
-        const int rowRef = yr, colRef = xr;
-        if (ok && (rowRef >= W || colRef >= H)) ok = 0;
+        // seed (FloodFill :656-691): (rowRef, colRef) = (2, W/2), fixed before the
+        // reference's diagonal walk off the cuts (:659-663), which therefore changes
+        // nothing; the seed may lie on a cut
+        const int rowRef = 2, colRef = W / 2;
+        const int ok = rowRef < W && colRef < H;
         int cnt = 0;
         if (ok) {
             const long seed = rowRef + (long)W * colRef;

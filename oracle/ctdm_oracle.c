@@ -739,18 +739,13 @@ int or_goldstein_floodfill(const uint8_t *cut, const float *phi, int w, int h, f
     long *stuck = (long *)malloc(sizeof(long) * n);
     memset(ub, 0, n);
     for (long i = 0; i < n; i++) out[i] = 0.0f;
-    int xRef = w / 2, yRef = 2;
-    int seed_ok = xRef < w && yRef < h;
-    /* the reference walks the diagonal without a bound; leaving the image (or a seed
-     * whose transposed coordinates fall outside it) stops the fill here */
-    while (seed_ok && cut[xRef + (long)w * yRef] == 1) {
-        xRef++;
-        yRef++;
-        if (xRef >= w || yRef >= h) seed_ok = 0;
-    }
-    int rowRef = yRef, colRef = xRef;
-    if (seed_ok && (rowRef >= w || colRef >= h)) seed_ok = 0;
-    if (!seed_ok) { free(adj); free(list); free(stuck); return 2; }
+    /* The seed is (rowRef, colRef) = (2, W/2), index rowRef + W colRef: the reference
+     * sets it (:656-657) before it walks the diagonal from (W/2, 2) off the cuts
+     * (:659-663), so the walk changes nothing (it only reads, past the image when the
+     * whole diagonal is cut) and the seed may lie on a cut.  A seed outside the image
+     * stops the fill here. */
+    const int rowRef = 2, colRef = w / 2;
+    if (rowRef >= w || colRef >= h) { free(adj); free(list); free(stuck); return 2; }
     long nbc = 0;
     for (long i = 0; i < n; i++) nbc += cut[i] != 0;
     if (rowRef > 0) adj[(rowRef - 1) + (long)w * colRef] = 1;

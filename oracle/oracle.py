@@ -85,6 +85,14 @@ def fft3(a, direction):
     return a
 
 
+def shift3d(a):
+    """Octant swap of a (nz, ny, nx) complex volume (or_shift3d)."""
+    a = _c128(a)
+    out = np.empty_like(a)
+    lib().or_shift3d(_p(a), _p(out), a.shape[2], a.shape[1], a.shape[0])
+    return out
+
+
 # ---- QPI -------------------------------------------------------------------
 def carrier_start_row(n):
     return lib().or_carrier_start_row(int(n))

@@ -46,6 +46,24 @@ def test_goldstein_bit_exact(ctx, dev, oracle, m, noise):
         assert np.count_nonzero(q) > 10   # the case exercises the branch cuts
 
 
+@pytest.mark.parametrize("m,x1,x2", [(64, 32, 40), (96, 48, 60)])
+def test_goldstein_walk_start_on_cut(ctx, dev, oracle, m, x1, x2):
+    """A residue at (W/2, 2) puts the start of the reference's diagonal seed walk on a
+    cut; the seed stays at (2, W/2) (FloodFill, cTDM/Goldstein.cu:656-663)."""
+    yy, xx = np.mgrid[0:m, 0:m].astype(np.float64)
+    th = np.arctan2(yy - 2.5, xx - (x1 + 0.5)) - np.arctan2(yy - 2.5, xx - (x2 + 0.5))
+    phi = np.angle(np.exp(1j * (th + 0.3 * xx + 0.1 * yy))).astype(np.float32)
+    q, c, o, st = run_gpu(ctx, dev, phi[None])
+    oq = oracle.goldstein_residues(phi)
+    oc = oracle.goldstein_cuts(oq)
+    assert oc[2, m // 2] == 1
+    assert np.array_equal(q[0], oq) and np.array_equal(c[0], oc)
+    oo, ub, ost = oracle.goldstein_floodfill(oc, phi)
+    assert st[0] == ost == 0
+    assert o[0, m // 2, 2] == phi[m // 2, 2]   # the seed keeps its wrapped value
+    assert np.sqrt(np.mean((o[0] - oo) ** 2)) < PHASE_TOL
+
+
 def test_goldstein_global_state_path(ctx, dev, oracle):
     m = 512   # above the shared-memory limit: state in global memory
     maps = noisy_phase(m, 7, 0.5)[None]
