@@ -626,8 +626,8 @@ static ctdm_status qpi_setup(ctdm_ctx *c, int N, int M, int A, const float *bg, 
         const int ac = (int)std::min<long>(chunk, nbg - a0);
         CK(qpi_forward_window(bg + a0 * nn, 4, ac, N, M, car, B<float2>(c, B_T1), B<float2>(c, B_S), s),
            "qpi bg fwd");
-        CK(qpi_inverse_window(B<float2>(c, B_S), ac, M, B<float2>(c, B_BGF) + a0 * mm, nullptr, 0, nullptr, nullptr,
-                              s),
+        CK(qpi_inverse_window(B<float2>(c, B_S), ac, M, car, B<float2>(c, B_BGF) + a0 * mm, nullptr, 0, nullptr,
+                              nullptr, s),
            "qpi bg inv");
     }
     return CTDM_OK;
@@ -648,7 +648,7 @@ static ctdm_status qpi_angles(ctdm_ctx *c, int N, int M, int A, int first, int c
                               B<float2>(c, B_T1), B<float2>(c, B_S), s),
            "qpi fwd");
         const float2 *bgf = B<float2>(c, B_BGF) + (bg_per_angle ? a0 * mm : 0);
-        CK(qpi_inverse_window(B<float2>(c, B_S), ac, M, nullptr, bgf, bg_per_angle ? mm : 0, phase + a0 * mm,
+        CK(qpi_inverse_window(B<float2>(c, B_S), ac, M, car, nullptr, bgf, bg_per_angle ? mm : 0, phase + a0 * mm,
                               amp + a0 * mm, s),
            "qpi inv");
     }
@@ -1724,8 +1724,8 @@ extern "C" void extractQPI_AlgorithmA(ctdm_cfloat *SP, ctdm_cfloat *BG, ctdm_cfl
         e = qpi_forward_window(B<float>(c, B_HOLO), 4, 1, N, M, B<int>(c, B_CARRIER), B<float2>(c, B_T1),
                                B<float2>(c, B_S), 0);
     if (e == cudaSuccess)
-        e = qpi_inverse_window(B<float2>(c, B_S), 1, M, reinterpret_cast<float2 *>(cuSP_FFT), nullptr, 0, nullptr,
-                               nullptr, 0);
+        e = qpi_inverse_window(B<float2>(c, B_S), 1, M, B<int>(c, B_CARRIER), reinterpret_cast<float2 *>(cuSP_FFT),
+                               nullptr, 0, nullptr, nullptr, 0);
     if (e != cudaSuccess) { cuda_fail(e, "extractQPI_AlgorithmA"); return; }
     finish("extractQPI_AlgorithmA");
 }

@@ -4,13 +4,15 @@
 //
 // The reference transforms the whole N x N hologram, swaps quadrants, copies an
 // M x M window around the carrier, swaps again and inverse-transforms.  Only the
-// M window columns and rows of the forward spectrum are ever used, so the
-// forward transform is pruned: a row pass computes full N-point row transforms
-// (two real rows packed in one complex transform) and keeps the M window
-// columns; a column pass transforms those columns and keeps the M window rows,
-// masks to the +-radius box and writes them at their ifftshifted positions.
-// The M x M inverse transform follows (rows, then columns with the 1/M^2 scale,
-// conjugate and the phase/amplitude epilogue fused).
+// window's +-radius box around the carrier survives get1stOrder_new's mask, so the
+// forward transform is pruned to it: a row pass computes full N-point row transforms
+// (two real rows packed in one complex transform) and keeps the box's columns of
+// the window; a column pass transforms those columns and keeps the window rows,
+// masks to the box and writes them at their ifftshifted positions (zeros elsewhere).
+// The M x M inverse transform follows: rows, skipping the rows outside the box, then
+// columns with the 1/M^2 scale, conjugate and the phase/amplitude epilogue fused.
+// On 1024^2 holograms with a 256 window and radius 42 the box holds 85 of the 256
+// columns and rows.
 #include <cmath>
 
 #include "fft_line.cuh"
@@ -122,17 +124,20 @@ __global__ void __launch_bounds__(QRows<N>::THREADS) qpi_rows_kernel(const T *__
     }
     P::template seq_row<false>(buf, v, tw);
     float2 *line = buf + b * Y::LINE;
-    // park only the points the window reads: k in [k0, k0 + M) mod N and their mirrors
-    const int c = __ldg(&carrier[1]);
-    const int k0 = (c - N / 2 - M / 2 + 2 * N) & (N - 1);
+    // Only the columns of the radius box survive the column pass's mask: window
+    // columns m in [mlo, mhi] (|m - M/2| <= radius), spectrum columns k in
+    // [kb, kb + W) mod N.  Park those points and their mirrors.
+    const int c = __ldg(&carrier[1]), rad = __ldg(&carrier[2]);
+    const int mlo = max(0, M / 2 - rad), mhi = min(M - 1, M / 2 + rad), W = mhi - mlo + 1;
+    const int kb = (c - N / 2 - M / 2 + mlo + 2 * N) & (N - 1);
 #pragma unroll
     for (int i = 0; i < P::E; i++) {
         const int k = fftl::slot_pos<N, P::T, P::RV0>(i, t);
-        if (((k - k0 + N) & (N - 1)) < M || ((((N - k) & (N - 1)) - k0 + N) & (N - 1)) < M) line[Y::at(k)] = v[i];
+        if (((k - kb + N) & (N - 1)) < W || ((((N - k) & (N - 1)) - kb + N) & (N - 1)) < W) line[Y::at(k)] = v[i];
     }
     __syncthreads();
     if (!ok) return;
-    for (int m = t; m < M; m += P::T) {
+    for (int m = mlo + t; m <= mhi; m += P::T) {
         int k = (c - N / 2 + m - M / 2) % N;
         if (k < 0) k += N;
         const float2 z1 = line[Y::at(k)];
@@ -151,7 +156,10 @@ __global__ void __launch_bounds__(QRows<N>::THREADS) qpi_rows_kernel(const T *__
 // ky = (r - N/2 + j - M/2) mod N, masks to |offsets| <= radius and stores at the
 // ifftshifted position of S (A x M x M).  T1 is L2-resident (one chunk of
 // holograms), the first stage loads straight into registers and the spectrum is
-// parked in shared memory only for the window extraction.
+// parked in shared memory only for the window extraction.  The row pass wrote only
+// the radius box's columns: a CTA whose lines all lie outside it writes their zero
+// columns and skips the transform (a line outside the box in a CTA that transforms
+// reads stale T1 values and masks them).
 template <int N>
 struct QCols : fftl::Plan<N> {};
 template <> struct QCols<1024> : fftl::PlanT<1024, 4, 64, fftl::Radices<16, 16, 4>, fftl::Radices<4, 16, 16>> {};
@@ -171,6 +179,20 @@ __global__ void __launch_bounds__(QCols<N>::THREADS) qpi_cols_kernel(const float
     const bool ok = l < nlines;
     const int m = ok ? (int)(l % M) : 0;
     const long a = ok ? l / M : 0;
+    const int r = carrier[0], rad = carrier[2];
+    const int ox = m - M / 2;
+    const int io = (m + M / 2) % M;
+    float2 *dst = S + a * (long)M * M;
+    bool any_in = false;   // the same for every thread of the CTA
+    for (int bb = 0; bb < P::B; bb++) {
+        const long lb = line0 + bb;
+        any_in |= lb < nlines && abs((int)(lb % M) - M / 2) <= rad;
+    }
+    if (!any_in) {
+        if (ok)
+            for (int j = t; j < M; j += P::T) dst[(long)((j + M / 2) % M) * M + io] = make_float2(0.f, 0.f);
+        return;
+    }
     const float2 *src = T1 + a * (long)N * M + m;
     float2 v[P::E];
 #pragma unroll
@@ -182,10 +204,6 @@ __global__ void __launch_bounds__(QCols<N>::THREADS) qpi_cols_kernel(const float
     for (int i = 0; i < P::E; i++) line[fftl::slot_pos<N, P::T, P::RV0>(i, t)] = v[i];
     __syncthreads();
     if (!ok) return;
-    const int r = carrier[0], rad = carrier[2];
-    const int ox = m - M / 2;
-    const int io = (m + M / 2) % M;
-    float2 *dst = S + a * (long)M * M;
     for (int j = t; j < M; j += P::T) {
         const int oy = j - M / 2;
         int ky = (r - N / 2 + oy) % N;
@@ -196,13 +214,51 @@ __global__ void __launch_bounds__(QCols<N>::THREADS) qpi_cols_kernel(const float
     }
 }
 
+// ------------------------------------------------------------ inverse row pass
+// Rows j' of S (ifftshifted window rows) outside the radius box, rad < j' < M - rad,
+// are zero (the column pass wrote them so) and stay zero: a CTA whose rows all lie
+// there returns at once.  Row mapping: the first stage loads straight from S, the
+// last one stores straight back.
+template <int M>
+__global__ void __launch_bounds__(Plan<M>::THREADS) qpi_rows_inv_kernel(float2 *S, long nlines,
+                                                                       const int *__restrict__ carrier,
+                                                                       const float2 *__restrict__ tw)
+{
+    using P = Plan<M>;
+    extern __shared__ float4 smem4[];
+    float2 *buf = reinterpret_cast<float2 *>(smem4);
+    const long line0 = (long)blockIdx.x * P::B;
+    const int rad = __ldg(&carrier[2]);
+    bool any_in = false;   // the same for every thread of the CTA
+    for (int bb = 0; bb < P::B; bb++) {
+        const long lb = line0 + bb;
+        const int j = (int)(lb % M);
+        any_in |= lb < nlines && (j <= rad || j >= M - rad);
+    }
+    if (!any_in) return;
+    const int t = threadIdx.x % P::T, b = threadIdx.x / P::T;
+    const long l = line0 + b;
+    const bool ok = l < nlines;
+    float2 *row = S + (ok ? l : 0) * (long)M;
+    float2 v[P::E];
+#pragma unroll
+    for (int i = 0; i < P::E; i++)
+        v[i] = ok ? __ldcs(&row[fftl::slot_pos<M, P::T, P::F0>(i, t)]) : make_float2(0.f, 0.f);
+    P::template seq_row<true>(buf, v, tw);
+    if (!ok) return;
+#pragma unroll
+    for (int i = 0; i < P::E; i++) __stcg(&row[fftl::slot_pos<M, P::T, P::RV0>(i, t)], v[i]);
+}
+
 // ------------------------------------------------------------ inverse column pass
 // Lines are the M columns of each M x M spectrum (rows already inverse
-// transformed).  Epilogue: x 1/M^2 and conjugate (scaleFFT2D), then either store
-// the complex field (background) or the phase arg BG - arg SP and amplitude
-// |SP|/|BG| with NaN/inf -> 0 (calcWrapPhase).
+// transformed; the rows outside the radius box are zero and not read).  Epilogue:
+// x 1/M^2 and conjugate (scaleFFT2D), then either store the complex field
+// (background) or the phase arg BG - arg SP and amplitude |SP|/|BG| with NaN/inf -> 0
+// (calcWrapPhase).
 template <int M>
 __global__ void __launch_bounds__(Plan<M>::THREADS) qpi_final_kernel(const float2 *__restrict__ S, long nlines,
+                                                                    const int *__restrict__ carrier,
                                                                     float2 *field_out, const float2 *__restrict__ bgf,
                                                                     long bg_stride, float *phase, float *amp,
                                                                     const float2 *__restrict__ tw)
@@ -218,7 +274,9 @@ __global__ void __launch_bounds__(Plan<M>::THREADS) qpi_final_kernel(const float
     const long a = ok ? l / M : 0;
     const long mm = (long)M * M;
     const float2 *src = S + a * mm + x;
-    for (int p = t; p < M; p += P::T) buf[b * P::LP + p] = ok ? src[(long)p * M] : make_float2(0.f, 0.f);
+    const int rad = __ldg(&carrier[2]);
+    for (int p = t; p < M; p += P::T)
+        buf[b * P::LP + p] = ok && (p <= rad || p >= M - rad) ? src[(long)p * M] : make_float2(0.f, 0.f);
     __syncthreads();
     P::template run<true>(buf, tw);
     if (!ok) return;
@@ -275,18 +333,22 @@ static cudaError_t qpi_fwd_launch(const void *holo, int bpc, int A, int M, const
 }
 
 template <int M>
-static cudaError_t qpi_inv_launch(float2 *S, int A, float2 *field_out, const float2 *bgf, long bg_stride,
-                                  float *phase, float *amp, cudaStream_t s)
+static cudaError_t qpi_inv_launch(float2 *S, int A, const int *carrier, float2 *field_out, const float2 *bgf,
+                                  long bg_stride, float *phase, float *amp, cudaStream_t s)
 {
     using P = Plan<M>;
-    cudaError_t e = fft_rows(S, M, (long)A * M, true, s);
+    const long nl = (long)A * M;
+    const size_t smem_r = fftl::plan_smem_row<P>();
+    cudaError_t e = set_smem<M>(qpi_rows_inv_kernel<M>, smem_r);
     if (e != cudaSuccess) return e;
+    qpi_rows_inv_kernel<M><<<(unsigned)((nl + P::B - 1) / P::B), P::THREADS, smem_r, s>>>(S, nl, carrier,
+                                                                                         twiddles(M)); note_launch();
     const size_t smem = fftl::smem_bytes<M>();
     e = set_smem<M>(qpi_final_kernel<M>, smem);
     if (e != cudaSuccess) return e;
-    const long nl = (long)A * M;
-    qpi_final_kernel<M><<<(unsigned)((nl + P::B - 1) / P::B), P::THREADS, smem, s>>>(S, nl, field_out, bgf, bg_stride,
-                                                                                    phase, amp, twiddles(M)); note_launch();
+    qpi_final_kernel<M><<<(unsigned)((nl + P::B - 1) / P::B), P::THREADS, smem, s>>>(S, nl, carrier, field_out, bgf,
+                                                                                    bg_stride, phase, amp, twiddles(M));
+    note_launch();
     return cudaGetLastError();
 }
 
@@ -296,10 +358,10 @@ cudaError_t qpi_forward_window(const void *holo, int bpc, int A, int N, int M, c
     CTDM_DISPATCH_L(N, qpi_fwd_launch, holo, bpc, A, M, carrier, T1, S, s)
 }
 
-cudaError_t qpi_inverse_window(float2 *S, int A, int M, float2 *field_out, const float2 *bgf, long bg_stride,
-                               float *phase, float *amp, cudaStream_t s)
+cudaError_t qpi_inverse_window(float2 *S, int A, int M, const int *carrier, float2 *field_out, const float2 *bgf,
+                               long bg_stride, float *phase, float *amp, cudaStream_t s)
 {
-    CTDM_DISPATCH_L(M, qpi_inv_launch, S, A, field_out, bgf, bg_stride, phase, amp, s)
+    CTDM_DISPATCH_L(M, qpi_inv_launch, S, A, carrier, field_out, bgf, bg_stride, phase, amp, s)
 }
 
 // ------------------------------------------------------------ QPI Algorithm B

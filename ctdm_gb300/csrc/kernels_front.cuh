@@ -10,14 +10,17 @@ namespace ctdm {
 cudaError_t qpi_find_carrier(const float *bg, int N, float2 *scratch, unsigned long long *key, int *carrier,
                              cudaStream_t s);
 // Pruned forward transform of A holograms into their M x M window spectra S
-// (ifftshifted, masked).  T1: A*N*M complex scratch.
+// (ifftshifted, masked to the carrier's radius box: every entry of S is written, the
+// rows and columns outside the box with zeros).  T1: A*N*M complex scratch, of which
+// only the box's columns are used.
 // holo: A holograms of N x N pixels, bpc bytes each (4 float, 2 uint16, 1 uint8 counts)
 cudaError_t qpi_forward_window(const void *holo, int bpc, int A, int N, int M, const int *carrier, float2 *T1,
                                float2 *S, cudaStream_t s);
-// Inverse M x M transform of S (destroyed) and the epilogue: field_out != NULL
-// stores the complex field, otherwise phase/amp against bgf[a * bg_stride].
-cudaError_t qpi_inverse_window(float2 *S, int A, int M, float2 *field_out, const float2 *bgf, long bg_stride,
-                               float *phase, float *amp, cudaStream_t s);
+// Inverse M x M transform of an S written by qpi_forward_window with the same carrier
+// (destroyed; its zero rows are skipped) and the epilogue: field_out != NULL stores
+// the complex field, otherwise phase/amp against bgf[a * bg_stride].
+cudaError_t qpi_inverse_window(float2 *S, int A, int M, const int *carrier, float2 *field_out, const float2 *bgf,
+                               long bg_stride, float *phase, float *amp, cudaStream_t s);
 
 // QPI Algorithm B --------------------------------------------------------
 // Carrier column of one hologram from its y-downsampled row spectra (mag: N/4 * N
