@@ -113,8 +113,10 @@ void mark_kernel_configured(const void *fn, int dev);
 // clusters; sides without one return cudaErrorNotSupported / 0 clusters.
 cudaError_t plane_pass_256(const LoopArgs &a, bool final_pass, int variant, cudaStream_t s);
 int plane_clusters_256();
+cudaError_t plane_pass_512(const LoopArgs &a, bool final_pass, int variant, cudaStream_t s);
+int plane_clusters_512();
 // Loop scheme of side R on this device: 0 = x / y / z / y passes, 1 and 2 = plane + z
-// passes (plane pass register targets of 3 and 4 CTAs per SM).
+// passes (two cluster sizes per plane: 8 and 4 CTAs at R = 256, 16 and 8 at R = 512).
 int loop_scheme(int R);
 cudaError_t launch_plane(const LoopArgs &a, bool final_pass, cudaStream_t s);
 

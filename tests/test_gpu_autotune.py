@@ -57,13 +57,15 @@ def test_autotune_reports_all_variants(ctx):
     assert got == chosen and tuned
 
 
-def test_loop_schemes_agree_at_256(ctx, dev, oracle):
-    """The plane + z schemes (8- and 4-CTA cluster plane passes) and the x / y / z / y
-    scheme give the oracle's volume at 256^3, with and without the hit-mask predicate,
-    and each scheme runs its own passes (the stage timer sees y passes only in scheme 0)."""
+@pytest.mark.parametrize("r", [256, 512])
+def test_loop_schemes_agree(ctx, dev, oracle, r):
+    """The plane + z schemes (two cluster sizes of plane pass: 8 and 4 CTAs per plane at
+    256^3, 16 and 8 at 512^3) and the x / y / z / y scheme give the oracle's volume, with
+    and without the hit-mask predicate, and each scheme runs its own passes (the stage
+    timer sees y passes only in scheme 0)."""
     import ctdm_gb300 as C
     import torch
-    r, iters = 256, 3
+    iters = 3 if r == 256 else 2
     f2 = synthetic_f2(r, seed=7)
     counts = ((f2.real != 0) & (f2.imag != 0)).astype(np.uint32)
     d_f2 = torch.from_numpy(f2).to(dev)
