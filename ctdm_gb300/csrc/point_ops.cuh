@@ -84,24 +84,35 @@ __device__ __forceinline__ float2 modify_f(float2 n, float k2, float nm2)
 // nz = mod(round_half_away((f_z - f_z0)/df), R) with
 // f_z = sqrt(fm0^2 - (fx^2 + fy^2)), fx = ii df + fx0, fy = jj df + fy0; no sample
 // where the radicand is negative.  The rule is defined in IEEE double without
-// contraction.  A float evaluation in units of df decides it whenever the result
-// is farther from a decision boundary than 20x its worst-case rounding error
-// (radicand >= 4 df^2, fraction more than 0.02 away from one half); otherwise the
-// double rule runs.  ewald_nz_signed returns the unwrapped index (kNoSample where the
-// radicand is negative) and fz (1/m) for the value; ewald_nz wraps it into [0, R).
+// contraction.  A float evaluation in units of df decides it whenever its result is
+// farther from a decision boundary than twice a bound on its error; otherwise the
+// double rule runs.  The bound (u = 2^-24, F = fm0/df, the float constants rounded
+// from double): the radicand's error is at most E = 10 u F^2 (the constants' rounding,
+// fx0/df and fy0/df carried through the squares, the squares, the sum and the
+// difference, each within u of its value, every term at most F^2), so
+// |sqrt(rads) - sqrt(RAD)| <= E / fzs + u fzs, and with the rounding of fz0/df, of
+// t = fzs - fz0s and of its fraction the index fraction is within
+// u (E / (u fzs) + fzs + |fz0s| + |t| + 1) of the double rule's.  For 256^3 at
+// 0.1 um voxels (F = 64.3) that is about 1e-4 at the cap's centre instead of a fixed
+// 0.02 margin: the double rule runs for well under 1% of the samples instead of 4%,
+// whose divergent FP64 division and square root dominated the mapping.
+// ewald_nz_signed returns the unwrapped index (kNoSample where the radicand is
+// negative) and fz (1/m) for the value; ewald_nz wraps it into [0, R).
 constexpr int kNoSample = -0x40000000;
 __device__ __forceinline__ int ewald_nz_signed(int ii, int jj, const AngleGeom &g, double df, double fm02,
                                                float fm02s, float &fz)
 {
     const float fxs = (float)ii + g.fx0s, fys = (float)jj + g.fy0s;
     const float rads = fm02s - (fxs * fxs + fys * fys);
-    if (rads < -1.0f) return kNoSample;
-    if (rads >= 4.0f) {
+    const float er = 5.9604645e-7f * fm02s;   // E = 10 u F^2
+    if (rads < -1.0f - er) return kNoSample;
+    if (rads >= fmaxf(1.0f, er)) {
         const float fzs = sqrtf(rads);
         const float t = fzs - g.fz0s;
         const float fl = floorf(t);
         const float fr = t - fl;
-        if (fabsf(fr - 0.5f) > 0.02f) {
+        const float bound = 1.1920929e-7f * (er * 16777216.0f / fzs + fzs + fabsf(g.fz0s) + fabsf(t) + 1.0f);
+        if (fabsf(fr - 0.5f) > bound) {
             fz = fzs * (float)df;
             return (fr > 0.5f) ? (int)fl + 1 : (int)fl;
         }
