@@ -59,13 +59,36 @@ __device__ __forceinline__ float tile_median(float (*s)[35], int ly, int lx)
                    s[ly + 1][lx - 1], s[ly + 1][lx], s[ly + 1][lx + 1]);
 }
 
+// The same taps read from a staged block of the source map: rows sy0 .. sy0 + SS - 1 and
+// columns sx0 .. sx0 + SS - 1 at s[row - sy0][col - sx0] (taps past the map's edge were
+// staged as 0).
+constexpr int PREP_SS = 40;
+__device__ __forceinline__ float resize_staged(const float (*t)[PREP_SS + 1], int sx0, int sy0, float xr, int i,
+                                               int j)
+{
+    const int ix = (int)(xr * (float)i);
+    const float a = xr * (float)i - (float)ix;
+    const int iy = (int)(xr * (float)j);
+    const float b = xr * (float)j - (float)iy;
+    const int x = ix - sx0, y = iy - sy0;
+    const float d00 = t[y][x], d10 = t[y][x + 1], d01 = t[y + 1][x], d11 = t[y + 1][x + 1];
+    const float t1 = a * d10 + (-d00 * a + d00);
+    const float t2 = a * d11 + (-d01 * a + d01);
+    return b * t2 + (-t1 * b + t1);
+}
+
 // MODE 0: resize+crop from M x M maps.  MODE 1: input is already an R x R stack.
 // OUT 0: Rytov complex (transposed, swapped).  OUT 1: phase/amp stack.
+// MODE 0 stages the source block that a tile's taps read (once per source pixel instead
+// of four times per resized pixel) when it fits PREP_SS x PREP_SS, which holds for every
+// enlargement and slight shrink ((M - 1) / N up to about 1.1); else the taps read the
+// maps directly.
 template <int MODE, int OUT>
 __global__ void __launch_bounds__(256) prep_kernel(const float *__restrict__ phase, const float *__restrict__ amp,
                                                   int M, int N, int R, float2 *U0, float *ph_out, float *am_out)
 {
     __shared__ float sp[34][35], sa[34][35];
+    __shared__ float tp[MODE == 0 ? PREP_SS : 1][PREP_SS + 1], ta[MODE == 0 ? PREP_SS : 1][PREP_SS + 1];
     const int a = blockIdx.z;
     const int tx0 = blockIdx.x * 32, ty0 = blockIdx.y * 32;
     const long in_sz = MODE == 0 ? (long)M * M : (long)R * R;
@@ -74,14 +97,36 @@ __global__ void __launch_bounds__(256) prep_kernel(const float *__restrict__ pha
     const float xr = (float)(M - 1) / (float)N;
     const int off = (N - R) / 2;
     const int tid = threadIdx.y * 32 + threadIdx.x;
+    // source block of the tile's taps: the tap index (int)(xr i) grows with i, so the
+    // block spans the taps of the tile's first and last (halo) pixels plus one
+    const int ia = max(tx0 - 1, 0) + off, ib = min(tx0 + 32, R - 1) + off;
+    const int ja = max(ty0 - 1, 0) + off, jb = min(ty0 + 32, R - 1) + off;
+    const int sx0 = (int)(xr * (float)ia), sy0 = (int)(xr * (float)ja);
+    const int sw = (int)(xr * (float)ib) + 2 - sx0, sh = (int)(xr * (float)jb) + 2 - sy0;
+    const bool staged = MODE == 0 && sw <= PREP_SS && sh <= PREP_SS;   // the same for the whole CTA
+    if (staged) {
+        for (int e = tid; e < sw * sh; e += 256) {
+            const int lx = e % sw, ly = e / sw;
+            const int x = sx0 + lx, y = sy0 + ly;
+            const bool in = x < M && y < M;
+            tp[ly][lx] = in ? __ldg(&P[(long)y * M + x]) : 0.f;
+            ta[ly][lx] = in ? __ldg(&Am[(long)y * M + x]) : 0.f;
+        }
+        __syncthreads();
+    }
     for (int e = tid; e < 34 * 34; e += 256) {
         const int lx = e % 34, ly = e / 34;
         const int i = tx0 - 1 + lx, j = ty0 - 1 + ly;
         float pv = 0.f, av = 1.f;
         if (i >= 0 && i < R && j >= 0 && j < R) {
             if (MODE == 0) {
-                pv = resize_at(P, M, xr, i + off, j + off);
-                av = resize_at(Am, M, xr, i + off, j + off);
+                if (staged) {
+                    pv = resize_staged(tp, sx0, sy0, xr, i + off, j + off);
+                    av = resize_staged(ta, sx0, sy0, xr, i + off, j + off);
+                } else {
+                    pv = resize_at(P, M, xr, i + off, j + off);
+                    av = resize_at(Am, M, xr, i + off, j + off);
+                }
                 if (isnan(pv) || isinf(pv)) pv = 0.f;   // Combine2Stack scrub
                 if (isnan(av) || isinf(av)) av = 1.f;
             } else {
