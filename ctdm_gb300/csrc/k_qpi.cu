@@ -102,9 +102,12 @@ template <> struct QRows<1024> : fftl::PlanT<1024, 4, 64, fftl::Radices<16, 16, 
 template <> struct QRows<2048> : fftl::PlanT<2048, 2, 128, fftl::Radices<16, 16, 8>, fftl::Radices<8, 16, 16>> {};
 
 // Holograms arrive as float or as 16- / 8-bit camera counts (read as they are and
-// converted on load, exact: every count is an integer below 2^24).
+// converted on load, exact: every count is an integer below 2^24).  4 CTAs per SM (64
+// registers, no spills) instead of the 3 that 78 registers allowed: 412 -> 399 us for
+// QPI A over 121 x 1024^2 holograms.
 template <int N, class T>
-__global__ void __launch_bounds__(QRows<N>::THREADS) qpi_rows_kernel(const T *__restrict__ holo, float2 *T1,
+__global__ void __launch_bounds__(QRows<N>::THREADS, 1024 / QRows<N>::THREADS)
+    qpi_rows_kernel(const T *__restrict__ holo, float2 *T1,
                                                                     const int *__restrict__ carrier, long npairs,
                                                                     int M, const float2 *__restrict__ tw)
 {
@@ -166,7 +169,8 @@ template <> struct QCols<1024> : fftl::PlanT<1024, 4, 64, fftl::Radices<16, 16, 
 template <> struct QCols<2048> : fftl::PlanT<2048, 2, 128, fftl::Radices<16, 16, 8>, fftl::Radices<8, 16, 16>> {};
 
 template <int N>
-__global__ void __launch_bounds__(QCols<N>::THREADS) qpi_cols_kernel(const float2 *__restrict__ T1, float2 *S,
+__global__ void __launch_bounds__(QCols<N>::THREADS, 1024 / QCols<N>::THREADS)
+    qpi_cols_kernel(const float2 *__restrict__ T1, float2 *S,
                                                                     const int *__restrict__ carrier, long nlines,
                                                                     int M, const float2 *__restrict__ tw)
 {
