@@ -107,9 +107,8 @@ template <> struct QRows<2048> : fftl::PlanT<2048, 2, 128, fftl::Radices<16, 16,
 // QPI A over 121 x 1024^2 holograms.
 template <int N, class T>
 __global__ void __launch_bounds__(QRows<N>::THREADS, 1024 / QRows<N>::THREADS)
-    qpi_rows_kernel(const T *__restrict__ holo, float2 *T1,
-                                                                    const int *__restrict__ carrier, long npairs,
-                                                                    int M, const float2 *__restrict__ tw)
+    qpi_rows_kernel(const T *__restrict__ holo, float2 *T1, const int *__restrict__ carrier, long npairs, int M,
+                    const float2 *__restrict__ tw)
 {
     using P = QRows<N>;
     using Y = fftl::Lay<N, P::LP, true>;
@@ -170,9 +169,8 @@ template <> struct QCols<2048> : fftl::PlanT<2048, 2, 128, fftl::Radices<16, 16,
 
 template <int N>
 __global__ void __launch_bounds__(QCols<N>::THREADS, 1024 / QCols<N>::THREADS)
-    qpi_cols_kernel(const float2 *__restrict__ T1, float2 *S,
-                                                                    const int *__restrict__ carrier, long nlines,
-                                                                    int M, const float2 *__restrict__ tw)
+    qpi_cols_kernel(const float2 *__restrict__ T1, float2 *S, const int *__restrict__ carrier, long nlines, int M,
+                    const float2 *__restrict__ tw)
 {
     using P = QCols<N>;
     extern __shared__ float4 smem4[];
