@@ -330,3 +330,41 @@ def test_accelerated_loop_is_projected_fista(ctx, dev, r, iters):
     diff = np.sqrt(np.mean(np.abs(plain.cpu().numpy().astype(np.complex128) - ref) ** 2))
     assert diff > 10 * err        # momentum changes the iterates
     tape.close()
+
+
+def test_accelerated_loop_at_512_across_schemes(ctx, dev):
+    """At 512^3 the accelerated loop carries its momentum through the 16- or 8-CTA plane
+    pass or through the x pass of the line scheme; every scheme gives the library's own
+    projected FISTA (the gradient driver, an independent set of passes) to RI RMSE <= 1e-5."""
+    import torch
+    import ctdm_gb300 as C
+    r, iters = 512, 3
+    k2 = float((2 * np.pi * 1.337 / 532e-9) ** 2)
+    n_med = 1.337
+    rng = np.random.default_rng(512)
+    keep = rng.random((r, r, r), dtype=np.float32) < 0.05
+    amp = np.float32(1e-2 * k2 * np.sqrt(r ** 3 / 0.05))
+    F2 = np.zeros((r, r, r), np.complex64)
+    n = int(keep.sum())
+    F2[keep] = (rng.standard_normal(n, dtype=np.float32) + 1j * rng.standard_normal(n, dtype=np.float32)) * amp
+    dF2 = T(F2, dev)
+    del F2, keep
+    tape = C.Tape(dF2, r, k2)
+    Vg = torch.zeros((r, r, r), dtype=torch.complex64, device=dev)
+    tape.reconstruct(Vg, iters + 1, 0.0, 1.0, step=1.0, positivity=True)
+    ref = torch.empty_like(Vg)
+    C.contrast_to_ri(Vg, r, n_med, ref, clamp=True)
+    tape.close()
+    del Vg
+    out = torch.empty_like(dF2)
+    saved = C.loop_scheme(r)
+    try:
+        for scheme in (0, 1, 2):
+            C.set_loop_scheme(r, scheme)
+            ctx.positivity(dF2, r, iters, k2, n_med, out, accelerated=True)
+            torch.cuda.synchronize()
+            err = float(torch.sqrt(torch.mean(torch.abs(out - ref) ** 2)).item())
+            assert err < 1e-5, (scheme, err)
+            assert ctx.device_status() == 0
+    finally:
+        C.set_loop_scheme(r, saved)
