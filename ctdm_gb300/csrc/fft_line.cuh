@@ -77,25 +77,57 @@ __device__ __forceinline__ void dft8(float2 *a)
     a[3] = cadd(e3, o3); a[7] = csub(e3, o3);
 }
 
+// x exp(-+ 2 pi i 2/16) = h (1 -+ i) and x exp(-+ 2 pi i 6/16) = h (-1 -+ i): two adds and
+// two multiplies each
+template <bool INV>
+__device__ __forceinline__ float2 mul_w16_2(float2 a)
+{
+    const float h = 0.70710678118654752440f;
+    return INV ? make_float2(h * (a.x - a.y), h * (a.x + a.y)) : make_float2(h * (a.x + a.y), h * (a.y - a.x));
+}
+template <bool INV>
+__device__ __forceinline__ float2 mul_w16_6(float2 a)
+{
+    const float h = 0.70710678118654752440f;
+    return INV ? make_float2(-h * (a.x + a.y), h * (a.x - a.y)) : make_float2(h * (a.y - a.x), -h * (a.x + a.y));
+}
+
 template <bool INV>
 __device__ __forceinline__ void dft16(float2 *a)
 {
-    // cos(2 pi k/16), sin(2 pi k/16), k = 0..7
-    const float c[8] = {1.0f, 0.92387953251128675613f, 0.70710678118654752440f, 0.38268343236508977173f,
-                        0.0f, -0.38268343236508977173f, -0.70710678118654752440f, -0.92387953251128675613f};
-    const float s[8] = {0.0f, 0.38268343236508977173f, 0.70710678118654752440f, 0.92387953251128675613f,
-                        1.0f, 0.92387953251128675613f, 0.70710678118654752440f, 0.38268343236508977173f};
-    float2 e[8], o[8];
+    // 16 = 4 x 4 (n = 4 n1 + n2, k = k1 + 4 k2): four 4-point DFTs over n1, the twiddles
+    // W16^(n2 k1) (W^4 = -+i free, W^2 and W^6 by mul_w16_*), four 4-point DFTs over n2;
+    // 160 real operations against 172 for two 8-point halves
+    const float c1 = 0.92387953251128675613f, s1 = 0.38268343236508977173f;
+    float2 b[16];
 #pragma unroll
-    for (int k = 0; k < 8; k++) { e[k] = a[2 * k]; o[k] = a[2 * k + 1]; }
-    dft8<INV>(e);
-    dft8<INV>(o);
+    for (int n2 = 0; n2 < 4; n2++) {
+        b[4 * n2 + 0] = a[n2];
+        b[4 * n2 + 1] = a[4 + n2];
+        b[4 * n2 + 2] = a[8 + n2];
+        b[4 * n2 + 3] = a[12 + n2];
+        dft4<INV>(b[4 * n2 + 0], b[4 * n2 + 1], b[4 * n2 + 2], b[4 * n2 + 3]);
+    }
+    const float2 w1 = make_float2(c1, INV ? s1 : -s1);
+    const float2 w3 = make_float2(s1, INV ? c1 : -c1);
+    const float2 w9 = make_float2(-c1, INV ? -s1 : s1);
+    b[5] = cmul(b[5], w1);
+    b[6] = mul_w16_2<INV>(b[6]);
+    b[7] = cmul(b[7], w3);
+    b[9] = mul_w16_2<INV>(b[9]);
+    b[10] = cmul_mi<INV>(b[10]);
+    b[11] = mul_w16_6<INV>(b[11]);
+    b[13] = cmul(b[13], w3);
+    b[14] = mul_w16_6<INV>(b[14]);
+    b[15] = cmul(b[15], w9);
 #pragma unroll
-    for (int k = 0; k < 8; k++) {
-        float2 w = make_float2(c[k], INV ? s[k] : -s[k]);
-        float2 t = (k == 0) ? o[k] : cmul(o[k], w);
-        a[k] = cadd(e[k], t);
-        a[k + 8] = csub(e[k], t);
+    for (int k1 = 0; k1 < 4; k1++) {
+        float2 x0 = b[k1], x1 = b[4 + k1], x2 = b[8 + k1], x3 = b[12 + k1];
+        dft4<INV>(x0, x1, x2, x3);
+        a[k1] = x0;
+        a[k1 + 4] = x1;
+        a[k1 + 8] = x2;
+        a[k1 + 12] = x3;
     }
 }
 
