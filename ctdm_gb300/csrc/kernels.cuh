@@ -115,11 +115,8 @@ cudaError_t plane_pass_256(const LoopArgs &a, bool final_pass, int variant, cuda
 int plane_clusters_256();
 cudaError_t plane_pass_512(const LoopArgs &a, bool final_pass, int variant, cudaStream_t s);
 int plane_clusters_512();
-cudaError_t plane_pass_768(const LoopArgs &a, bool final_pass, int variant, cudaStream_t s);
-int plane_clusters_768();
 // Loop scheme of side R on this device: 0 = x / y / z / y passes, 1 and 2 = plane + z
-// passes (two cluster sizes or plans per plane: 8 and 4 CTAs at R = 256, 16 and 8 at R = 512,
-// 16 CTAs of two plans at R = 768).
+// passes (two cluster sizes per plane: 8 and 4 CTAs at R = 256, 16 and 8 at R = 512).
 int loop_scheme(int R);
 cudaError_t launch_plane(const LoopArgs &a, bool final_pass, cudaStream_t s);
 

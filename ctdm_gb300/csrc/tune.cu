@@ -110,7 +110,7 @@ static std::map<std::pair<int, int>, int> g_plane_ok;   // (device, R) -> cluste
 
 static bool plane_available(int R)
 {
-    if (R != 256 && R != 512 && R != 768) return false;
+    if (R != 256 && R != 512) return false;
     int dev = 0;
     cudaGetDevice(&dev);
     {
@@ -118,7 +118,7 @@ static bool plane_available(int R)
         auto it = g_plane_ok.find({dev, R});
         if (it != g_plane_ok.end()) return it->second > 0;
     }
-    const int n = R == 256 ? plane_clusters_256() : (R == 512 ? plane_clusters_512() : plane_clusters_768());
+    const int n = R == 256 ? plane_clusters_256() : plane_clusters_512();
     std::lock_guard<std::mutex> lk(g_tune_mu);
     g_plane_ok[{dev, R}] = n;
     return n > 0;
@@ -135,7 +135,6 @@ static cudaError_t plane_variant(const LoopArgs &a, bool final_pass, int scheme,
 {
     if (a.R == 256) return plane_pass_256(a, final_pass, scheme, s);
     if (a.R == 512) return plane_pass_512(a, final_pass, scheme, s);
-    if (a.R == 768) return plane_pass_768(a, final_pass, scheme, s);
     return cudaErrorNotSupported;
 }
 

@@ -173,40 +173,3 @@ def test_packed_z_pass_at_large_sides_bit_identical(ctx, dev, r, variant):
         C.set_plans(r, saved)
     del outs, f2
     torch.cuda.empty_cache()
-
-
-def test_loop_schemes_agree_at_768(ctx, dev):
-    """At 768^3 the plane + z schemes (16-CTA clusters, two line plans) give the volume of
-    the x / y / z / y scheme to float rounding (the FP64 loop at this size is beyond the
-    test's budget; the 256^3 and 512^3 schemes are checked against it above)."""
-    import ctdm_gb300 as C
-    import torch
-    r, iters = 768, 2
-    rng = np.random.default_rng(768)
-    keep = rng.random((r, r, r), dtype=np.float32) < 0.05
-    n = int(keep.sum())
-    f2 = np.zeros((r, r, r), np.complex64)
-    amp = np.float32(1e-2 * K2 * np.sqrt(r ** 3 / 0.05))
-    f2[keep] = (rng.standard_normal(n, dtype=np.float32) + 1j * rng.standard_normal(n, dtype=np.float32)) * amp
-    d_f2 = torch.from_numpy(f2).to(dev)
-    del f2, keep
-    out = torch.empty_like(d_f2)
-    saved = C.loop_scheme(r)
-    try:
-        C.set_loop_scheme(r, 0)
-        ctx.positivity(d_f2, r, iters, K2, N_MED, out)
-        torch.cuda.synchronize()
-        ref = out.clone()
-        for scheme in (1, 2):
-            C.set_loop_scheme(r, scheme)
-            ctx.set_timing(True)
-            ctx.positivity(d_f2, r, iters, K2, N_MED, out)
-            torch.cuda.synchronize()
-            st = ctx.stage_times()
-            ctx.set_timing(False)
-            assert st["y_inverse"][1] + st["y_forward"][1] == 0, (scheme, st)
-            err = float(torch.sqrt(torch.mean(torch.abs(out - ref) ** 2)).item())
-            assert err < 1e-6, (scheme, err)
-            assert ctx.device_status() == 0
-    finally:
-        C.set_loop_scheme(r, saved)
