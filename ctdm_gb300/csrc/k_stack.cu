@@ -59,6 +59,17 @@ __device__ __forceinline__ float tile_median(float (*s)[35], int ly, int lx)
                    s[ly + 1][lx - 1], s[ly + 1][lx], s[ly + 1][lx + 1]);
 }
 
+__device__ __forceinline__ float med3(float a, float b, float c) { return fmaxf(fminf(a, b), fminf(fmaxf(a, b), c)); }
+
+// The three values of a window column in order.
+__device__ __forceinline__ void sort3(float a, float b, float c, float &lo, float &md, float &hi)
+{
+    const float l = fminf(a, b), h = fmaxf(a, b);
+    lo = fminf(l, c);
+    hi = fmaxf(h, c);
+    md = fmaxf(l, fminf(h, c));
+}
+
 // The same taps read from a staged block of the source map: rows sy0 .. sy0 + SS - 1 and
 // columns sx0 .. sx0 + SS - 1 at s[row - sy0][col - sx0] (taps past the map's edge were
 // staged as 0).
@@ -139,15 +150,35 @@ __global__ void __launch_bounds__(256) prep_kernel(const float *__restrict__ pha
     }
     __syncthreads();
     const long rr = (long)R * R;
+    // MODE 0 (values scrubbed of NaN and inf above): a thread takes 4 adjacent pixels of
+    // one tile row, sorts the 6 window columns they span once, and takes each median as
+    // med3(max of the column minima, med3 of the column middles, min of the column
+    // maxima) over its 3 columns, the median of the 9 values.  MODE 1 keeps the
+    // 19-exchange network per pixel.
+    const int li0 = MODE == 0 ? 4 * (int)threadIdx.y : (int)threadIdx.y, lstep = MODE == 0 ? 1 : 8;
+    float plo[6], pmd[6], phv[6], alo[6], amd[6], ahv[6];
+    if constexpr (MODE == 0) {
+        const int lj = threadIdx.x;
+#pragma unroll
+        for (int c = 0; c < 6; c++) {
+            sort3(sp[lj][li0 + c], sp[lj + 1][li0 + c], sp[lj + 2][li0 + c], plo[c], pmd[c], phv[c]);
+            sort3(sa[lj][li0 + c], sa[lj + 1][li0 + c], sa[lj + 2][li0 + c], alo[c], amd[c], ahv[c]);
+        }
+    }
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-        const int li = threadIdx.y + 8 * k, lj = threadIdx.x;
+        const int li = li0 + lstep * k, lj = threadIdx.x;
         const int i = tx0 + li, j = ty0 + lj;
         if (i >= R || j >= R) continue;
         float pv, av;
         if (i == 0 || i == R - 1 || j == 0 || j == R - 1) {
             pv = sp[lj + 1][li + 1];
             av = sa[lj + 1][li + 1];
+        } else if constexpr (MODE == 0) {
+            pv = med3(fmaxf(fmaxf(plo[k], plo[k + 1]), plo[k + 2]), med3(pmd[k], pmd[k + 1], pmd[k + 2]),
+                      fminf(fminf(phv[k], phv[k + 1]), phv[k + 2]));
+            av = med3(fmaxf(fmaxf(alo[k], alo[k + 1]), alo[k + 2]), med3(amd[k], amd[k + 1], amd[k + 2]),
+                      fminf(fminf(ahv[k], ahv[k + 1]), ahv[k + 2]));
         } else {
             pv = tile_median(sp, lj + 1, li + 1);
             av = tile_median(sa, lj + 1, li + 1);
