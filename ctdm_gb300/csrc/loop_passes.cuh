@@ -47,7 +47,7 @@ static cudaError_t prep_plan_kernel(K kernel, int L, size_t smem)
 // CTA (0 when the occupancy query fails), once per kernel and device.  A z-pass CTA
 // prefetches into L2 the z lines of the CTA that starts when it ends, so that CTA's
 // strided loads (one 8 B x B segment per plane) find L2 instead of HBM: the pass's
-// loads all issue at its start, and with 3 CTAs per SM the transforms otherwise
+// loads all issue at its start, and with 3 or 4 CTAs per SM the transforms otherwise
 // leave HBM idle.  At 256^3 the packed z pass went from 77.6 to 69.2 us per launch in
 // the headline step (69.0 to 61.5 without Goldstein beside it).
 template <class P, class K>
