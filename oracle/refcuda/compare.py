@@ -11,6 +11,7 @@ does it), and times this library through its host-buffer entry point
 one call at a time) and with the holograms resident in HBM.
 
     python oracle/refcuda/compare.py [--configs plain_small,wrap_heavy,plain_512] [--reps 3] [--out FILE]
+    python oracle/refcuda/compare.py --qpib [--out FILE]   (QPI Algorithm B only)
 """
 import argparse
 import json
@@ -49,12 +50,66 @@ def workload(name):
 
 
 def build():
-    """The Release-flag binary (--use_fast_math, as the reference ships) and an IEEE one."""
+    """The Release-flag binaries (--use_fast_math, as the reference ships) and IEEE ones;
+    returns the pipeline binaries (the Algorithm B ones, ref_qpib, sit beside them)."""
     if not os.path.isdir(os.path.join(REF, "src")):
         raise SystemExit("oracle/_ref/refcuda/src is missing: run oracle/refcuda/assemble.py <reference root> first")
     subprocess.check_call(["make", "-s", "-j4", "-C", HERE])
     subprocess.check_call(["make", "-s", "-j4", "-C", HERE, "VARIANT=ieee"])
     return {"release": os.path.join(REF, "ref_pipeline"), "ieee": os.path.join(REF, "ieee", "ref_pipeline")}
+
+
+def qpib_workload(n=1024, angles=16, seed=6000):
+    """Holograms with the carrier along x, as QPI Algorithm B (a 1-D filter along x) needs."""
+    from ctdm_gb300 import phantom
+    return phantom.acquisition(n, n // 4, angles, seed=seed, pixel=0.1e-6 * 256 / n, carrier=(0.25, 0.0))
+
+
+def qpib_parity(O, exes, acq, ctx=None):
+    """QPI Algorithm B: the reference's own extractQPI_AlgorithmB + calcWrapPhase (both
+    builds) and, given a context, this library's ctdm_qpi_b, against the FP64 oracle on
+    the same holograms: carrier column, worst-frame wrapped-phase RMS and amplitude RMS.
+    The job loop's order: frame 1 takes its own carrier column, the background and every
+    later frame the background's."""
+    A, n = len(acq.ang_x), acq.n_holo
+    m = n // 4
+    ocb, ocs = O.qpib_center(acq.background), O.qpib_center(acq.holograms[0])
+    bgf = O.qpib_field(acq.background, ocb)
+    oracle_maps = [O.wrap_phase(O.qpib_field(acq.holograms[a], ocs if a == 0 else ocb), bgf) for a in range(A)]
+
+    def errors(ph, am):
+        pe = [float(np.sqrt(np.mean(wrap(ph[a] - oracle_maps[a][0]) ** 2))) for a in range(A)]
+        ae = [float(np.sqrt(np.mean((am[a] - oracle_maps[a][1]) ** 2))) for a in range(A)]
+        return {"wrapped_phase_rms_rad_max": max(pe), "amplitude_rmse_max": max(ae)}
+
+    out = {"frames": A, "hologram": n, "carrier_column_oracle": ocb, "carrier_column_frame1_oracle": ocs}
+    with tempfile.TemporaryDirectory() as tmp:
+        fin = os.path.join(tmp, "in.bin")
+        write_input(fin, acq, 1, (0, 0, 0))
+        for kind, exe in exes.items():
+            qexe = os.path.join(os.path.dirname(exe), "ref_qpib")
+            prefix = os.path.join(tmp, kind)
+            r = subprocess.run([qexe, fin, prefix], capture_output=True, text=True, timeout=1800)
+            if r.returncode != 0:
+                raise SystemExit(f"ref_qpib failed ({r.returncode}): {r.stderr[-2000:]}")
+            info = json.loads(r.stdout.strip().splitlines()[-1])
+            ph = np.fromfile(prefix + ".phase.f32", np.float32).reshape(A, m, m)
+            am = np.fromfile(prefix + ".amp.f32", np.float32).reshape(A, m, m)
+            out[f"reference_{kind}"] = dict(errors(ph, am), carrier_column=info["carrier_column"],
+                                            ms_per_frame=info["ms_per_frame"],
+                                            non_finite=int(np.count_nonzero(~np.isfinite(ph)) +
+                                                           np.count_nonzero(~np.isfinite(am))))
+    if ctx is not None:
+        import torch
+        dev = torch.device("cuda", ctx.device if hasattr(ctx, "device") else 0)
+        ph = torch.zeros((A, m, m), dtype=torch.float32, device=dev)
+        am = torch.zeros_like(ph)
+        cb, cs = ctx.qpi_b(n, torch.from_numpy(acq.holograms).to(dev), torch.from_numpy(acq.background).to(dev),
+                           ph, am, A)
+        torch.cuda.synchronize()
+        out["this_library"] = dict(errors(ph.cpu().numpy(), am.cpu().numpy()), carrier_column=cb,
+                                   carrier_column_frame1=cs)
+    return out
 
 
 def run_reference(exe, fin, reps, R, dump=None):
@@ -178,11 +233,21 @@ def main():
     ap.add_argument("--configs", default="plain_small,wrap_heavy,plain_512")
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--out", default=None)
+    ap.add_argument("--qpib", action="store_true",
+                    help="only QPI Algorithm B: the reference's own against the oracle and this library")
     args = ap.parse_args()
     import oracle as O
     from ctdm_gb300 import build as cbuild
     cbuild.build()
     exes = build()
+    if args.qpib:
+        import ctdm_gb300 as C
+        line = qpib_parity(O, exes, qpib_workload(), C.Context(0))
+        print(json.dumps(line))
+        if args.out:
+            with open(args.out, "w") as f:
+                json.dump(line, f, indent=1)
+        return
     lines = []
     for name in args.configs.split(","):
         iters, gold = CONFIGS[name]

@@ -63,3 +63,22 @@ def test_reference_stages_and_volume(compare, oracle, ctx, dev):
     assert np.isfinite(ref_vol).all()
     assert ref_err < 1e-3          # the reference's own float error (median race, float est_n, voxel rule)
     assert our_err < 1e-5
+
+
+def test_reference_qpi_b(compare, oracle, ctx):
+    """QPI Algorithm B (the reference's default method): the reference's own
+    extractQPI_AlgorithmB and calcWrapPhase (IEEE build) and this library's, each against
+    the FP64 oracle on the same holograms with the carrier along x."""
+    exes = compare.build()
+    acq = compare.qpib_workload(n=512, angles=4, seed=91)
+    res = compare.qpib_parity(oracle, {"ieee": exes["ieee"]}, acq, ctx)
+    ref, mine = res["reference_ieee"], res["this_library"]
+    print(res)
+    assert ref["non_finite"] == 0
+    assert ref["carrier_column"] == res["carrier_column_oracle"], res
+    assert mine["carrier_column"] == res["carrier_column_oracle"], res
+    assert mine["carrier_column_frame1"] == res["carrier_column_frame1_oracle"], res
+    assert ref["wrapped_phase_rms_rad_max"] < 1e-4, res   # the reference's float transforms
+    assert ref["amplitude_rmse_max"] < 1e-4, res
+    assert mine["wrapped_phase_rms_rad_max"] < 1e-4, res
+    assert mine["amplitude_rmse_max"] < 1e-5, res
