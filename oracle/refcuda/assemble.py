@@ -7,7 +7,8 @@ comparison build takes:
 
 * whole files, unmodified: cTDM/FFT.cu (cuFFT wrappers and shift / scale kernels),
   cTDM/Recon_kernel.cu (median, Ewald mapping, F/F2, est_n, modify, check),
-  cTDM/DCT_Unwrapping.cu and the headers they include;
+  cTDM/DCT_Unwrapping.cu, cTDM/FastUnwrapping.cu (driven by harness_fast.cu) and the
+  headers they include;
 * five functions cut verbatim from cTDM/HilbertTransform.cu by line range:
   extractQPI_AlgorithmA (:1546-1585), obtainRadius (:3425-3455), get1stOrder_new
   (:3566-3586), calcWrapPhase (:3618-3639) and bilinear_interpolation_kernel
@@ -33,7 +34,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(os.path.dirname(HERE), "_ref", "refcuda", "src")
 
 WHOLE = ["FFT.cu", "FFT.cuh", "Recon_kernel.cu", "Recon_kernel.cuh", "DCT_Unwrapping.cu", "DCT_Unwrapping.cuh",
-         "dct8x8_kernel2.cuh", "Common.h"]
+         "dct8x8_kernel2.cuh", "Common.h", "FastUnwrapping.cu", "FastUnwrapping.cuh"]
 
 # (first line, last line, text the first line must start with), 1-based inclusive
 CUTS = [

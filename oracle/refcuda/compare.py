@@ -12,6 +12,7 @@ one call at a time) and with the holograms resident in HBM.
 
     python oracle/refcuda/compare.py [--configs plain_small,wrap_heavy,plain_512] [--reps 3] [--out FILE]
     python oracle/refcuda/compare.py --qpib [--out FILE]   (QPI Algorithm B only)
+    python oracle/refcuda/compare.py --fastuw [--out FILE] (FastUnwrapping only)
 """
 import argparse
 import json
@@ -57,6 +58,59 @@ def build():
     subprocess.check_call(["make", "-s", "-j4", "-C", HERE])
     subprocess.check_call(["make", "-s", "-j4", "-C", HERE, "VARIANT=ieee"])
     return {"release": os.path.join(REF, "ref_pipeline"), "ieee": os.path.join(REF, "ieee", "ref_pipeline")}
+
+
+def fastuw_maps(m=256, count=4, seed=7000):
+    """Wrapped phase maps of smooth surfaces (several wraps across the map) with mild noise."""
+    rng = np.random.default_rng(seed)
+    y, x = np.mgrid[0:m, 0:m] / m
+    maps = []
+    for k in range(count):
+        a, b, c = rng.uniform(4, 8), rng.uniform(1.5, 3), rng.uniform(1.5, 3)
+        true = a * np.sin(b * x + k) * np.cos(c * y) + 3 * x + 0.02 * rng.standard_normal((m, m))
+        maps.append(wrap(true))
+    return np.stack(maps).astype(np.float32)
+
+
+def fastuw_parity(O, exes, maps, ctx=None):
+    """FastUnwrapping: the reference's own function (FTUP plans at the (2M)^2 its code
+    transforms) and, given a context, this library's, against the FP64 oracle: the input
+    normalised in place, and the unwrapped map (pixels within 1e-3 of the oracle's; the
+    congruence rounding of a pixel near a half turn may differ by 2 pi)."""
+    A, m = maps.shape[0], maps.shape[1]
+    oracle = [O.fast_unwrap(maps[a].astype(np.float64)) for a in range(A)]
+
+    def errors(unw, norm):
+        agree = [float(np.mean(np.abs(unw[a] - oracle[a][0]) < 1e-3)) for a in range(A)]
+        nerr = [float(np.sqrt(np.mean((norm[a] - oracle[a][1]) ** 2))) for a in range(A)]
+        return {"agree_fraction_min": min(agree), "normalised_rmse_max": max(nerr)}
+
+    out = {"maps": A, "side": m}
+    with tempfile.TemporaryDirectory() as tmp:
+        fin = os.path.join(tmp, "in.bin")
+        with open(fin, "wb") as f:
+            f.write(b"CTDMFU01")
+            f.write(np.array([m, A], np.int32).tobytes())
+            f.write(np.ascontiguousarray(maps, np.float32).tobytes())
+        for kind, exe in exes.items():
+            fexe = os.path.join(os.path.dirname(exe), "ref_fastuw")
+            prefix = os.path.join(tmp, kind)
+            r = subprocess.run([fexe, fin, prefix], capture_output=True, text=True, timeout=1800)
+            if r.returncode != 0:
+                raise SystemExit(f"ref_fastuw failed ({r.returncode}): {r.stderr[-2000:]}")
+            info = json.loads(r.stdout.strip().splitlines()[-1])
+            unw = np.fromfile(prefix + ".unwrapped.f32", np.float32).reshape(A, m, m)
+            norm = np.fromfile(prefix + ".normalised.f32", np.float32).reshape(A, m, m)
+            out[f"reference_{kind}"] = dict(errors(unw, norm), ms_per_map=info["ms_per_map"])
+    if ctx is not None:
+        import torch
+        dev = torch.device("cuda", 0)
+        t = torch.from_numpy(np.ascontiguousarray(maps)).to(dev)
+        o = torch.zeros_like(t)
+        ctx.unwrap_fast(t, o, A, m)
+        torch.cuda.synchronize()
+        out["this_library"] = errors(o.cpu().numpy(), t.cpu().numpy())
+    return out
 
 
 def qpib_workload(n=1024, angles=16, seed=6000):
@@ -235,14 +289,17 @@ def main():
     ap.add_argument("--out", default=None)
     ap.add_argument("--qpib", action="store_true",
                     help="only QPI Algorithm B: the reference's own against the oracle and this library")
+    ap.add_argument("--fastuw", action="store_true",
+                    help="only FastUnwrapping: the reference's own against the oracle and this library")
     args = ap.parse_args()
     import oracle as O
     from ctdm_gb300 import build as cbuild
     cbuild.build()
     exes = build()
-    if args.qpib:
+    if args.qpib or args.fastuw:
         import ctdm_gb300 as C
-        line = qpib_parity(O, exes, qpib_workload(), C.Context(0))
+        line = (qpib_parity(O, exes, qpib_workload(), C.Context(0)) if args.qpib
+                else fastuw_parity(O, exes, fastuw_maps(), C.Context(0)))
         print(json.dumps(line))
         if args.out:
             with open(args.out, "w") as f:

@@ -82,3 +82,18 @@ def test_reference_qpi_b(compare, oracle, ctx):
     assert ref["amplitude_rmse_max"] < 1e-4, res
     assert mine["wrapped_phase_rms_rad_max"] < 1e-4, res
     assert mine["amplitude_rmse_max"] < 1e-5, res
+
+
+def test_reference_fast_unwrapping(compare, oracle, ctx):
+    """FastUnwrapping: the reference's own function (with FTUP plans of the (2M)^2 size its
+    code transforms; the reference's driver creates them at (M/2)^2) and this library's,
+    each against the FP64 oracle: the in-place normalisation, and the unwrapped maps."""
+    exes = compare.build()
+    maps = compare.fastuw_maps(m=256, count=3, seed=71)
+    res = compare.fastuw_parity(oracle, {"ieee": exes["ieee"]}, maps, ctx)
+    ref, mine = res["reference_ieee"], res["this_library"]
+    print(res)
+    assert ref["normalised_rmse_max"] < 1e-6, res
+    assert mine["normalised_rmse_max"] < 1e-6, res
+    assert ref["agree_fraction_min"] > 0.999, res
+    assert mine["agree_fraction_min"] > 0.999, res
