@@ -19,7 +19,9 @@ comparison build takes:
   extractQPI_AlgorithmB (:1587-1606), sequence1DFFT (:1608-1662), real2cufft
   (:1664-1702), copySharedMem (:1704-1726), HistogramFT (:1728-1748), shiftArray
   (:1750-1763), CropFTdomain (:1811-1823), calcWrapPhase and
-  bilinear_interpolation_kernel, driven by oracle/refcuda/harness_b.cu.
+  bilinear_interpolation_kernel, driven by oracle/refcuda/harness_b.cu;
+* for the Goldstein residues, gold_res.cu: cudaPhaseResidues (cTDM/Goldstein.cu:52-103) and
+  cudaMod (:1193-1201), driven by oracle/refcuda/harness_res.cu.
 
 Output: oracle/_ref/refcuda/src/ (git-ignored; it travels with the tree to the GPU
 machine, where oracle/refcuda/Makefile builds it with nvcc and cuFFT).
@@ -107,13 +109,28 @@ __global__ void bilinear_interpolation_kernel(float *__restrict__ d_result_1, co
 """
 
 
-def cut(lines, cuts, prologue):
+# Goldstein residues: cudaPhaseResidues (cTDM/Goldstein.cu:52-103) and the cudaMod it calls
+# (:1193-1201), driven by harness_res.cu.
+CUTS_RES = [
+    (52, 103, "__global__ void cudaPhaseResidues("),
+    (1193, 1201, "__device__ float cudaMod("),
+]
+
+PROLOGUE_RES = """// Cut from cTDM/Goldstein.cu by oracle/refcuda/assemble.py (comparison build only).
+#define _USE_MATH_DEFINES
+#include <math.h>
+#include <cuda_runtime.h>
+__device__ float cudaMod(float a, float b);
+"""
+
+
+def cut(lines, cuts, prologue, name="HilbertTransform.cu"):
     parts = [prologue]
     for first, last, head in cuts:
         chunk = lines[first - 1:last]
         if not chunk or not chunk[0].startswith(head) or not chunk[-1].startswith("}"):
-            raise SystemExit(f"HilbertTransform.cu:{first}-{last} is not {head}... (reference changed?)")
-        parts.append(f"// cTDM/HilbertTransform.cu:{first}-{last}\n" + "\n".join(chunk) + "\n")
+            raise SystemExit(f"{name}:{first}-{last} is not {head}... (reference changed?)")
+        parts.append(f"// cTDM/{name}:{first}-{last}\n" + "\n".join(chunk) + "\n")
     return "\n".join(parts)
 
 
@@ -128,6 +145,10 @@ def main(root):
         f.write(cut(lines, CUTS, PROLOGUE))
     with open(os.path.join(OUT, "qpi_b.cu"), "w", encoding="latin-1") as f:
         f.write(cut(lines, CUTS_B, PROLOGUE_B))
+    # Goldstein.cu carries BIG5 comments: latin-1 keeps the bytes
+    glines = [ln.rstrip("\r") for ln in open(os.path.join(src, "Goldstein.cu"), encoding="latin-1").read().split("\n")]
+    with open(os.path.join(OUT, "gold_res.cu"), "w", encoding="latin-1") as f:
+        f.write(cut(glines, CUTS_RES, PROLOGUE_RES, "Goldstein.cu"))
     return OUT
 
 

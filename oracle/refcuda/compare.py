@@ -13,6 +13,7 @@ one call at a time) and with the holograms resident in HBM.
     python oracle/refcuda/compare.py [--configs plain_small,wrap_heavy,plain_512] [--reps 3] [--out FILE]
     python oracle/refcuda/compare.py --qpib [--out FILE]   (QPI Algorithm B only)
     python oracle/refcuda/compare.py --fastuw [--out FILE] (FastUnwrapping only)
+    python oracle/refcuda/compare.py --residues [--out FILE] (Goldstein residues only)
 """
 import argparse
 import json
@@ -110,6 +111,64 @@ def fastuw_parity(O, exes, maps, ctx=None):
         ctx.unwrap_fast(t, o, A, m)
         torch.cuda.synchronize()
         out["this_library"] = errors(o.cpu().numpy(), t.cpu().numpy())
+    return out
+
+
+def residue_maps(seed=7100):
+    """Wrapped phase maps with many residues: noisy tilted surfaces at three noise levels on
+    256^2, a ragged 100 x 37 one (the border rules of both edges), and a map drawn from
+    {0, +-pi, +-pi/2, +-1e-7} in float, whose differences land on the remainder's
+    boundaries (exactly +-pi, +-2 pi, and values that round to them)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for m, n, noise in [(256, 256, 0.6), (256, 256, 1.2), (256, 256, 2.5), (100, 37, 1.0)]:
+        y, x = np.mgrid[0:n, 0:m]
+        true = 0.7 * x + 0.2 * y + 3 * np.sin(x / 11.0) + noise * rng.standard_normal((n, m))
+        out.append(wrap(true).astype(np.float32))
+    pi = np.float32(np.pi)
+    vals = np.array([0, pi, -pi, pi / 2, -pi / 2, 1e-7, -1e-7], np.float32)
+    out.append(vals[rng.integers(0, len(vals), (128, 128))])
+    return out
+
+
+def residues_parity(O, exes, maps, ctx=None):
+    """Goldstein residues: the reference's own cudaPhaseResidues (each build) and, given a
+    context, this library's ctdm_goldstein charges, against the oracle's
+    or_goldstein_residues, map by map: the count of differing pixels (0 is bit-exact) and
+    the residue count."""
+    out = {"maps": [f"{m.shape[1]}x{m.shape[0]}" for m in maps]}
+    orc = [O.goldstein_residues(m) for m in maps]
+    out["residues_oracle"] = [int(np.count_nonzero(q)) for q in orc]
+    with tempfile.TemporaryDirectory() as tmp:
+        for kind, exe in exes.items():
+            rexe = os.path.join(os.path.dirname(exe), "ref_residues")
+            diff, ms = [], []
+            for i, m in enumerate(maps):
+                fin, prefix = os.path.join(tmp, f"in{i}.bin"), os.path.join(tmp, f"{kind}{i}")
+                with open(fin, "wb") as f:
+                    f.write(b"CTDMRS01")
+                    f.write(np.array([m.shape[1], m.shape[0], 1], np.int32).tobytes())
+                    f.write(np.ascontiguousarray(m, np.float32).tobytes())
+                r = subprocess.run([rexe, fin, prefix], capture_output=True, text=True, timeout=600)
+                if r.returncode != 0:
+                    raise SystemExit(f"ref_residues failed ({r.returncode}): {r.stderr[-2000:]}")
+                ms.append(json.loads(r.stdout.strip().splitlines()[-1])["ms_per_map"])
+                q = np.fromfile(prefix + ".charges.f32", np.float32).reshape(m.shape)
+                diff.append(int(np.count_nonzero(q != orc[i])))
+            out[f"reference_{kind}"] = {"pixels_differing": diff, "ms_per_map": ms}
+    if ctx is not None:
+        import torch
+        dev = torch.device("cuda", 0)
+        diff = []
+        for i, m in enumerate(maps):
+            h, w = m.shape
+            q = torch.zeros((1, h, w), dtype=torch.int8, device=dev)
+            c = torch.zeros((1, h, w), dtype=torch.uint8, device=dev)
+            o = torch.zeros((1, h, w), dtype=torch.float32, device=dev)
+            ctx.goldstein(torch.from_numpy(np.ascontiguousarray(m)).to(dev), q, c, o, 1, w, h)
+            torch.cuda.synchronize()
+            diff.append(int(np.count_nonzero(q[0].cpu().numpy() != orc[i])))
+        out["this_library"] = {"pixels_differing": diff}
     return out
 
 
@@ -291,15 +350,18 @@ def main():
                     help="only QPI Algorithm B: the reference's own against the oracle and this library")
     ap.add_argument("--fastuw", action="store_true",
                     help="only FastUnwrapping: the reference's own against the oracle and this library")
+    ap.add_argument("--residues", action="store_true",
+                    help="only the Goldstein residues: the reference's own against the oracle and this library")
     args = ap.parse_args()
     import oracle as O
     from ctdm_gb300 import build as cbuild
     cbuild.build()
     exes = build()
-    if args.qpib or args.fastuw:
+    if args.qpib or args.fastuw or args.residues:
         import ctdm_gb300 as C
         line = (qpib_parity(O, exes, qpib_workload(), C.Context(0)) if args.qpib
-                else fastuw_parity(O, exes, fastuw_maps(), C.Context(0)))
+                else fastuw_parity(O, exes, fastuw_maps(), C.Context(0)) if args.fastuw
+                else residues_parity(O, exes, residue_maps(), C.Context(0)))
         print(json.dumps(line))
         if args.out:
             with open(args.out, "w") as f:

@@ -7,7 +7,8 @@ reference checkout) or nvcc is missing.
 Stage by stage: the wrapped phase and amplitude of calcWrapPhase, the DCT unwrap, the
 Ewald hit counts (the reference decides the voxel index in float, the oracle in FP64:
 a few boundary voxels may differ) and F2; then the RI volumes of the reference, of the
-oracle and of this library."""
+oracle and of this library.  Beside them, one stage each: QPI Algorithm B, FastUnwrapping
+and the Goldstein residues (bit-exact)."""
 import os
 import shutil
 import sys
@@ -97,3 +98,15 @@ def test_reference_fast_unwrapping(compare, oracle, ctx):
     assert mine["normalised_rmse_max"] < 1e-6, res
     assert ref["agree_fraction_min"] > 0.999, res
     assert mine["agree_fraction_min"] > 0.999, res
+
+
+def test_reference_goldstein_residues(compare, oracle, ctx):
+    """Goldstein residues: the reference's own cudaPhaseResidues (IEEE and Release builds)
+    and this library's charges, bit-exact against the oracle, on noisy maps, a ragged one
+    and a map whose phase differences land on the remainder's boundaries."""
+    exes = compare.build()
+    res = compare.residues_parity(oracle, exes, compare.residue_maps(seed=73), ctx)
+    print(res)
+    assert min(res["residues_oracle"]) > 100, res
+    assert res["reference_ieee"]["pixels_differing"] == [0] * len(res["maps"]), res
+    assert res["this_library"]["pixels_differing"] == [0] * len(res["maps"]), res
