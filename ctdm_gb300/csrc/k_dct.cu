@@ -125,6 +125,42 @@ __device__ __forceinline__ float2 idct_input(const float *X, int p, int M, const
     return make_float2(w.y * v2, -w.x * v2);
 }
 
+// Two real lines per complex transform.  Every line of the three passes is real (the
+// mirrored rows and columns of the forward transforms) or has only its real part kept
+// (the inverse transforms), so a CTA of the plan's B complex lines covers 2B real
+// lines, line 2b in the real and line 2b + 1 in the imaginary part of complex line b.
+// Forward: Z = FFT(z_a + i z_b) gives Y_a[k] = (Z[k] + conj Z[-k]) / 2 and
+// Y_b[k] = (Z[k] - conj Z[-k]) / 2i.  Inverse: the reference keeps Re IFFT(V) of the
+// countIDCT input V, and Re IFFT(V) = IFFT(H) with H[p] = (V[p] + conj V[-p]) / 2
+// (Hermitian, so its transform is real); IFFT(H_a + i H_b) = x_a + i x_b.  Half the
+// transforms of the one-line-per-transform form, the same results up to float rounding.
+template <int L2>
+__host__ __device__ constexpr int dct_lines_per_cta()
+{
+    return 2 * DctPlan<L2>::B;
+}
+
+// Y_a, Y_b of the two real lines packed in complex line `line` (length L2, stride 1).
+__device__ __forceinline__ void unpack_pair(const float2 *line, int k, int L2, float2 &ya, float2 &yb)
+{
+    const float2 z = line[k];
+    const float2 r = line[k == 0 ? 0 : L2 - k];   // Z[-k]
+    ya = make_float2(0.5f * (z.x + r.x), 0.5f * (z.y - r.y));
+    yb = make_float2(0.5f * (z.y + r.y), -0.5f * (z.x - r.x));
+}
+
+// H_a + i H_b at point p of the inverse input of the two coefficient rows Xa, Xb.
+__device__ __forceinline__ float2 idct_pair_input(const float *Xa, const float *Xb, int p, int M,
+                                                  const float2 *__restrict__ dtw, float dT, int mode)
+{
+    const int q = p == 0 ? 0 : 2 * M - p;
+    const float2 a0 = idct_input(Xa, p, M, dtw, dT, mode), a1 = idct_input(Xa, q, M, dtw, dT, mode);
+    const float2 b0 = idct_input(Xb, p, M, dtw, dT, mode), b1 = idct_input(Xb, q, M, dtw, dT, mode);
+    const float2 ha = make_float2(0.5f * (a0.x + a1.x), 0.5f * (a0.y - a1.y));
+    const float2 hb = make_float2(0.5f * (b0.x + b1.x), 0.5f * (b0.y - b1.y));
+    return make_float2(ha.x - hb.y, ha.y + hb.x);
+}
+
 // Pass 1: rows.  phi: A x M x M; T: A x M x M (row DCT coefficients, [a][y][kx]).
 template <int L2>
 __global__ void __launch_bounds__(DctPlan<L2>::THREADS, dct_min_ctas<DctPlan<L2>>())
@@ -132,19 +168,19 @@ __global__ void __launch_bounds__(DctPlan<L2>::THREADS, dct_min_ctas<DctPlan<L2>
                     const float2 *__restrict__ dtw, const float2 *__restrict__ tw)
 {
     using P = DctPlan<L2>;
-    constexpr int M = L2 / 2;
+    constexpr int M = L2 / 2, RL = dct_lines_per_cta<L2>();
     extern __shared__ float4 smem4[];
     float2 *buf = reinterpret_cast<float2 *>(smem4);
-    const long line0 = (long)blockIdx.x * P::B;
-    // map and row of the CTA's first line; a line b further on is y0 + b rows later
+    const long line0 = (long)blockIdx.x * RL;
+    // map and row of the CTA's first line; a line j further on is y0 + j rows later
     const long a0 = line0 / M;
     const int y0 = (int)(line0 - a0 * M);
-    if constexpr (P::B <= M) {
-        // B divides M, so the CTA's lines are rows y0 .. y0 + B - 1 of one map: rows
-        // y0 - 1 .. y0 + B are staged in shared memory by independent coalesced loads
+    if constexpr (RL <= M) {
+        // RL divides M, so the CTA's lines are rows y0 .. y0 + RL - 1 of one map: rows
+        // y0 - 1 .. y0 + RL are staged in shared memory by independent coalesced loads
         // (a thread's loads are all in flight together), and the Laplacian is taken
-        // from there.  The staging fits in the line buffer: (B + 2) M floats <= 4 B M.
-        constexpr int SR = P::B + 2, NS = (SR * M + P::THREADS - 1) / P::THREADS, PER = M / P::T;
+        // from there.  The staging fits in the line buffer: (RL + 2) M floats <= 4 B M.
+        constexpr int SR = RL + 2, NS = (SR * M + P::THREADS - 1) / P::THREADS, PER = M / P::T;
         float *S = reinterpret_cast<float *>(buf);
         const float *map = phi + a0 * (long)M * M;
         const bool live = line0 < nlines;
@@ -157,38 +193,43 @@ __global__ void __launch_bounds__(DctPlan<L2>::THREADS, dct_min_ctas<DctPlan<L2>
             }
         }
         __syncthreads();
-        float v[PER];
+        float2 v[PER];
 #pragma unroll
         for (int k = 0; k < PER; ++k) {
             const int e = threadIdx.x + k * P::THREADS;
             const int b = e / M, x = e - b * M;
-            v[k] = lap_rows(S + (b + 1) * M, x, y0 + b, M);
+            v[k] = make_float2(lap_rows(S + (2 * b + 1) * M, x, y0 + 2 * b, M),
+                               lap_rows(S + (2 * b + 2) * M, x, y0 + 2 * b + 1, M));
         }
         __syncthreads();
 #pragma unroll
         for (int k = 0; k < PER; ++k) {
             const int e = threadIdx.x + k * P::THREADS;
             const int b = e / M, x = e - b * M;
-            buf[b * P::LP + x] = make_float2(v[k], 0.f);
-            buf[b * P::LP + (L2 - 1 - x)] = make_float2(v[k], 0.f);
+            buf[b * P::LP + x] = v[k];
+            buf[b * P::LP + (L2 - 1 - x)] = v[k];
         }
     } else {
-        // maps smaller than B lines: the CTA covers several maps
+        // maps smaller than RL lines: the CTA covers several maps
         for (int e = threadIdx.x; e < P::B * M; e += P::THREADS) {
             const int b = e / M, x = e - b * M;
-            const long l = line0 + b;
-            float v = 0.f;
-            if (l < nlines) {
-                int y = y0 + b;
-                long a = a0;
-                while (y >= M) {
-                    y -= M;
-                    a++;
+            float v[2];
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const long l = line0 + 2 * b + h;
+                v[h] = 0.f;
+                if (l < nlines) {
+                    int y = y0 + 2 * b + h;
+                    long a = a0;
+                    while (y >= M) {
+                        y -= M;
+                        a++;
+                    }
+                    v[h] = lap_at(phi + a * (long)M * M, x, y, M);
                 }
-                v = lap_at(phi + a * (long)M * M, x, y, M);
             }
-            buf[b * P::LP + x] = make_float2(v, 0.f);
-            buf[b * P::LP + (L2 - 1 - x)] = make_float2(v, 0.f);
+            buf[b * P::LP + x] = make_float2(v[0], v[1]);
+            buf[b * P::LP + (L2 - 1 - x)] = make_float2(v[0], v[1]);
         }
     }
     __syncthreads();
@@ -196,62 +237,74 @@ __global__ void __launch_bounds__(DctPlan<L2>::THREADS, dct_min_ctas<DctPlan<L2>
     const float dT = 1.0f / sqrtf((float)L2);
     for (int e = threadIdx.x; e < P::B * M; e += P::THREADS) {
         const int b = e / M, k = e - b * M;
-        const long l = line0 + b;
-        if (l < nlines) T[l * M + k] = dct_from_fft(buf[b * P::LP + k], k, dtw, dT);
+        const long l = line0 + 2 * b;   // nlines is even: l < nlines covers both lines
+        if (l < nlines) {
+            float2 ya, yb;
+            unpack_pair(buf + b * P::LP, k, L2, ya, yb);
+            T[l * M + k] = dct_from_fft(ya, k, dtw, dT);
+            T[(l + 1) * M + k] = dct_from_fft(yb, k, dtw, dT);
+        }
     }
 }
 
-// Row stride of the column pass's coefficient staging: a warp holds min(B, 32) lines
-// at 32 / B consecutive positions each, so a stride of M (a multiple of 32 from M = 32
-// up) plus 32 / B puts all of them on distinct banks.
+// Row stride of the column pass's coefficient staging (2B rows, rows 2b and 2b + 1 for
+// complex line b): a warp holds min(B, 32) complex lines at 32 / B consecutive
+// positions each, so rows 2b need 2 x stride = 32 / B (mod 32), a stride of M (a
+// multiple of 16) plus 16 / B, to fall on distinct banks.
 template <int L2>
 __host__ __device__ constexpr int x_stride(int M)
 {
-    return M + (DctPlan<L2>::B >= 32 ? 1 : 32 / DctPlan<L2>::B);
+    return M + (DctPlan<L2>::B >= 16 ? 1 : 16 / DctPlan<L2>::B);
 }
 
-// Pass 2: columns.  Line l = kx + M*a, element y at T[a*M*M + y*M + kx].
+// Pass 2: columns.  Real line l = kx + M*a, element y at T[a*M*M + y*M + kx]; complex
+// line b holds columns kx, kx + 1 (kx even), read and written as float2.
 template <int L2>
 __global__ void __launch_bounds__(DctPlan<L2>::THREADS, dct_min_ctas<DctPlan<L2>>())
     dct_cols_kernel(float *T, long nlines, int /* M = L2 / 2 */, int mode, const float2 *__restrict__ dtw,
                     const float *__restrict__ eig, const float2 *__restrict__ tw)
 {
     using P = DctPlan<L2>;
-    constexpr int M = L2 / 2;
+    constexpr int M = L2 / 2, RL = dct_lines_per_cta<L2>();
     extern __shared__ float4 smem4[];
     float2 *buf = reinterpret_cast<float2 *>(smem4);
-    float *X = reinterpret_cast<float *>(buf + P::B * P::LP);   // B rows of x_stride(M)
-    const long line0 = (long)blockIdx.x * P::B;
+    float *X = reinterpret_cast<float *>(buf + P::B * P::LP);   // 2B rows of x_stride(M)
+    const long line0 = (long)blockIdx.x * RL;
     const int b = threadIdx.x % P::B, t = threadIdx.x / P::B;
-    float *Xb = X + b * x_stride<L2>(M);
-    const long l = line0 + b;
+    float *Xa = X + (2 * b) * x_stride<L2>(M), *Xb = Xa + x_stride<L2>(M);
+    const long l = line0 + 2 * b;   // nlines is even: l < nlines covers both lines
     const bool ok = l < nlines;
     const int kx = ok ? (int)(l % M) : 0;
     const long a = ok ? l / M : 0;
-    float *col = T + a * (long)M * M + kx;
+    float2 *col = reinterpret_cast<float2 *>(T + a * (long)M * M + kx);   // kx even: 8-byte aligned
     for (int y = t; y < M; y += P::T) {
-        const float v = ok ? col[(long)y * M] : 0.f;
-        buf[b * P::LP + y] = make_float2(v, 0.f);
-        buf[b * P::LP + (L2 - 1 - y)] = make_float2(v, 0.f);
+        const float2 v = ok ? col[(long)y * (M / 2)] : make_float2(0.f, 0.f);
+        buf[b * P::LP + y] = v;
+        buf[b * P::LP + (L2 - 1 - y)] = v;
     }
     __syncthreads();
     P::template run<false>(buf, tw);
     const float dT = 1.0f / sqrtf((float)L2);
-    const float ex = __ldg(&eig[kx]);
+    const float exa = __ldg(&eig[kx]), exb = __ldg(&eig[kx + 1]);
     for (int ky = t; ky < M; ky += P::T) {
-        float v = dct_from_fft(buf[b * P::LP + ky], ky, dtw, dT);
+        float2 ya, yb;
+        unpack_pair(buf + b * P::LP, ky, L2, ya, yb);
+        float va = dct_from_fft(ya, ky, dtw, dT), vb = dct_from_fft(yb, ky, dtw, dT);
         // devConstant (:300-311): / (2cos(4 pi i/(4M-1)) + 2cos(4 pi j/(4M-1)) - 4), (0,0) -> 0;
         // the denominator is -(4 sin^2(2 pi i/(4M-1)) + 4 sin^2(2 pi j/(4M-1))), free of cancellation
-        if (kx == 0 && ky == 0) v = 0.f;
-        else v = v / (-(ex + __ldg(&eig[ky])));
-        Xb[ky] = v;
+        const float ey = __ldg(&eig[ky]);
+        if (kx == 0 && ky == 0) va = 0.f;
+        else va = va / (-(exa + ey));
+        vb = vb / (-(exb + ey));
+        Xa[ky] = va;
+        Xb[ky] = vb;
     }
     __syncthreads();
-    for (int p = t; p < L2; p += P::T) buf[b * P::LP + p] = idct_input(Xb, p, M, dtw, dT, mode);
+    for (int p = t; p < L2; p += P::T) buf[b * P::LP + p] = idct_pair_input(Xa, Xb, p, M, dtw, dT, mode);
     __syncthreads();
     P::template run<true>(buf, tw);
     if (!ok) return;
-    for (int y = t; y < M; y += P::T) col[(long)y * M] = buf[b * P::LP + y].x;
+    for (int y = t; y < M; y += P::T) col[(long)y * (M / 2)] = buf[b * P::LP + y];
 }
 
 // Pass 3: rows inverse.  T: [a][y][kx] -> out [a][y][x].
@@ -261,28 +314,32 @@ __global__ void __launch_bounds__(DctPlan<L2>::THREADS, dct_min_ctas<DctPlan<L2>
                         const float2 *__restrict__ dtw, const float2 *__restrict__ tw)
 {
     using P = DctPlan<L2>;
-    constexpr int M = L2 / 2;
+    constexpr int M = L2 / 2, RL = dct_lines_per_cta<L2>();
     extern __shared__ float4 smem4[];
     float2 *buf = reinterpret_cast<float2 *>(smem4);
-    float *X = reinterpret_cast<float *>(buf + P::B * P::LP);
-    const long line0 = (long)blockIdx.x * P::B;
-    for (int e = threadIdx.x; e < P::B * M; e += P::THREADS) {
-        const int b = e / M, k = e - b * M;
-        const long l = line0 + b;
-        X[b * M + k] = (l < nlines) ? T[l * M + k] : 0.f;
+    float *X = reinterpret_cast<float *>(buf + P::B * P::LP);   // 2B rows of M
+    const long line0 = (long)blockIdx.x * RL;
+    for (int e = threadIdx.x; e < RL * M; e += P::THREADS) {
+        const int j = e / M, k = e - j * M;
+        const long l = line0 + j;
+        X[j * M + k] = (l < nlines) ? T[l * M + k] : 0.f;
     }
     __syncthreads();
     const float dT = 1.0f / sqrtf((float)L2);
     for (int e = threadIdx.x; e < P::B * L2; e += P::THREADS) {
         const int b = e / L2, p = e - b * L2;
-        buf[b * P::LP + p] = idct_input(X + b * M, p, M, dtw, dT, mode);
+        buf[b * P::LP + p] = idct_pair_input(X + (2 * b) * M, X + (2 * b + 1) * M, p, M, dtw, dT, mode);
     }
     __syncthreads();
     P::template run<true>(buf, tw);
     for (int e = threadIdx.x; e < P::B * M; e += P::THREADS) {
         const int b = e / M, x = e - b * M;
-        const long l = line0 + b;
-        if (l < nlines) out[l * M + x] = buf[b * P::LP + x].x;
+        const long l = line0 + 2 * b;
+        if (l < nlines) {
+            const float2 o = buf[b * P::LP + x];
+            out[l * M + x] = o.x;
+            out[(l + 1) * M + x] = o.y;
+        }
     }
 }
 
@@ -299,9 +356,10 @@ static cudaError_t dct_launch(const float *phi, float *out, float *T, int A, int
 {
     using P = DctPlan<L2>;
     const long nl = (long)A * M;
-    const unsigned grid = (unsigned)((nl + P::B - 1) / P::B);
+    constexpr int RL = dct_lines_per_cta<L2>();
+    const unsigned grid = (unsigned)((nl + RL - 1) / RL);
     const size_t smem1 = fftl::plan_smem<P>();
-    const size_t smem2 = smem1 + sizeof(float) * P::B * x_stride<L2>(M);
+    const size_t smem2 = smem1 + sizeof(float) * RL * x_stride<L2>(M);
     const float2 *dtw = dct_twiddles(M);
     const float2 *tw = twiddles(L2);
     if (!dtw || !tw || !dct_eigen(M)) return cudaErrorInitializationError;   // device tables not built
@@ -336,9 +394,10 @@ static cudaError_t dct_launch_explicit(const float *phi, float *out, float *T, i
 {
     using P = DctPlan<L2>;
     const long nl = (long)A * M;
-    const unsigned grid = (unsigned)((nl + P::B - 1) / P::B);
+    constexpr int RL = dct_lines_per_cta<L2>();
+    const unsigned grid = (unsigned)((nl + RL - 1) / RL);
     const size_t smem1 = fftl::plan_smem<P>();
-    const size_t smem2 = smem1 + sizeof(float) * P::B * x_stride<L2>(M);
+    const size_t smem2 = smem1 + sizeof(float) * RL * x_stride<L2>(M);
     cudaError_t e = set_smem2<L2>(dct_rows_kernel<L2>, smem1);
     if (e != cudaSuccess) return e;
     dct_rows_kernel<L2><<<grid, P::THREADS, smem1, s>>>(phi, T, nl, M, dtw, tw); note_launch();
