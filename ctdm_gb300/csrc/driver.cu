@@ -115,9 +115,12 @@ struct KV {
     std::string key, value;
 };
 
-// Every "key=value" of a parameter file in order.  Like fscanf("%*[^=]%s") the value
-// is the white-space free token after '=' (leading spaces are skipped here, where the
-// reference would read an empty value); the key is the last word before '='.
+// Every "key=value" of a parameter file in order, the way scriptFileRead reads them
+// (:96-120): fscanf("%*[^=]%s") skips to the next '=' and takes the white-space free
+// token from there, and obtainParameter (:200-221) keeps the last non-empty piece of
+// that token split at '=' ("=a=b" gives "b").  Spaces after '=' are skipped here, where
+// the reference would read a token of '=' alone and return an unset pointer.  The key
+// is the last word before '='.
 std::vector<KV> key_values(const std::string &text)
 {
     std::vector<KV> out;
@@ -132,8 +135,13 @@ std::vector<KV> key_values(const std::string &text)
         size_t b = eq + 1;
         while (b < text.size() && (text[b] == ' ' || text[b] == '\t')) b++;
         size_t e = b;
-        while (e < text.size() && !isspace((unsigned char)text[e]) && text[e] != '=') e++;
-        out.push_back({text.substr(kb, ke - kb), text.substr(b, e - b)});
+        while (e < text.size() && !isspace((unsigned char)text[e])) e++;
+        // the last non-empty '='-separated piece of [b, e)
+        size_t ve = e;
+        while (ve > b && text[ve - 1] == '=') ve--;
+        size_t vb = ve;
+        while (vb > b && text[vb - 1] != '=') vb--;
+        out.push_back({text.substr(kb, ke - kb), text.substr(vb, ve - vb)});
         pos = e;
     }
     return out;

@@ -11,6 +11,12 @@ stall.  Skipped where the assembled sources are absent.
 Bars: the flood fill and the resize bit-exact (the oracle evaluates the same float
 expressions); the transforms within float rounding (the reference stores float between
 the axes, the oracle keeps FP64 throughout); the octant swap exact.
+
+The same binary runs the reference's job-list and parameter-file reading
+(scriptFileRead, obtainParameter; a stand-in HilbertTransform records each job), its
+frame reader (bmp_header, read_bmp), its .phimap writer (outputImg) and its frame check
+(checkArray), against this library's host functions through the C ABI: parsed fields,
+stored bytes, written bytes and check results equal.
 """
 import os
 import subprocess
@@ -31,6 +37,12 @@ def ref_cpu():
         pytest.skip("oracle/_ref/refcpu/src is missing: the reference checkout was not present at build time")
     subprocess.check_call(["make", "-s", "-C", REFCPU], timeout=300)
     return EXE
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from ctdm_gb300 import _lib
+    return _lib.load()
 
 
 def run(exe, op, header, payload, dtype, count, timeout=120):
@@ -133,3 +145,131 @@ def test_octant_shift_matches_reference(ref_cpu, oracle, w, h, s):
     c = cnoise((s, h, w), w * h * s)
     ref = run(ref_cpu, "shift3d", [w, h, s], [c], np.complex64, c.size).reshape(c.shape)
     assert np.array_equal(ref, oracle.shift3d(c).astype(np.complex64))
+
+
+# ---------------------------------------------------------------- job files and frame formats
+def run_paths(exe, op, src, out, timeout=60):
+    r = subprocess.run([exe, op, str(src), str(out)], timeout=timeout, capture_output=True)
+    assert r.returncode == 0, (op, r.returncode, r.stderr[-400:])
+
+
+JOB3 = """# parameter file with notes before the keys
+sample folder   SPDir={d}/SP
+background BGDir={d}/BG
+AngDir={d}/Ang
+SaveDir={d}/out=run7
+rowPts0=12abc
+rowPts1=1035
+colPts0=0
+colPts1=1023
+ReconFlag=2.9
+ReconSave=1
+SizeType=1
+ResizeFlag=0
+Nmed=1.333e0
+Mag=62.5
+CameraPixelSize=6.5
+wavelength=0.532e3
+SavePhaseStack=1.7
+SaveAmpStack=0
+criteriaRange=9.42477796076938
+criteriaSTD=0.25
+"""
+
+
+def test_job_list_matches_reference(ref_cpu, tmp_path):
+    """scriptFileRead (cTDM/HilbertTransform.cu:70-175) with obtainParameter, on a job
+    list of three parameter files, against ctdm_parse_job_file: the 20 fields in order,
+    including notes before the keys, integers read by atoi from decimals and trailing
+    text, exponents, and a value with '=' in it (the reference keeps its last piece).
+    The reference ignores the optional fields after the 20th.  No value here has a space
+    after its '=': the reference then reads a token of '=' alone and returns an unset
+    pointer, where this library skips the spaces."""
+    from ctdm_gb300 import jobs
+    d = str(tmp_path)
+    p1 = jobs.write_job_file(tmp_path / "job1.txt", optional=False, sp_dir=d + "/SP", bg_dir=d + "/BG",
+                             ang_dir=d + "/Ang", save_dir=d + "/Save", row_pts=(0, 511), col_pts=(10, 521),
+                             recon_flag=2, n_med=1.337, mag=62.5, camera_pixel_um=6.5, wavelength_nm=532.5,
+                             criteria_range=7.25, criteria_std=0.75)
+    p2 = jobs.write_job_file(tmp_path / "job2.txt", optional=True, sp_dir=d + "/a", bg_dir=d + "/b",
+                             ang_dir=d + "/c", save_dir=d + "/e", recon_flag=0, recon_save=2, qpi_method=1,
+                             iter_time=19, n_med=1.3371234567890123)
+    p3 = tmp_path / "job3.txt"
+    p3.write_text(JOB3.format(d=d))
+    lst = tmp_path / "JobList.txt"
+    lst.write_text(f"{p1}\n{p2}\n{p3}\n")
+    out = tmp_path / "jobs.json"
+    run_paths(ref_cpu, "joblist", lst, out)
+    import json
+    ref = [json.loads(x) for x in out.read_text().splitlines()]
+    assert len(ref) == 3
+    keys = ["sp_dir", "bg_dir", "ang_dir", "save_dir", "row_pts", "col_pts", "recon_flag", "recon_save",
+            "size_type", "resize_flag", "n_med", "mag", "camera_pixel_um", "wavelength_nm", "save_phase_stack",
+            "save_amp_stack", "criteria_range", "criteria_std"]
+    for path, r in zip((p1, p2, p3), ref):
+        mine = jobs.job_dict(jobs.parse_job_file(path))
+        assert {k: mine[k] for k in keys} == {k: r[k] for k in keys}, path
+    assert ref[2]["save_dir"] == "run7" and ref[2]["recon_flag"] == 2 and ref[2]["row_pts"] == [12, 1035]
+
+
+@pytest.mark.parametrize("h,w", [(8, 8), (30, 30), (64, 64), (8, 30)])
+def test_bmp_reader_matches_reference(ref_cpu, tmp_path, h, w):
+    """bmp_header + read_bmp (cTDM/HilbertTransform.cu:2680-2731) against ctdm_read_bmp:
+    the same header fields and storage bytes, padded lines included (the reference reads
+    width as its row count, so a wide picture is stored the same odd way by both)."""
+    from ctdm_gb300 import dataset, jobs
+    pic = np.random.default_rng(h * 100 + w).integers(0, 256, (h, w), dtype=np.uint8)
+    path, out = tmp_path / "Buffer1.bmp", tmp_path / "ref.bin"
+    dataset.write_bmp(path, pic)
+    run_paths(ref_cpu, "bmp", path, out)
+    raw = out.read_bytes()
+    nr, nc = np.frombuffer(raw[:8], np.int32)
+    assert (nr, nc) == jobs.bmp_size(path)
+    assert np.array_equal(np.frombuffer(raw[8:], np.uint8), jobs.read_bmp(path).ravel())
+
+
+@pytest.mark.parametrize("sx,sy,status", [(64, 64, 1), (37, 53, 0)])
+def test_phimap_writer_matches_reference(ref_cpu, tmp_path, sx, sy, status):
+    """outputImg (cTDM/HilbertTransform.cu:2437-2455) against ctdm_write_phimap: the same
+    bytes; ctdm_read_phimap reads the reference's file back exactly."""
+    from ctdm_gb300 import jobs
+    rng = np.random.default_rng(sx * sy)
+    ph = rng.standard_normal((sy, sx)).astype(np.float32)
+    am = rng.random((sy, sx)).astype(np.float32)
+    ax, ay = float(rng.standard_normal()), float(rng.standard_normal())
+    src, ref_file, mine = tmp_path / "in.bin", tmp_path / "ref.phimap", tmp_path / "mine.phimap"
+    with open(src, "wb") as f:
+        np.array([status, sx, sy], np.int32).tofile(f)
+        np.array([ax, ay], np.float64).tofile(f)
+        ph.tofile(f)
+        am.tofile(f)
+    run_paths(ref_cpu, "phimap", src, ref_file)
+    jobs.write_phimap(mine, status, ax, ay, ph, am)
+    assert ref_file.read_bytes() == mine.read_bytes()
+    back = jobs.read_phimap(ref_file)
+    assert back["status"] == bool(status) and back["angle_x"] == ax and back["angle_y"] == ay
+    assert np.array_equal(back["phase"], ph) and np.array_equal(back["amp"], am)
+
+
+def test_check_array_matches_reference(ref_cpu, lib, tmp_path):
+    """checkArray (cTDM/HilbertTransform.cu:3056-3092) against this library's drop-in with
+    the limits at the float nearest to each statistic and one float either side."""
+    import ctypes
+    rng = np.random.default_rng(11)
+    for seed in range(6):
+        n = int(rng.integers(16, 5000))
+        v = (rng.standard_normal(n) * rng.uniform(0.1, 3) + rng.uniform(-2, 2)).astype(np.float32)
+        s = np.float32(np.sqrt(np.mean((v.astype(np.float64) - v.astype(np.float64).mean()) ** 2)))
+        r = np.float32(abs(float(v.max()) - float(v.min())))
+        for ls in (s, np.nextafter(s, np.float32(np.inf)), np.nextafter(s, np.float32(-np.inf))):
+            for lr in (r, np.nextafter(r, np.float32(np.inf)), np.nextafter(r, np.float32(-np.inf)),
+                       np.float32(1e9)):
+                src = tmp_path / "chk.bin"
+                with open(src, "wb") as f:
+                    np.array([n], np.int32).tofile(f)
+                    np.array([ls, lr], np.float32).tofile(f)
+                    v.tofile(f)
+                run_paths(ref_cpu, "check", src, tmp_path / "chk.out")
+                ref = bool(np.fromfile(tmp_path / "chk.out", np.int32)[0])
+                mine = lib.checkArray(v.ctypes.data, ctypes.c_float(ls), ctypes.c_float(lr), n)
+                assert mine == ref, (seed, float(ls), float(lr))
