@@ -441,7 +441,8 @@ typedef struct {
 /* The reference's defaults (cTDM/HilbertTransform.cu:11-35). */
 CTDM_API void ctdm_job_defaults(ctdm_job_file *job);
 /* Parses one parameter file (fields in the reference's order; spaces after '=' are
- * allowed; values end at white space). */
+ * allowed; values end at white space, and a value containing '=' keeps its last
+ * '='-separated piece, as the reference's obtainParameter does). */
 CTDM_API ctdm_status ctdm_parse_job_file(const char *path, ctdm_job_file *job);
 /* Runs one job like HilbertTransform with SpeedTestFlag = 0 (the mode that writes maps
  * and reconstructs): all frames' QPI, unwrapping and resizing run batched on the GPU;
