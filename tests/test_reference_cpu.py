@@ -179,7 +179,7 @@ criteriaSTD=0.25
 
 def test_job_list_matches_reference(ref_cpu, tmp_path):
     """scriptFileRead (cTDM/HilbertTransform.cu:70-175) with obtainParameter, on a job
-    list of three parameter files, against ctdm_parse_job_file: the 20 fields in order,
+    list of four parameter files, against ctdm_parse_job_file: the 20 fields in order,
     including notes before the keys, integers read by atoi from decimals and trailing
     text, exponents, and a value with '=' in it (the reference keeps its last piece).
     The reference ignores the optional fields after the 20th.  No value here has a space
@@ -196,20 +196,25 @@ def test_job_list_matches_reference(ref_cpu, tmp_path):
                              iter_time=19, n_med=1.3371234567890123)
     p3 = tmp_path / "job3.txt"
     p3.write_text(JOB3.format(d=d))
+    # a trailing '=' and doubled '=' signs: the last non-empty piece is kept
+    p4 = tmp_path / "job4.txt"
+    p4.write_text(JOB3.format(d=d).replace("SaveDir={d}/out=run7".format(d=d), "SaveDir={d}/keep=".format(d=d))
+                  .replace("Mag=62.5", "Mag==62.5").replace("ReconSave=1", "ReconSave=2==="))
     lst = tmp_path / "JobList.txt"
-    lst.write_text(f"{p1}\n{p2}\n{p3}\n")
+    lst.write_text(f"{p1}\n{p2}\n{p3}\n{p4}\n")
     out = tmp_path / "jobs.json"
     run_paths(ref_cpu, "joblist", lst, out)
     import json
     ref = [json.loads(x) for x in out.read_text().splitlines()]
-    assert len(ref) == 3
+    assert len(ref) == 4
     keys = ["sp_dir", "bg_dir", "ang_dir", "save_dir", "row_pts", "col_pts", "recon_flag", "recon_save",
             "size_type", "resize_flag", "n_med", "mag", "camera_pixel_um", "wavelength_nm", "save_phase_stack",
             "save_amp_stack", "criteria_range", "criteria_std"]
-    for path, r in zip((p1, p2, p3), ref):
+    for path, r in zip((p1, p2, p3, p4), ref):
         mine = jobs.job_dict(jobs.parse_job_file(path))
         assert {k: mine[k] for k in keys} == {k: r[k] for k in keys}, path
     assert ref[2]["save_dir"] == "run7" and ref[2]["recon_flag"] == 2 and ref[2]["row_pts"] == [12, 1035]
+    assert ref[3]["save_dir"] == d + "/keep" and ref[3]["mag"] == 62.5 and ref[3]["recon_save"] == 2
 
 
 @pytest.mark.parametrize("h,w", [(8, 8), (30, 30), (64, 64), (8, 30)])
